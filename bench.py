@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark: spectral path samples/s of the GB300 sky tracer.
+
+Workload (default): the production-size plain render — a 512x256 equirect
+panorama, 81 wavelengths at 5 nm from 380 to 780 nm, 256 samples per
+pixel and wavelength, Russian roulette after order 8, no order cap, sun at 5
+degrees, 64 majorant layers over 0-100 km, tabulated phase sampling.  One
+"step" is one full render: 512*256*81*256 = 2,717,908,992 chains (a chain is
+one (pixel, wavelength, sample) path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value   chains/s with the scene resident on the device, CUDA events around the
+        render on the launching stream, L2 flushed between timed steps.
+e2e     the same metric through the one-shot C-ABI call
+        (sky_cuda_render_desc): host tables in, host film out, both copies
+        inside the timed region.
+Under torchrun each rank renders its own frame (a different sun elevation):
+weak scaling, no collective on the data path.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "sky-tracer_gb300"))
+DATA_DIR = ROOT / "tests" / "golden" / "data"
+
+# Frozen per-event FP32 work weights (FLOP, an FMA counted as 2), counted
+# from the reference shader's arithmetic for each event type.
+EVENT_FLOPS = {"track_step": 72, "segment": 48, "boundary": 40, "scatter": 200, "nee": 40, "ground": 150,
+               "chain": 46}
+
+WORKLOADS = {
+    "plain-512x256-81wl-256spp": dict(width=512, height=256, lam=(380.0, 780.0, 81), spp=256, sun=5.0,
+                                      rr_start_depth=8, max_orders=0),
+    "plain-64x32-32wl-64spp": dict(width=64, height=32, lam=(380.0, 780.0, 32), spp=64, sun=10.0,
+                                   rr_start_depth=0, max_orders=16),
+}
+DEFAULT_WORKLOAD = "plain-512x256-81wl-256spp"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
+    p.add_argument("--tracking", type=int, default=1, help="SkyTracking (1 = residual carry)")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_scene(w, rank: int):
+    from sky_cuda import synthetic_scene, wavelengths
+    lo, hi, n = w["lam"]
+    return synthetic_scene(wavelengths(lo, hi, n), DATA_DIR, sun_elevation_deg=w["sun"] + 0.5 * rank)
+
+
+def make_config(w, args, rank: int):
+    from sky_cuda import RenderConfig
+    from sky_cuda import _abi
+    return RenderConfig(width=w["width"], height=w["height"], spp=w["spp"], seed=0x5EC7_2026_0430 + rank,
+                        sun_elevation_deg=w["sun"], phase_sampling=_abi.PHASE_TABULATED,
+                        rr_start_depth=w["rr_start_depth"], max_orders=w["max_orders"], tracking=args.tracking,
+                        kernel=args.kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        power = [float(r[3]) for r in self.rows if len(r) > 3 and r[3].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows),
+                "power_w_max": max(power) if power else None}
+
+
+def measure_fp32_peak(torch, dev):
+    """FP32 FMA peak measured with cuBLAS SGEMM (TF32 off), best of 5, TFLOP/s."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device=dev, dtype=torch.float32)
+    b = torch.randn(n, n, device=dev, dtype=torch.float32)
+    c = torch.empty(n, n, device=dev, dtype=torch.float32)
+    for _ in range(2):
+        torch.matmul(a, b, out=c)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    return best
+
+
+def time_to_1pct(xyz, var, seconds_per_render):
+    """Time to 1 % per-pixel XYZ error: the 95th percentile over pixels of the
+    worst X/Y/Z relative standard error, pixels with Y < 1e-3 p99(Y)
+    excluded, scaled as 1/sqrt(samples)."""
+    y = xyz[:, 1]
+    keep = y >= 1e-3 * np.percentile(y, 99)
+    rel = np.sqrt(np.maximum(var[keep], 0)) / np.maximum(np.abs(xyz[keep]), 1e-30)
+    p95 = float(np.percentile(rel.max(axis=1), 95))
+    return p95, seconds_per_render * (p95 / 0.01) ** 2
+
+
+def cpu_baseline_run(w, args, budget_s):
+    """The oracle (C++ restatement of the reference shader) on all host cores,
+    on a bounded row sample of the same render; returns chains/s and the
+    sample description."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import sky_oracle
+    from sky_cuda import RenderConfig
+    sky_oracle.load()
+    scene = make_scene(w, 0)
+    cfg = make_config(w, args, 0)
+    threads = os.cpu_count() or 1
+    # pilot: one row at 1/8 of the samples to size the sample
+    pilot = RenderConfig(**{**cfg.__dict__, "spp": max(1, cfg.spp // 8)})
+    t0 = time.perf_counter()
+    sky_oracle.render(scene, pilot, row_begin=cfg.height // 2, row_step=cfg.height, threads=threads)
+    pilot_s = time.perf_counter() - t0
+    per_row_s = pilot_s * cfg.spp / pilot.spp
+    rows = int(max(1, min(cfg.height, budget_s / max(per_row_s, 1e-6))))
+    step = max(1, cfg.height // rows)
+    t0 = time.perf_counter()
+    sky_oracle.render(scene, cfg, row_begin=step // 2, row_step=step, threads=threads)
+    dt = time.perf_counter() - t0
+    n_rows = len(range(step // 2, cfg.height, step))
+    chains = n_rows * cfg.width * scene.band_count * cfg.spp
+    return chains / dt, threads, (f"every {step}th row ({n_rows} of {cfg.height} rows) at full spp: "
+                                  f"{chains} chains in {dt:.1f} s")
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    import platform
+    vals = []
+    for _ in range(max(1, args.warmup // 3)):
+        cpu_baseline_run(w, args, min(5.0, args.cpu_seconds))
+    sample = ""
+    threads = os.cpu_count() or 1
+    for _ in range(args.steps):
+        v, threads, sample = cpu_baseline_run(w, args, args.cpu_seconds)
+        vals.append(v)
+    value = statistics.median(vals)
+    cfgw = {"workload": args.workload, "width": w["width"], "height": w["height"], "wavelengths": w["lam"][2],
+            "spp": w["spp"], "l2": "compute-bound, tables < 1 MB"}
+    out = {"impl": "reference", "metric": "spectral path samples/s (chains/s)", "value": value,
+           "unit": "chains/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": cfgw,
+           "cpu_baseline": {"value": value, "unit": "chains/s", "cores": threads, "kind": "port",
+                            "sample": sample, "cpu": platform.processor() or platform.machine()},
+           "e2e": {"value": value, "unit": "chains/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "the reference tracer is WGSL run through wgpu, which needs a graphics API absent on "
+                   "this machine; this arm times the oracle, a C++ restatement of that shader"}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    from sky_cuda import GpuScene, render
+    from sky_cuda import _abi
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]
+    scene = make_scene(w, rank)
+    cfg = make_config(w, args, rank)
+    B = scene.band_count
+    cells = cfg.pixels * B
+    chains = cells * cfg.spp
+
+    gs = GpuScene(scene)
+    stream = torch.cuda.current_stream(dev)
+    s = torch.zeros(cells, dtype=torch.float64, device=dev)
+    q = torch.zeros(cells, dtype=torch.float64, device=dev)
+    film = torch.zeros(cells, dtype=torch.float32, device=dev)
+    xyz = torch.zeros(cfg.pixels * 3, dtype=torch.float64, device=dev)
+    xyz_var = torch.zeros(cfg.pixels * 3, dtype=torch.float64, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    counters = torch.zeros(8, dtype=torch.int64, device=dev)
+    outs = {"cell_sum": s.data_ptr(), "cell_sumsq": q.data_ptr(), "film": film.data_ptr(), "xyz": xyz.data_ptr(),
+            "xyz_var": xyz_var.data_ptr(), "status": status.data_ptr()}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    # warm-up; the first step also counts events (identical work: same seed)
+    for i in range(max(args.warmup, 1)):
+        o = dict(outs)
+        if i == 0:
+            o["counters"] = counters.data_ptr()
+        gs.render_device(cfg, o, stream.cuda_stream)
+    torch.cuda.synchronize()
+    if int(status.item()) != 0:
+        raise SystemExit("watchdog tripped during warm-up")
+    ev = {k: int(v) for k, v in zip(_abi.EVENT_NAMES, counters.cpu().tolist())}
+    flops_per_step = sum(EVENT_FLOPS[k] * ev[k] for k in EVENT_FLOPS)
+
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        gs.render_device(cfg, outs, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    torch.cuda.synchronize()
+    clocks.stop()
+    if world > 1:
+        dist.barrier()
+    total_s = sum(times)
+    if world > 1:
+        t = torch.tensor([total_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    step_s = total_s / args.steps
+    value = world * chains / step_s
+
+    # time to 1 % XYZ error from the last render
+    p95, t1pct = time_to_1pct(xyz.cpu().numpy().reshape(-1, 3), xyz_var.cpu().numpy().reshape(-1, 3), step_s)
+
+    # end to end through the one-shot C ABI: host tables in, host film out
+    desc_bytes = sum(a.nbytes for a in scene._keep) if scene._keep else 0
+    e2e_times = []
+    for i in range(args.e2e_steps + 1):
+        t0 = time.perf_counter()
+        render(scene, cfg)
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2e_times.append(dt)
+    desc_bytes = sum(a.nbytes for a in scene._keep)
+    e2e_s = statistics.median(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    peak = measure_fp32_peak(torch, dev) if rank == 0 else None
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_baseline_run(w, args, args.cpu_seconds)
+        import platform
+        cpu = {"value": v, "unit": "chains/s", "cores": cores, "kind": "port", "sample": sample,
+               "cpu": platform.machine()}
+    if rank == 0:
+        achieved = flops_per_step / step_s / 1e12
+        out = {
+            "metric": "spectral path samples/s (chains/s)", "value": value, "unit": "chains/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "width": cfg.width, "height": cfg.height, "wavelengths": B,
+                       "spp": cfg.spp, "chains_per_step": chains, "sun_elevation_deg": w["sun"],
+                       "tracking": "residual-carry" if cfg.tracking else "segment-restart",
+                       "phase_sampling": "tabulated", "kernel": cfg.kernel,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}"},
+            "e2e": {"value": world * chains / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(desc_bytes),
+                    "d2h_bytes_per_step": int(cells * 4 + 8 * 8 + 4)},
+            "time_to_1pct_xyz_s": t1pct, "p95_rel_se_at_spp": p95,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "peak_source": "measured: cuBLAS SGEMM 8192^3 with TF32 off (MEASURED_PEAKS.json "
+                                        "has no FP32 figure)",
+                         "flops_per_step": flops_per_step, "events_per_step": ev},
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": 2 * args.steps,
+        }
+        print(json.dumps(out))
+    gs.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

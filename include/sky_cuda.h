@@ -1,0 +1,280 @@
+/*
+ * sky_cuda.h — C ABI of the GB300 spectral sky path tracer.
+ *
+ * This is the drop-in boundary for the hot path of the reference's
+ * `sky-spectral-path-tracer` crate: every entry point takes plain pointers and
+ * sizes, and every table row below has the byte layout the reference uploads
+ * to its compute shader, so a host that already packs those rows
+ * (crates/sky-spectral-path-tracer/src/integrator.rs:319-418) can hand them to
+ * this library unchanged.
+ *
+ * Conventions
+ *   - Every function returns an `int` status (SkyStatus); 0 is success.  The
+ *     message of the last failure on the calling thread is available through
+ *     sky_cuda_last_error().
+ *   - The caller owns every host buffer.  The library owns the device memory
+ *     behind an opaque SkyScene and frees it in sky_cuda_scene_destroy().
+ *   - Calls are thread-compatible per scene: one scene is used by one thread
+ *     at a time; different scenes may be used from different threads.
+ */
+#ifndef SKY_CUDA_H
+#define SKY_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKY_CUDA_ABI_VERSION 1u
+/* Aerosol species per band: inso, waso, soot, suso
+ * (crates/sky-core/src/atmosphere.rs:6-8). */
+#define SKY_SPECIES_COUNT 4u
+
+/* Status codes.  Codes 1-6 correspond one-to-one to the reference's
+ * `RenderError` variants (integrator.rs:18-26). */
+typedef enum SkyStatus {
+    SKY_OK = 0,
+    SKY_ERR_INVALID_CONFIG = 1, /* RenderError::InvalidConfig */
+    SKY_ERR_NO_DEVICE = 2,      /* RenderError::NoAdapter     */
+    SKY_ERR_DEVICE_INIT = 3,    /* RenderError::RequestDevice */
+    SKY_ERR_COPY = 4,           /* RenderError::BufferMap     */
+    SKY_ERR_SYNC = 5,           /* RenderError::Poll          */
+    SKY_ERR_WATCHDOG = 6,       /* RenderError::Watchdog      */
+    SKY_ERR_OUT_OF_MEMORY = 7,
+    SKY_ERR_LAUNCH = 8,
+    SKY_ERR_IO = 9              /* host-side table loading      */
+} SkyStatus;
+
+/* ---- Table rows (layouts of integrator.rs:77-112) ---------------------- */
+
+/* = GpuBand (integrator.rs:79-86), 24 bytes. */
+typedef struct SkyBand {
+    float center_nm;
+    float lower_nm;
+    float upper_nm;
+    float ozone_cross_section_cm2;
+    float solar_radiance_w_m2_sr;
+    float rayleigh_cross_section_m2;
+} SkyBand;
+
+/* = GpuAtmospherePoint (integrator.rs:90-95), 16 bytes. */
+typedef struct SkyAtmospherePoint {
+    float altitude_km;
+    float temperature_k;
+    float air_cm3;
+    float ozone_cm3;
+} SkyAtmospherePoint;
+
+/* = GpuAerosolPoint (integrator.rs:99-105), 32 bytes. */
+typedef struct SkyAerosolPoint {
+    float altitude_km;
+    float mass_g_m3[SKY_SPECIES_COUNT];
+    float _pad[3];
+} SkyAerosolPoint;
+
+/* = GpuAerosolOptics (integrator.rs:109-112), 8 bytes. */
+typedef struct SkyAerosolOptics {
+    float scattering_km_inv_per_g_m3;
+    float absorption_km_inv_per_g_m3;
+} SkyAerosolOptics;
+
+/* ---- Scene ------------------------------------------------------------- */
+
+/*
+ * Everything the reference's `SceneData` contributes to the shader
+ * (atmosphere.rs:121-133, packed at integrator.rs:321-416).  Band count and
+ * phase-bin count are run-time fields here, not the reference's compile-time
+ * 41 and 1024.
+ */
+typedef struct SkySceneDesc {
+    uint32_t band_count;
+    uint32_t atmosphere_len;      /* rows in `atmosphere`, ascending altitude */
+    uint32_t aerosol_len;         /* rows in `aerosol`, ascending altitude    */
+    uint32_t majorant_layers;     /* MajorantGrid::layer_count                */
+    uint32_t phase_bins;          /* bins per (species, band) phase table     */
+    uint32_t _reserved0;
+    float ground_radius_km;       /* Planet (geometry.rs:12-17)               */
+    float atmosphere_radius_km;
+    float top_altitude_km;        /* MajorantGrid::top_altitude_km            */
+    float sun_direction[3];       /* Sun (atmosphere.rs:12-37)                */
+    float sun_angular_radius_rad;
+    float sun_solid_angle_sr;
+    float ground_albedo;          /* GROUND_ALBEDO, 0.18 in atmosphere.rs:9   */
+    float _reserved1;
+    const SkyBand* bands;                    /* [band_count]                   */
+    const SkyAtmospherePoint* atmosphere;    /* [atmosphere_len]               */
+    const SkyAerosolPoint* aerosol;          /* [aerosol_len]                  */
+    const SkyAerosolOptics* aerosol_optics;  /* [band_count][SPECIES]          */
+    const float* majorants_km_inv;           /* [band_count][majorant_layers]  */
+    const float* phase_values;               /* [SPECIES][band_count][bins], cube-root mu grid */
+    const float* band_xyz_weights;           /* [band_count][3] CIE 1931 at band centre; may be NULL */
+} SkySceneDesc;
+
+typedef struct SkyScene SkyScene;
+
+/* ---- Render configuration ---------------------------------------------- */
+
+typedef enum SkyProjection {
+    SKY_PROJECTION_PANORAMA = 0,     /* OutputProjection::Panorama   */
+    SKY_PROJECTION_SKY_VIEW_LUT = 1  /* OutputProjection::SkyViewLut */
+} SkyProjection;
+
+typedef enum SkyPhaseSampling {
+    /* The reference shader: isotropic direction, weighted by the mixed phase
+     * (sky_trace.wgsl:735-738). */
+    SKY_PHASE_ISOTROPIC = 0,
+    /* Pick a component by sigma_s,i / sigma_s and invert its tabulated CDF
+     * (phase.rs:53-69, sampling.rs:182-185). */
+    SKY_PHASE_TABULATED = 1
+} SkyPhaseSampling;
+
+typedef enum SkyTracking {
+    /* The reference's layered delta tracking: every majorant segment starts a
+     * fresh exponential flight and the draw that overshoots the segment is
+     * discarded (sky_trace.wgsl:405-475).  Reproduces its random stream. */
+    SKY_TRACKING_SEGMENT_RESTART = 0,
+    /* Same collision distribution, one exponential draw per tentative
+     * collision: the residual optical depth is carried across segment
+     * boundaries instead of being re-drawn. */
+    SKY_TRACKING_RESIDUAL_CARRY = 1
+} SkyTracking;
+
+typedef enum SkyKernel {
+    SKY_KERNEL_AUTO = 0,       /* the persistent regenerating kernel */
+    SKY_KERNEL_PLAIN = 1,      /* one thread per chain, one launch   */
+    SKY_KERNEL_WAVEFRONT = 2   /* persistent, per-lane regeneration  */
+} SkyKernel;
+
+/* Add into the sums already held by the outputs instead of overwriting them
+ * (progressive rendering; the reference accumulates 2-spp dispatches the
+ * same way, integrator.rs:252-283). */
+#define SKY_FLAG_ACCUMULATE 1u
+
+/*
+ * = RenderConfig (config.rs:2-12) followed by extensions.  A config whose
+ * extension fields are all zero renders exactly what the reference shader
+ * renders.
+ */
+typedef struct SkyRenderConfig {
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t direct_light_samples;  /* 0 is treated as 1 (integrator.rs:325) */
+    uint64_t seed;
+    float sun_elevation_deg;        /* recorded only; the sun is in the scene */
+    float sun_azimuth_deg;
+    float observer_altitude_km;
+    uint32_t output_projection;     /* SkyProjection */
+    /* extensions */
+    uint32_t sample_offset;         /* index of the first sample (resume)      */
+    uint32_t phase_sampling;        /* SkyPhaseSampling                        */
+    uint32_t rr_start_depth;        /* 0 -> 4 (sky_trace.wgsl:692)            */
+    uint32_t max_orders;            /* 0 -> unbounded; else paths end after this many events */
+    uint32_t watchdog_limit;        /* 0 -> 1024 (integrator.rs:14)           */
+    uint32_t kernel;                /* SkyKernel                               */
+    uint32_t flags;                 /* SKY_FLAG_*                              */
+    uint32_t tracking;              /* SkyTracking                             */
+    uint32_t _reserved[2];
+} SkyRenderConfig;
+
+/* Event counters, indexed by these values (the per-event work weights of
+ * the roofline are defined over them). */
+typedef enum SkyEvent {
+    SKY_EVENT_TRACK_STEP = 0,  /* free-flight sample inside a segment + accept test */
+    SKY_EVENT_SEGMENT = 1,     /* majorant-layer segment set-up                   */
+    SKY_EVENT_BOUNDARY = 2,    /* ground / top-of-atmosphere intersection          */
+    SKY_EVENT_SCATTER = 3,     /* real scattering event                            */
+    SKY_EVENT_NEE = 4,         /* sun-cone light sample                            */
+    SKY_EVENT_GROUND = 5,      /* ground hit                                       */
+    SKY_EVENT_CHAIN = 6,       /* camera ray start + accumulation                  */
+    SKY_EVENT_COUNT = 8
+} SkyEvent;
+
+typedef struct SkyRenderStats {
+    double kernel_ms;       /* device time of the tracing kernel(s), CUDA events */
+    double total_ms;        /* host wall time of the call                         */
+    uint64_t chains;        /* pixel x band x sample paths traced                 */
+    uint64_t events[SKY_EVENT_COUNT];
+    uint32_t watchdog;      /* nonzero when a path reached the watchdog           */
+    uint32_t kernel_used;   /* SkyKernel actually launched                         */
+} SkyRenderStats;
+
+/*
+ * Device-resident outputs of sky_cuda_render_device().  All pointers are
+ * device pointers; every one except `cell_sum` may be NULL.
+ *   cell_sum   [pixels][bands]  sum of path radiance over the samples (FP64)
+ *   cell_sumsq [pixels][bands]  sum of squared path radiance (FP64)
+ *   film       [pixels][bands]  mean radiance, clamped >= 0 (the reference Film)
+ *   xyz        [pixels][3]      CIE XYZ of the mean spectrum (FP64)
+ *   xyz_var    [pixels][3]      variance of that XYZ estimate (FP64)
+ *   counters   [SKY_EVENT_COUNT] event counts, added to (not overwritten)
+ *   status     [1]              nonzero after a watchdog; left for the caller
+ */
+typedef struct SkyDeviceOutputs {
+    double* cell_sum;
+    double* cell_sumsq;
+    float* film;
+    double* xyz;
+    double* xyz_var;
+    unsigned long long* counters;
+    uint32_t* status;
+} SkyDeviceOutputs;
+
+/* ---- Entry points ------------------------------------------------------ */
+
+/* Library version string, e.g. "sky_cuda 0.1.0 (abi 1, sm_103a)". */
+const char* sky_cuda_version(void);
+
+/* Copy the last error message of the calling thread into `buf` (always NUL
+ * terminated); returns the status that produced it. */
+int sky_cuda_last_error(char* buf, size_t buf_len);
+
+/* Validate a scene (integrator.rs:130-163, :401-407) and upload its tables to
+ * the current CUDA device.  Replaces the buffer creation of
+ * integrator.rs:192-216. */
+int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene);
+
+void sky_cuda_scene_destroy(SkyScene* scene);
+
+/*
+ * Render the spectral film into host memory: `film_out` receives
+ * width*height*band_count floats, pixel-major and band-minor, divided by the
+ * sample count and clamped at zero, exactly like the `Film` returned by
+ * `render` (integrator.rs:125-128, :306-316).  Synchronous.
+ */
+int sky_cuda_render(const SkyScene* scene, const SkyRenderConfig* config,
+                    float* film_out, size_t film_len, SkyRenderStats* stats);
+
+/*
+ * Like sky_cuda_render, and also returns per-pixel CIE XYZ (FP64, [pixels][3])
+ * and its variance.  `film_out` may be NULL.  Requires band_xyz_weights in
+ * the scene.
+ */
+int sky_cuda_render_xyz(const SkyScene* scene, const SkyRenderConfig* config,
+                        float* film_out, size_t film_len,
+                        double* xyz_out, double* xyz_var_out, size_t pixel_count,
+                        SkyRenderStats* stats);
+
+/*
+ * One-shot form of `render(&SceneData, &RenderConfig)`: uploads the scene,
+ * renders, copies the film back and frees the device tables, all inside the
+ * call (integrator.rs:125-317).
+ */
+int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config,
+                         float* film_out, size_t film_len, SkyRenderStats* stats);
+
+/*
+ * Asynchronous render into device buffers on `cuda_stream` (a cudaStream_t,
+ * NULL for the legacy default stream).  Returns after the launches are
+ * queued; the watchdog word is left in `outputs->status`.
+ */
+int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
+                           const SkyDeviceOutputs* outputs, void* cuda_stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKY_CUDA_H */

@@ -1,0 +1,374 @@
+// sky_cuda_api.cu — the C ABI declared in include/sky_cuda.h.
+//
+// Mirrors the reference integrator's host flow (integrator.rs:125-317):
+// validate, pack tables into device memory, dispatch the tracer, read back,
+// divide by the sample count and clamp at zero, and map failures to the
+// RenderError kinds.  Device tables live in one allocation per scene; the
+// per-render workspace is kept on the scene and grown on demand.
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/sky_cuda.h"
+#include "scene_build.h"
+#include "trace_kernels.h"
+
+using namespace sky;
+
+struct SkyScene {
+    int device = 0;
+    DevScene dev{};
+    void* blob = nullptr;
+    bool has_xyz = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    // workspace
+    double* ws_sum = nullptr;
+    double* ws_sumsq = nullptr;
+    float* ws_film = nullptr;
+    double* ws_xyz = nullptr;
+    double* ws_xyz_var = nullptr;
+    unsigned long long* ws_counters = nullptr;
+    uint32_t* ws_status = nullptr;
+    uint64_t ws_cells = 0, ws_pixels = 0;
+};
+
+namespace {
+
+thread_local std::string g_error;
+thread_local int g_error_status = SKY_OK;
+
+int set_error(int status, const std::string& msg) {
+    g_error = msg;
+    g_error_status = status;
+    return status;
+}
+
+int cuda_fail(int status, const char* what, cudaError_t e) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) status = SKY_ERR_OUT_OF_MEMORY;
+    return set_error(status, msg);
+}
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+void free_workspace(SkyScene* s) {
+    cudaFree(s->ws_sum);
+    cudaFree(s->ws_sumsq);
+    cudaFree(s->ws_film);
+    cudaFree(s->ws_xyz);
+    cudaFree(s->ws_xyz_var);
+    cudaFree(s->ws_counters);
+    cudaFree(s->ws_status);
+    s->ws_sum = s->ws_sumsq = nullptr;
+    s->ws_film = nullptr;
+    s->ws_xyz = s->ws_xyz_var = nullptr;
+    s->ws_counters = nullptr;
+    s->ws_status = nullptr;
+    s->ws_cells = s->ws_pixels = 0;
+}
+
+int ensure_workspace(SkyScene* s, uint64_t pixels) {
+    uint64_t cells = pixels * s->dev.band_count;
+    if (cells <= s->ws_cells && pixels <= s->ws_pixels && s->ws_sum) return SKY_OK;
+    free_workspace(s);
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&s->ws_sum, cells * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_sumsq, cells * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_film, cells * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_xyz, pixels * 3 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_xyz_var, pixels * 3 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_counters, SKY_EVENT_COUNT * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_status, sizeof(uint32_t))) != cudaSuccess) {
+        free_workspace(s);
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "workspace allocation", e);
+    }
+    s->ws_cells = cells;
+    s->ws_pixels = pixels;
+    return SKY_OK;
+}
+
+// validate_config (integrator.rs:130-163) with run-time band count.
+int validate_config(const SkyScene* scene, const SkyRenderConfig* c) {
+    if (!scene) return set_error(SKY_ERR_INVALID_CONFIG, "scene is null");
+    if (!c) return set_error(SKY_ERR_INVALID_CONFIG, "render config is null");
+    if (c->width == 0 || c->height == 0 || c->spp == 0)
+        return set_error(SKY_ERR_INVALID_CONFIG, "width, height, and spp must be greater than zero");
+    uint64_t cells = uint64_t(c->width) * c->height * scene->dev.band_count;
+    if (cells > 0xffffffffull)
+        return set_error(SKY_ERR_INVALID_CONFIG, "film is too large for the GPU shader index type");
+    if (uint64_t(c->sample_offset) + c->spp > 0xffffffffull)
+        return set_error(SKY_ERR_INVALID_CONFIG, "sample indices overflow 32 bits");
+    if (c->output_projection > SKY_PROJECTION_SKY_VIEW_LUT)
+        return set_error(SKY_ERR_INVALID_CONFIG, "unknown output projection");
+    if (c->phase_sampling > SKY_PHASE_TABULATED)
+        return set_error(SKY_ERR_INVALID_CONFIG, "unknown phase sampling mode");
+    if (c->tracking > SKY_TRACKING_RESIDUAL_CARRY)
+        return set_error(SKY_ERR_INVALID_CONFIG, "unknown tracking mode");
+    if (c->kernel > SKY_KERNEL_WAVEFRONT) return set_error(SKY_ERR_INVALID_CONFIG, "unknown kernel");
+    if (!std::isfinite(c->observer_altitude_km))
+        return set_error(SKY_ERR_INVALID_CONFIG, "observer altitude must be finite");
+    if (c->observer_altitude_km >= scene->dev.atmosphere_radius - scene->dev.ground_radius)
+        return set_error(SKY_ERR_INVALID_CONFIG, "observer must be inside the atmosphere");
+    return SKY_OK;
+}
+
+// Per-launch constants, including the sky-view LUT frame of
+// sky_trace.wgsl:632-681 evaluated once on the host.
+DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
+    DevLaunch L{};
+    L.width = c->width;
+    L.height = c->height;
+    L.spp = c->spp;
+    L.sample_offset = c->sample_offset;
+    L.band_count = s->dev.band_count;
+    L.direct_light_samples = c->direct_light_samples ? c->direct_light_samples : 1u;
+    L.projection = c->output_projection;
+    L.phase_sampling = c->phase_sampling;
+    L.rr_start_depth = c->rr_start_depth ? c->rr_start_depth : kDefaultRrDepth;
+    L.max_orders = c->max_orders;
+    L.watchdog_limit = c->watchdog_limit ? c->watchdog_limit : kDefaultWatchdog;
+    L.tracking = c->tracking;
+    L.seed_lo = uint32_t(c->seed);
+    L.seed_hi = uint32_t(c->seed >> 32);
+    L.observer_altitude = c->observer_altitude_km;
+    L.inv_width = 1.0f / float(c->width);
+    L.inv_height = 1.0f / float(c->height);
+    const float rg = s->dev.ground_radius;
+    const float oy = rg + std::max(c->observer_altitude_km, 0.0f);
+    const float view_height = std::sqrt(0.0f * 0.0f + oy * oy + 0.0f * 0.0f);
+    const float v_horizon = std::sqrt(std::max(view_height * view_height - rg * rg, 0.0f));
+    const float cos_beta = std::min(std::max(v_horizon / std::max(view_height, 0.000001f), 0.0f), 1.0f);
+    const float beta = std::acos(cos_beta);
+    L.lut_beta = beta;
+    L.lut_zenith_horizon_angle = 3.14159265358979323846f - beta;
+    const float* sun = s->dev.sun;
+    float sh[3] = {sun[0], sun[1] - sun[1], sun[2]};
+    float sh_len = std::sqrt(sh[0] * sh[0] + sh[1] * sh[1] + sh[2] * sh[2]);
+    float f[3] = {1.0f, 0.0f, 0.0f};
+    if (sh_len > 0.00001f)
+        for (int i = 0; i < 3; ++i) f[i] = sh[i] / std::max(sh_len, 0.00001f);
+    // side = normalize(cross(up, forward))
+    float side[3] = {f[2], 0.0f, -f[0]};
+    float sl = std::sqrt(side[0] * side[0] + side[1] * side[1] + side[2] * side[2]);
+    for (int i = 0; i < 3; ++i) {
+        L.lut_forward[i] = f[i];
+        L.lut_side[i] = side[i] / sl;
+    }
+    return L;
+}
+
+int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs* o, cudaStream_t stream,
+                  bool timed) {
+    DevLaunch L = make_launch(s, c);
+    const uint64_t pixels = uint64_t(c->width) * c->height;
+    const uint64_t cells = pixels * s->dev.band_count;
+    (void)cells;
+    cudaError_t e;
+    const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
+    if (timed) cudaEventRecord(s->ev_start, stream);
+    e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "tracing kernel launch", e);
+    if (timed) cudaEventRecord(s->ev_stop, stream);
+    const uint32_t total_spp = (c->flags & SKY_FLAG_ACCUMULATE) ? c->sample_offset + c->spp : c->spp;
+    double* xyz = s->has_xyz ? o->xyz : nullptr;
+    double* xyz_var = s->has_xyz ? o->xyz_var : nullptr;
+    e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
+    return SKY_OK;
+}
+
+// Synchronous render into the scene workspace, with host copies.
+int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t film_len, double* xyz_out,
+                double* xyz_var_out, size_t pixel_count, SkyRenderStats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    int st = validate_config(s, c);
+    if (st) return st;
+    const uint64_t pixels = uint64_t(c->width) * c->height;
+    const uint64_t cells = pixels * s->dev.band_count;
+    if (film_out && film_len < cells)
+        return set_error(SKY_ERR_INVALID_CONFIG, "film buffer is smaller than width*height*bands");
+    if ((xyz_out || xyz_var_out) && pixel_count < pixels)
+        return set_error(SKY_ERR_INVALID_CONFIG, "xyz buffer is smaller than width*height");
+    if ((xyz_out || xyz_var_out) && !s->has_xyz)
+        return set_error(SKY_ERR_INVALID_CONFIG, "scene has no band_xyz_weights");
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    if ((st = ensure_workspace(s, pixels))) return st;
+    cudaError_t e;
+    e = cudaMemsetAsync(s->ws_counters, 0, SKY_EVENT_COUNT * sizeof(unsigned long long), s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->ws_status, 0, sizeof(uint32_t), s->stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "clearing counters", e);
+    SkyDeviceOutputs o{s->ws_sum, s->ws_sumsq, film_out ? s->ws_film : nullptr, xyz_out ? s->ws_xyz : nullptr,
+                       xyz_var_out ? s->ws_xyz_var : nullptr, s->ws_counters, s->ws_status};
+    if ((st = launch_render(s, c, &o, s->stream, true))) return st;
+    uint32_t status = 0;
+    unsigned long long counters[SKY_EVENT_COUNT] = {};
+    if (film_out &&
+        (e = cudaMemcpyAsync(film_out, s->ws_film, cells * sizeof(float), cudaMemcpyDeviceToHost, s->stream)))
+        return cuda_fail(SKY_ERR_COPY, "film readback", e);
+    if (xyz_out &&
+        (e = cudaMemcpyAsync(xyz_out, s->ws_xyz, pixels * 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream)))
+        return cuda_fail(SKY_ERR_COPY, "xyz readback", e);
+    if (xyz_var_out && (e = cudaMemcpyAsync(xyz_var_out, s->ws_xyz_var, pixels * 3 * sizeof(double),
+                                            cudaMemcpyDeviceToHost, s->stream)))
+        return cuda_fail(SKY_ERR_COPY, "xyz variance readback", e);
+    if ((e = cudaMemcpyAsync(counters, s->ws_counters, sizeof(counters), cudaMemcpyDeviceToHost, s->stream)) ||
+        (e = cudaMemcpyAsync(&status, s->ws_status, sizeof(status), cudaMemcpyDeviceToHost, s->stream)))
+        return cuda_fail(SKY_ERR_COPY, "diagnostics readback", e);
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) return cuda_fail(SKY_ERR_SYNC, "waiting for the GPU", e);
+    if (stats) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, s->ev_start, s->ev_stop);
+        stats->kernel_ms = ms;
+        stats->chains = uint64_t(cells) * c->spp;
+        for (int i = 0; i < SKY_EVENT_COUNT; ++i) stats->events[i] = counters[i];
+        stats->watchdog = status;
+        stats->kernel_used = SKY_KERNEL_PLAIN;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (status) return set_error(SKY_ERR_WATCHDOG, "GPU path watchdog was reached");
+    return SKY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sky_cuda_version(void) { return "sky_cuda 0.1.0 (abi 1, sm_103a)"; }
+
+int sky_cuda_last_error(char* buf, size_t buf_len) {
+    if (buf && buf_len) {
+        std::snprintf(buf, buf_len, "%s", g_error.c_str());
+    }
+    return g_error_status;
+}
+
+int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
+    if (!out_scene) return set_error(SKY_ERR_INVALID_CONFIG, "out_scene is null");
+    *out_scene = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return set_error(SKY_ERR_NO_DEVICE, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+    HostTables h;
+    std::string err;
+    int st = build_host_tables(desc, h, err);
+    if (st) return set_error(st, err);
+
+    SkyScene* s = new SkyScene();
+    cudaGetDevice(&s->device);
+    const size_t A = 256;
+    size_t off = 0;
+    auto reserve = [&](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes, A);
+        return at;
+    };
+    size_t o_knot = reserve(h.knot_z.size() * sizeof(float));
+    size_t o_finder = reserve(h.finder.size() * sizeof(uint16_t));
+    size_t o_sig = reserve(h.sigma_t.size() * sizeof(float2));
+    size_t o_maj = reserve(h.majorants.size() * sizeof(float));
+    size_t o_band = reserve(h.bands.size() * sizeof(DevBand));
+    size_t o_prof = reserve(h.profile.size() * sizeof(DevProfileKnot));
+    size_t o_opt = reserve(h.optics.size() * sizeof(SkyAerosolOptics));
+    size_t o_pv = reserve(h.phase_values.size() * sizeof(float));
+    size_t o_pc = reserve(h.phase_cdf.size() * sizeof(float));
+    size_t o_pp = reserve(h.phase_bin_pdf.size() * sizeof(float));
+    std::vector<unsigned char> host(off, 0);
+    auto put = [&](size_t at, const void* src, size_t bytes) { std::memcpy(host.data() + at, src, bytes); };
+    put(o_knot, h.knot_z.data(), h.knot_z.size() * sizeof(float));
+    put(o_finder, h.finder.data(), h.finder.size() * sizeof(uint16_t));
+    put(o_sig, h.sigma_t.data(), h.sigma_t.size() * sizeof(float2));
+    put(o_maj, h.majorants.data(), h.majorants.size() * sizeof(float));
+    put(o_band, h.bands.data(), h.bands.size() * sizeof(DevBand));
+    put(o_prof, h.profile.data(), h.profile.size() * sizeof(DevProfileKnot));
+    put(o_opt, h.optics.data(), h.optics.size() * sizeof(SkyAerosolOptics));
+    put(o_pv, h.phase_values.data(), h.phase_values.size() * sizeof(float));
+    put(o_pc, h.phase_cdf.data(), h.phase_cdf.size() * sizeof(float));
+    put(o_pp, h.phase_bin_pdf.data(), h.phase_bin_pdf.size() * sizeof(float));
+    if ((e = cudaMalloc(&s->blob, off)) != cudaSuccess) {
+        delete s;
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "scene table allocation", e);
+    }
+    if ((e = cudaMemcpy(s->blob, host.data(), off, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cudaFree(s->blob);
+        delete s;
+        return cuda_fail(SKY_ERR_COPY, "scene table upload", e);
+    }
+    unsigned char* base = static_cast<unsigned char*>(s->blob);
+    s->dev = h.scene;
+    s->dev.knot_z = reinterpret_cast<const float*>(base + o_knot);
+    s->dev.finder = reinterpret_cast<const uint16_t*>(base + o_finder);
+    s->dev.sigma_t = reinterpret_cast<const float2*>(base + o_sig);
+    s->dev.majorants = reinterpret_cast<const float*>(base + o_maj);
+    s->dev.bands = reinterpret_cast<const DevBand*>(base + o_band);
+    s->dev.profile = reinterpret_cast<const DevProfileKnot*>(base + o_prof);
+    s->dev.optics = reinterpret_cast<const SkyAerosolOptics*>(base + o_opt);
+    s->dev.phase_values = reinterpret_cast<const float*>(base + o_pv);
+    s->dev.phase_cdf = reinterpret_cast<const float*>(base + o_pc);
+    s->dev.phase_bin_pdf = reinterpret_cast<const float*>(base + o_pp);
+    s->has_xyz = h.has_xyz;
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&s->ev_start)) != cudaSuccess || (e = cudaEventCreate(&s->ev_stop)) != cudaSuccess) {
+        sky_cuda_scene_destroy(s);
+        return cuda_fail(SKY_ERR_DEVICE_INIT, "stream creation", e);
+    }
+    *out_scene = s;
+    return SKY_OK;
+}
+
+void sky_cuda_scene_destroy(SkyScene* s) {
+    if (!s) return;
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_workspace(s);
+    cudaFree(s->blob);
+    if (s->ev_start) cudaEventDestroy(s->ev_start);
+    if (s->ev_stop) cudaEventDestroy(s->ev_stop);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int sky_cuda_render(const SkyScene* scene, const SkyRenderConfig* config, float* film_out, size_t film_len,
+                    SkyRenderStats* stats) {
+    if (!film_out) return set_error(SKY_ERR_INVALID_CONFIG, "film_out is null");
+    return render_host(const_cast<SkyScene*>(scene), config, film_out, film_len, nullptr, nullptr, 0, stats);
+}
+
+int sky_cuda_render_xyz(const SkyScene* scene, const SkyRenderConfig* config, float* film_out, size_t film_len,
+                        double* xyz_out, double* xyz_var_out, size_t pixel_count, SkyRenderStats* stats) {
+    if (!xyz_out) return set_error(SKY_ERR_INVALID_CONFIG, "xyz_out is null");
+    return render_host(const_cast<SkyScene*>(scene), config, film_out, film_len, xyz_out, xyz_var_out, pixel_count,
+                       stats);
+}
+
+int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config, float* film_out, size_t film_len,
+                         SkyRenderStats* stats) {
+    SkyScene* s = nullptr;
+    int st = sky_cuda_scene_create(desc, &s);
+    if (st) return st;
+    st = sky_cuda_render(s, config, film_out, film_len, stats);
+    std::string keep = g_error;
+    int keep_status = g_error_status;
+    sky_cuda_scene_destroy(s);
+    g_error = keep;
+    g_error_status = keep_status;
+    return st;
+}
+
+int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config, const SkyDeviceOutputs* outputs,
+                           void* cuda_stream) {
+    int st = validate_config(scene, config);
+    if (st) return st;
+    if (!outputs || !outputs->cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
+    if (!outputs->status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.status is required");
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    return launch_render(s, config, outputs, static_cast<cudaStream_t>(cuda_stream), false);
+}
+
+}  // extern "C"

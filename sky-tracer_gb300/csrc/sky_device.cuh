@@ -1,0 +1,467 @@
+// sky_device.cuh — device building blocks shared by the tracing kernels.
+//
+// Each function follows the reference shader's semantics (the WGSL line
+// ranges are cited) but is laid out for the GPU:
+//   * the pcg4d counter RNG is bit-exact with sky_trace.wgsl:156-189; the
+//     three chain-constant lanes of the counter are hashed once per chain;
+//   * a ray is described by its impact parameter p = |o x d| and b = o.d, so
+//     the shell quadratic  t = -b +- sqrt(R^2 - p^2)  is evaluated as
+//     sqrt((R - p)(R + p)) without the cancellation of b^2 - c at Earth
+//     radius, one square root per shell instead of the two full sphere
+//     intersections of sky_trace.wgsl:211-221;
+//   * the medium is read from the union-knot tables of sky_scene.h (one
+//     lookup + one FMA instead of two linear profile scans).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sky_scene.h"
+
+namespace sky {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kInvPi = 0.31830988618379067154f;
+constexpr float kTau = 6.28318530717958647692f;
+constexpr float kIsotropicPdf = 0.07957747154594766788f;
+constexpr float kRayleighNorm = 3.0f / (16.0f * kPi);
+constexpr float kF32Epsilon = 1.1920929e-7f;
+
+// ---- counters ---------------------------------------------------------------
+
+struct Counters {
+    uint32_t e[SKY_EVENT_COUNT];
+    __device__ __forceinline__ void clear() {
+#pragma unroll
+        for (int i = 0; i < SKY_EVENT_COUNT; ++i) e[i] = 0;
+    }
+};
+
+// ---- RNG: pcg4d counter hash (sky_trace.wgsl:156-189) -----------------------
+
+struct Rng {
+    uint32_t k0, k1, k2;  // first LCG step of (pixel^seed_lo, sample^seed_hi, band)
+    uint32_t dim;
+
+    __device__ __forceinline__ void init(uint32_t pixel, uint32_t sample, uint32_t band, uint32_t seed_lo,
+                                         uint32_t seed_hi) {
+        k0 = (pixel ^ seed_lo) * 1664525u + 1013904223u;
+        k1 = (sample ^ seed_hi) * 1664525u + 1013904223u;
+        k2 = band * 1664525u + 1013904223u;
+        dim = 0u;
+    }
+    __device__ __forceinline__ uint32_t next_u32() {
+        uint32_t x = k0, y = k1, z = k2, w = dim * 1664525u + 1013904223u;
+        dim += 1u;
+        x += y * w;
+        y += z * x;
+        z += x * y;
+        w += y * z;
+        x ^= x >> 16;
+        y ^= y >> 16;
+        z ^= z >> 16;
+        w ^= w >> 16;
+        x += y * w;
+        y += z * x;
+        z += x * y;
+        w += y * z;
+        return x ^ y ^ z ^ w;
+    }
+    // rng_f32: 24 high bits scaled by 2^-24 (exact conversion).
+    __device__ __forceinline__ float next() {
+        return __uint2float_rz(next_u32() >> 8) * 0.000000059604644775390625f;
+    }
+};
+
+// ---- small vector helpers -----------------------------------------------------
+
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 mk(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 add(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 scale(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 madd(V3 a, V3 b, float s) {  // a + b*s
+    return mk(fmaf(b.x, s, a.x), fmaf(b.y, s, a.y), fmaf(b.z, s, a.z));
+}
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ V3 cross3(V3 a, V3 b) {
+    return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+// normalize_or_y (sky_trace.wgsl:191-197)
+__device__ __forceinline__ V3 normalize_or_y(V3 v) {
+    float l2 = dot3(v, v);
+    if (l2 > 0.0f) return scale(v, rsqrtf(l2));
+    return mk(0.0f, 1.0f, 0.0f);
+}
+__device__ __forceinline__ V3 load3(const float* p) { return mk(p[0], p[1], p[2]); }
+
+// ---- ray geometry -----------------------------------------------------------------
+
+// Invariants of a ray o + t d (|d| = 1) with respect to the planet centre.
+struct RayGeo {
+    float b;     // o . d      (t = s - b, s measured from the closest approach)
+    float p;     // impact parameter |o x d|
+    float r0sq;  // |o|^2
+};
+
+__device__ __forceinline__ RayGeo ray_geo(V3 o, V3 d) {
+    RayGeo g;
+    g.b = dot3(o, d);
+    V3 c = cross3(o, d);
+    g.p = sqrtf(dot3(c, c));
+    g.r0sq = dot3(o, o);
+    return g;
+}
+
+// Altitude at distance t along the ray.
+__device__ __forceinline__ float altitude_at(const RayGeo& g, float t, float ground_radius) {
+    return sqrtf(fmaxf(fmaf(t, t + 2.0f * g.b, g.r0sq), 0.0f)) - ground_radius;
+}
+
+// Half chord sqrt(R^2 - p^2) (negative when the ray misses the shell).
+__device__ __forceinline__ float half_chord(float radius, float p) {
+    float disc = (radius - p) * (radius + p);
+    return disc >= 0.0f ? sqrtf(disc) : -1.0f;
+}
+
+// next_boundary (sky_trace.wgsl:233-250): ground (kind 0) or top exit (kind 1).
+__device__ __forceinline__ bool next_boundary(const DevScene& S, const RayGeo& g, float& t_out, uint32_t& kind) {
+    float q_top = half_chord(S.atmosphere_radius, g.p);
+    if (q_top < 0.0f) return false;
+    float t_exit = fmaxf(q_top - g.b, kRayEpsilonKm);
+    float t_ground = -1.0f;
+    float q_g = half_chord(S.ground_radius, g.p);
+    if (q_g >= 0.0f) {
+        float t0 = -q_g - g.b, t1 = q_g - g.b;
+        t_ground = t0 > kRayEpsilonKm ? t0 : (t1 > kRayEpsilonKm ? t1 : -1.0f);
+    }
+    if (t_ground > kRayEpsilonKm && t_ground < t_exit) {
+        t_out = t_ground;
+        kind = 0u;
+    } else {
+        t_out = t_exit;
+        kind = 1u;
+    }
+    return true;
+}
+
+// layer_for_altitude (sky_trace.wgsl:252-257)
+__device__ __forceinline__ uint32_t layer_for_altitude(const DevScene& S, float altitude) {
+    float top = fmaxf(S.top_altitude, 0.000001f);
+    float clamped = fminf(fmaxf(altitude, 0.0f), top - 0.000001f);
+    uint32_t layer = uint32_t(floorf(clamped / top * float(S.layer_count)));
+    return min(layer, S.layer_count - 1u);
+}
+
+// boundary_candidate for one layer shell (sky_trace.wgsl:263-282), both roots.
+__device__ __forceinline__ void shell_candidate(const DevScene& S, const RayGeo& g, float t, float alt_boundary,
+                                                float& next_t) {
+    if (alt_boundary <= 0.0f || alt_boundary >= S.top_altitude) return;
+    float q = half_chord(S.ground_radius + alt_boundary, g.p);
+    if (q < 0.0f) return;
+    float t0 = -q - g.b, t1 = q - g.b;
+    if (t0 > t + kRayEpsilonKm && t0 < next_t) next_t = t0;
+    if (t1 > t + kRayEpsilonKm && t1 < next_t) next_t = t1;
+}
+
+// next_majorant_segment_end (sky_trace.wgsl:284-294): the nearest crossing of
+// the current layer's lower or upper shell beyond t + epsilon; also returns
+// the layer whose majorant covers the segment (:419).
+__device__ __forceinline__ float next_segment_end(const DevScene& S, const RayGeo& g, float t, float t_max,
+                                                  uint32_t& layer) {
+    float probe = fminf(t + kRayEpsilonKm, t_max);
+    uint32_t k = layer_for_altitude(S, altitude_at(g, probe, S.ground_radius));
+    float next_t = t_max;
+    shell_candidate(S, g, t, float(k) * S.layer_dz, next_t);
+    shell_candidate(S, g, t, float(k + 1u) * S.layer_dz, next_t);
+    float probe2 = fminf(t + kRayEpsilonKm, next_t);
+    layer = probe2 == probe ? k : layer_for_altitude(S, altitude_at(g, probe2, S.ground_radius));
+    return next_t;
+}
+
+// ---- medium ---------------------------------------------------------------------------
+
+// Knot interval containing `alt` (alt in [0, top]).
+__device__ __forceinline__ uint32_t knot_interval(const DevScene& S, const float* knot_z, const uint16_t* finder,
+                                                  float alt) {
+    int cell = min(int(alt * S.finder_scale), int(kFinderCells) - 1);
+    uint32_t k = finder[cell];
+    while (k + 2u < S.knot_count && alt >= knot_z[k + 1u]) ++k;
+    return k;
+}
+
+// Total extinction of `band` at `alt` (extinction_total(coefficients_at()),
+// sky_trace.wgsl:356-403), from the per-band (value, slope) knot table.
+__device__ __forceinline__ float sigma_t_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
+                                            const float2* sigma_t, uint32_t band, float alt) {
+    if (!(alt >= 0.0f && alt <= S.top_altitude)) return 0.0f;
+    uint32_t k = knot_interval(S, knot_z, finder, alt);
+    float2 e = sigma_t[band * S.knot_count + k];
+    return fmaf(alt - knot_z[k], e.y, e.x);
+}
+
+struct Coeffs {  // MediumCoefficients (sky_trace.wgsl:101-106)
+    float rayleigh;
+    float sca[kSpecies];
+    float abs_total;  // ozone + aerosol absorption
+    float scattering;
+    float extinction;
+};
+
+// coefficients_at (sky_trace.wgsl:356-386) from the band-independent knot
+// profile and the per-band cross sections.
+__device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
+                                                  uint32_t band, float alt) {
+    Coeffs c;
+    c.rayleigh = 0.0f;
+#pragma unroll
+    for (int i = 0; i < int(kSpecies); ++i) c.sca[i] = 0.0f;
+    c.abs_total = 0.0f;
+    c.scattering = 0.0f;
+    c.extinction = 0.0f;
+    if (!(alt >= 0.0f && alt <= S.top_altitude)) return c;
+    uint32_t k = knot_interval(S, knot_z, finder, alt);
+    float dz = alt - knot_z[k];
+    const DevProfileKnot& P = S.profile[k];
+    const DevBand& B = S.bands[band];
+    float air = fmaf(dz, P.air_slope, P.air);
+    float ozone = fmaf(dz, P.ozone_slope, P.ozone);
+    c.rayleigh = fmaxf(air * B.rayleigh_xs, 0.0f);
+    float absorption = fmaxf(ozone * B.ozone_xs, 0.0f);
+    float scattering = c.rayleigh;
+#pragma unroll
+    for (int i = 0; i < int(kSpecies); ++i) {
+        float mass = fmaxf(fmaf(dz, P.mass_slope[i], P.mass[i]), 0.0f);
+        SkyAerosolOptics o = S.optics[band * kSpecies + i];
+        c.sca[i] = fmaxf(mass * o.scattering_km_inv_per_g_m3, 0.0f);
+        absorption += fmaxf(mass * o.absorption_km_inv_per_g_m3, 0.0f);
+        scattering += c.sca[i];
+    }
+    c.abs_total = absorption;
+    c.scattering = scattering;
+    c.extinction = scattering + absorption;
+    return c;
+}
+
+// ---- phase functions ----------------------------------------------------------------
+
+__device__ __forceinline__ float rayleigh_phase(float mu) { return kRayleighNorm * (1.0f + mu * mu); }
+
+// mie_phase (sky_trace.wgsl:485-494): lerp between bin centres on the
+// cube-root mu grid.
+__device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, uint32_t band, float mu) {
+    uint32_t bins = S.phase_bins;
+    float x = (1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f;
+    float u = cbrtf(x);
+    float f = u * float(bins) - 0.5f;
+    uint32_t i0 = min(uint32_t(fminf(fmaxf(floorf(f), 0.0f), float(bins - 1u))), bins - 1u);
+    uint32_t i1 = min(i0 + 1u, bins - 1u);
+    float t = fminf(fmaxf(f - float(i0), 0.0f), 1.0f);
+    const float* row = S.phase_values + (size_t(species) * S.band_count + band) * bins;
+    float p0 = __ldg(row + i0), p1 = __ldg(row + i1);
+    return fmaxf(fmaf(t, p1 - p0, p0), 0.0f);
+}
+
+// mixed_phase_value (sky_trace.wgsl:496-510)
+__device__ __forceinline__ float mixed_phase(const DevScene& S, const Coeffs& c, uint32_t band, float mu) {
+    if (c.scattering <= 0.0f) return 0.0f;
+    float acc = c.rayleigh * rayleigh_phase(mu);
+#pragma unroll
+    for (int i = 0; i < int(kSpecies); ++i)
+        if (c.sca[i] > 0.0f) acc = fmaf(c.sca[i], mie_phase(S, uint32_t(i), band, mu), acc);
+    return acc / c.scattering;
+}
+
+// phase.rs:137-140
+__device__ __forceinline__ float mu_edge(uint32_t edge, uint32_t bins) {
+    float u = float(edge) / float(bins);
+    return 1.0f - 2.0f * u * u * u;
+}
+
+// MiePhaseTable::sample_mu_pdf (phase.rs:53-69): binary search of the CDF.
+__device__ __forceinline__ float sample_mie_mu(const DevScene& S, uint32_t species, uint32_t band, float xi) {
+    uint32_t bins = S.phase_bins;
+    const float* cdf = S.phase_cdf + (size_t(species) * S.band_count + band) * bins;
+    xi = fminf(fmaxf(xi, 0.0f), 1.0f - kF32Epsilon);
+    uint32_t lo = 0, hi = bins;  // first index with cdf > xi
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) <= xi) lo = mid + 1u;
+        else hi = mid;
+    }
+    uint32_t bin = min(lo, bins - 1u);
+    float prev = bin == 0u ? 0.0f : __ldg(cdf + bin - 1u);
+    float next = __ldg(cdf + bin);
+    float t = next > prev ? (xi - prev) / (next - prev) : 0.5f;
+    float e0 = mu_edge(bin, bins), e1 = mu_edge(bin + 1u, bins);
+    return e0 * (1.0f - t) + e1 * t;
+}
+
+// MiePhaseTable::sampling_pdf (phase.rs:71-75, mu_to_bin :142-146)
+__device__ __forceinline__ float mie_sampling_pdf(const DevScene& S, uint32_t species, uint32_t band, float mu) {
+    uint32_t bins = S.phase_bins;
+    float u = cbrtf((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
+    uint32_t bin = min(uint32_t(floorf(u * float(bins))), bins - 1u);
+    return fmaxf(__ldg(S.phase_bin_pdf + (size_t(species) * S.band_count + band) * bins + bin), 1.0e-12f);
+}
+
+// Inverse Rayleigh CDF (sampling.rs:182-185): 2 sinh(asinh(y)/3) = u - 1/u
+// with u = cbrt(y + sqrt(y^2 + 1)), y = 4 xi - 2.
+__device__ __forceinline__ float invert_rayleigh_cdf(float xi) {
+    float y = 4.0f * fminf(fmaxf(xi, 0.0f), 1.0f) - 2.0f;
+    float u = cbrtf(y + sqrtf(fmaf(y, y, 1.0f)));
+    return fminf(fmaxf(u - 1.0f / u, -1.0f), 1.0f);
+}
+
+// ---- directions (sky_trace.wgsl:512-564) ----------------------------------------------
+
+__device__ __forceinline__ void orthonormal_basis(V3 n_in, V3& t, V3& bt) {  // :512-520
+    V3 n = normalize_or_y(n_in);
+    float sign = n.z >= 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (sign + n.z);
+    float b = n.x * n.y * a;
+    t = normalize_or_y(mk(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x));
+    bt = normalize_or_y(mk(b, sign + n.y * n.y * a, -n.y));
+}
+
+// direction_from_axis_mu with sin(theta) given by the caller (:522-532).
+__device__ __forceinline__ V3 direction_from_frame(V3 axis, V3 t, V3 bt, float mu, float sin_theta, float xi_phi) {
+    float s, c;
+    __sincosf(kTau * xi_phi, &s, &c);
+    V3 d = scale(axis, mu);
+    d = madd(d, t, sin_theta * c);
+    d = madd(d, bt, sin_theta * s);
+    return normalize_or_y(d);
+}
+
+__device__ __forceinline__ V3 direction_from_axis_mu(V3 axis_in, float mu_in, float xi_phi) {
+    float mu = fminf(fmaxf(mu_in, -1.0f), 1.0f);
+    float sin_theta = sqrtf(fmaxf(1.0f - mu * mu, 0.0f));
+    V3 t, bt;
+    orthonormal_basis(axis_in, t, bt);
+    return direction_from_frame(normalize_or_y(axis_in), t, bt, mu, sin_theta, xi_phi);
+}
+
+// sample_uniform_cone around the sun (:541-546); the sun's frame is
+// precomputed per scene, and sin(theta) uses (1-c)(1+c) to stay accurate for
+// the 0.27-degree cone.
+__device__ __forceinline__ V3 sample_sun_cone(const DevScene& S, Rng& rng) {
+    float xi = fminf(fmaxf(rng.next(), 0.0f), 0.99999994f);
+    float one_minus_cos = xi * S.one_minus_cos_max;
+    float cos_theta = 1.0f - one_minus_cos;
+    float sin_theta = sqrtf(fmaxf(one_minus_cos * (2.0f - one_minus_cos), 0.0f));
+    float xi_phi = rng.next();
+    return direction_from_frame(load3(S.sun), load3(S.sun_t), load3(S.sun_b), cos_theta, sin_theta, xi_phi);
+}
+
+// sample_isotropic (:534-539)
+__device__ __forceinline__ V3 sample_isotropic(Rng& rng) {
+    float z = 1.0f - 2.0f * rng.next();
+    float r = sqrtf(fmaxf(1.0f - z * z, 0.0f));
+    float s, c;
+    __sincosf(kTau * rng.next(), &s, &c);
+    return mk(r * c, z, r * s);
+}
+
+// sample_cosine_hemisphere (:548-560); returns the direction and its pdf.
+__device__ __forceinline__ V3 sample_cosine_hemisphere(V3 axis, Rng& rng, float& pdf) {
+    float u = rng.next();
+    float r = sqrtf(u);
+    float xi_phi = rng.next();
+    float cos_theta = sqrtf(fmaxf(1.0f - u, 0.0f));
+    V3 t, bt;
+    orthonormal_basis(axis, t, bt);
+    V3 n = normalize_or_y(axis);
+    V3 dir = direction_from_frame(n, t, bt, cos_theta, r, xi_phi);
+    pdf = fmaxf(dot3(n, dir), 0.0f) * kInvPi;
+    return dir;
+}
+
+// Tabulated continuation direction (phase.rs:53-75, sampling.rs:182-185):
+// component by sigma_s,i / sigma_s, mu from its inverse CDF, then phi.
+// Returns mixed_phase(mu) / mixture_pdf(mu).
+__device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeffs& c, uint32_t band, V3 axis,
+                                                  Rng& rng, V3& out_dir) {
+    float target = rng.next() * c.scattering;
+    int chosen = -1;
+    float acc = c.rayleigh;
+    if (target < acc) chosen = 0;
+#pragma unroll
+    for (int i = 0; i < int(kSpecies); ++i) {
+        acc = acc + c.sca[i];
+        if (chosen < 0 && target < acc) chosen = i + 1;
+    }
+    if (chosen < 0) {
+        chosen = 0;
+#pragma unroll
+        for (int i = 0; i < int(kSpecies); ++i)
+            if (c.sca[i] > 0.0f) chosen = i + 1;
+    }
+    float xi_mu = rng.next();
+    float mu = chosen == 0 ? invert_rayleigh_cdf(xi_mu) : sample_mie_mu(S, uint32_t(chosen - 1), band, xi_mu);
+    float xi_phi = rng.next();
+    out_dir = direction_from_axis_mu(axis, mu, xi_phi);
+    float inv_s = 1.0f / c.scattering;
+    float pdf = c.rayleigh * inv_s * rayleigh_phase(mu);
+#pragma unroll
+    for (int i = 0; i < int(kSpecies); ++i)
+        if (c.sca[i] > 0.0f) pdf = fmaf(c.sca[i] * inv_s, mie_sampling_pdf(S, uint32_t(i), band, mu), pdf);
+    return mixed_phase(S, c, band, mu) / pdf;
+}
+
+// ---- cameras (sky_trace.wgsl:610-689) --------------------------------------------------
+
+__device__ __forceinline__ V3 panorama_dir(float u, float v) {  // :614-623
+    float azimuth = (u - 0.5f) * kTau;
+    float elevation = (0.5f - v) * kPi;
+    float sa, ca, se, ce;
+    sincosf(azimuth, &sa, &ca);
+    sincosf(elevation, &se, &ce);
+    return normalize_or_y(mk(ce * sa, se, ce * ca));
+}
+
+__device__ __forceinline__ float from_sub_uvs_to_unit(float u, float resolution) {  // :625-630
+    if (resolution <= 1.0f) return 0.5f;
+    return (u - 0.5f / resolution) * (resolution / (resolution - 1.0f));
+}
+
+__device__ __forceinline__ V3 sky_view_lut_dir(const DevLaunch& L, float u_in, float v_in) {  // :641-681
+    float ux = fminf(fmaxf(from_sub_uvs_to_unit(u_in, float(L.width)), 0.0f), 1.0f);
+    float uy = fminf(fmaxf(from_sub_uvs_to_unit(v_in, float(L.height)), 0.0f), 1.0f);
+    float view_zenith_cos;
+    if (uy < 0.75f) {
+        float coord = uy / 0.75f;
+        coord = 1.0f - coord;
+        coord = coord * coord;
+        coord = 1.0f - coord;
+        view_zenith_cos = cosf(L.lut_zenith_horizon_angle * coord);
+    } else {
+        float coord = (uy - 0.75f) / 0.25f;
+        coord = coord * coord;
+        view_zenith_cos = cosf(L.lut_zenith_horizon_angle + L.lut_beta * coord);
+    }
+    float coord = ux * ux;
+    float light_view_cos = -(coord * 2.0f - 1.0f);
+    float sin_view = sqrtf(fmaxf(1.0f - view_zenith_cos * view_zenith_cos, 0.0f));
+    float side_scale = sqrtf(fmaxf(1.0f - light_view_cos * light_view_cos, 0.0f));
+    V3 f = load3(L.lut_forward), s = load3(L.lut_side);
+    V3 h = madd(scale(f, light_view_cos), s, side_scale);
+    return normalize_or_y(mk(sin_view * h.x, view_zenith_cos + sin_view * h.y, sin_view * h.z));
+}
+
+// Camera ray of sample `rng` for pixel (x, y) (sky_trace.wgsl:800-807): two
+// jitter draws are always consumed, also for the sky-view LUT.
+__device__ __forceinline__ V3 camera_dir(const DevLaunch& L, uint32_t x, uint32_t y, Rng& rng) {
+    float u = __fdiv_rn(float(x) + rng.next(), float(L.width));
+    float v = __fdiv_rn(float(y) + rng.next(), float(L.height));
+    if (L.projection == SKY_PROJECTION_SKY_VIEW_LUT) {
+        u = __fdiv_rn(float(x) + 0.5f, float(L.width));
+        v = __fdiv_rn(float(y) + 0.5f, float(L.height));
+        return sky_view_lut_dir(L, u, v);
+    }
+    return panorama_dir(u, v);
+}
+
+}  // namespace sky

@@ -1,0 +1,107 @@
+// sky_scene.h — device-resident scene layout shared by the host set-up code
+// and the kernels.
+//
+// The reference shader reads its medium through linear scans of the raw
+// atmosphere and aerosol profiles on every null-collision candidate
+// (sky_trace.wgsl:300-354).  Here the scene is re-tabulated once, at scene
+// creation, onto the union of both profiles' altitude knots: every
+// coefficient is linear in altitude between consecutive union knots, so the
+// extinction of a band is stored as (value, slope) per knot interval and a
+// lookup is one table read plus one FMA.  A uniform "finder" grid maps an
+// altitude to its knot interval in O(1).  Nothing about the medium changes:
+// between knots the reference's lerp of each profile is exactly linear, and
+// the tables are evaluated with the reference's own formulas at the knots
+// (sky_trace.wgsl:356-386).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sky_cuda.h"
+
+namespace sky {
+
+constexpr uint32_t kSpecies = SKY_SPECIES_COUNT;
+constexpr uint32_t kMaxBands = 256;
+constexpr uint32_t kMaxKnots = 1024;
+constexpr uint32_t kFinderCells = 512;
+constexpr uint32_t kMaxLayers = 1024;
+constexpr uint32_t kDefaultWatchdog = 1024;  // integrator.rs:14
+constexpr uint32_t kDefaultRrDepth = 4;      // sky_trace.wgsl:692
+constexpr float kRayEpsilonKm = 0.005f;      // sky_trace.wgsl:8
+
+// Per-band constants.
+struct DevBand {
+    float solar_radiance;  // SkyBand::solar_radiance_w_m2_sr
+    float rayleigh_xs;     // rayleigh_cross_section_m2 * 1e9 (sky_trace.wgsl:383)
+    float ozone_xs;        // ozone_cross_section_cm2 * 1e5  (sky_trace.wgsl:384)
+    float xyz[3];          // CIE 1931 weights at the band centre
+    float _pad[2];
+};
+static_assert(sizeof(DevBand) == 32, "DevBand layout");
+
+// Band-independent profile on the union knots: value at the knot and slope
+// per km up to the next knot, for air, ozone and the four aerosol masses.
+struct DevProfileKnot {
+    float air, air_slope;
+    float ozone, ozone_slope;
+    float mass[kSpecies];
+    float mass_slope[kSpecies];
+};
+static_assert(sizeof(DevProfileKnot) == 48, "DevProfileKnot layout");
+
+// Everything a kernel needs, passed by value as a kernel parameter.
+struct DevScene {
+    uint32_t band_count;
+    uint32_t knot_count;
+    uint32_t layer_count;
+    uint32_t phase_bins;
+    float ground_radius;
+    float atmosphere_radius;
+    float top_altitude;
+    float layer_dz;          // top / layers
+    float finder_scale;      // kFinderCells / top
+    float ground_albedo;
+    float sun[3];            // normalised sun direction
+    float sun_t[3];          // orthonormal basis of the sun axis
+    float sun_b[3];
+    float cos_max;           // cos(sun angular radius)
+    float one_minus_cos_max;
+    float light_pdf;         // 1 / (2 pi (1 - cos_max))
+    uint32_t mie_mask;       // bit i set when species i scatters in some band
+    // device tables
+    const float* knot_z;               // [K]
+    const uint16_t* finder;            // [kFinderCells] knot interval of each cell's lower edge
+    const float2* sigma_t;             // [B][K] extinction (value, slope) per knot interval
+    const float* majorants;            // [B][L]
+    const DevBand* bands;              // [B]
+    const DevProfileKnot* profile;     // [K]
+    const SkyAerosolOptics* optics;    // [B][species]
+    const float* phase_values;         // [species][B][bins]
+    const float* phase_cdf;            // [species][B][bins]
+    const float* phase_bin_pdf;        // [species][B][bins]
+};
+
+// Per-launch constants.
+struct DevLaunch {
+    uint32_t width, height, spp, sample_offset;
+    uint32_t band_count;
+    uint32_t direct_light_samples;
+    uint32_t projection;
+    uint32_t phase_sampling;
+    uint32_t rr_start_depth;
+    uint32_t max_orders;      // 0 = unbounded
+    uint32_t watchdog_limit;
+    uint32_t tracking;        // SkyTracking
+    uint32_t seed_lo, seed_hi;
+    float observer_altitude;
+    // sky-view LUT frame (sky_trace.wgsl:641-681), computed once per launch
+    float lut_zenith_horizon_angle;
+    float lut_beta;
+    float lut_forward[3];
+    float lut_side[3];
+    float inv_width, inv_height;
+};
+
+}  // namespace sky

@@ -1,0 +1,182 @@
+"""ctypes mirror of include/sky_cuda.h and the loader of libsky_cuda.so.
+
+The library is built in-tree (sky-tracer_gb300/_build/libsky_cuda.so, see
+build.py).  There is no CPU fallback: if the library is missing, importing the
+render entry points raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+PACKAGE_ROOT = Path(__file__).resolve().parent.parent
+LIB_PATH = PACKAGE_ROOT / "_build" / "libsky_cuda.so"
+
+SPECIES_COUNT = 4
+
+# Status codes (SkyStatus); 1-6 = RenderError variants (integrator.rs:18-26).
+SKY_OK = 0
+SKY_ERR_INVALID_CONFIG = 1
+SKY_ERR_NO_DEVICE = 2
+SKY_ERR_DEVICE_INIT = 3
+SKY_ERR_COPY = 4
+SKY_ERR_SYNC = 5
+SKY_ERR_WATCHDOG = 6
+SKY_ERR_OUT_OF_MEMORY = 7
+SKY_ERR_LAUNCH = 8
+SKY_ERR_IO = 9
+
+PROJECTION_PANORAMA = 0
+PROJECTION_SKY_VIEW_LUT = 1
+PHASE_ISOTROPIC = 0
+PHASE_TABULATED = 1
+TRACKING_SEGMENT_RESTART = 0
+TRACKING_RESIDUAL_CARRY = 1
+KERNEL_AUTO = 0
+KERNEL_PLAIN = 1
+KERNEL_WAVEFRONT = 2
+FLAG_ACCUMULATE = 1
+
+EVENT_NAMES = ("track_step", "segment", "boundary", "scatter", "nee", "ground", "chain")
+EVENT_COUNT = 8
+
+# numpy dtypes with the byte layout of the C rows (integrator.rs:77-112).
+BAND_DTYPE = np.dtype([
+    ("center_nm", "<f4"), ("lower_nm", "<f4"), ("upper_nm", "<f4"),
+    ("ozone_cross_section_cm2", "<f4"), ("solar_radiance_w_m2_sr", "<f4"),
+    ("rayleigh_cross_section_m2", "<f4"),
+])
+ATMOSPHERE_DTYPE = np.dtype([
+    ("altitude_km", "<f4"), ("temperature_k", "<f4"), ("air_cm3", "<f4"), ("ozone_cm3", "<f4"),
+])
+AEROSOL_DTYPE = np.dtype([("altitude_km", "<f4"), ("mass_g_m3", "<f4", (4,)), ("_pad", "<f4", (3,))])
+OPTICS_DTYPE = np.dtype([("scattering_km_inv_per_g_m3", "<f4"), ("absorption_km_inv_per_g_m3", "<f4")])
+assert BAND_DTYPE.itemsize == 24 and ATMOSPHERE_DTYPE.itemsize == 16
+assert AEROSOL_DTYPE.itemsize == 32 and OPTICS_DTYPE.itemsize == 8
+
+_f = ctypes.c_float
+_u32 = ctypes.c_uint32
+_fp = ctypes.POINTER(ctypes.c_float)
+_vp = ctypes.c_void_p
+
+
+class SkySceneDesc(ctypes.Structure):
+    _fields_ = [
+        ("band_count", _u32), ("atmosphere_len", _u32), ("aerosol_len", _u32),
+        ("majorant_layers", _u32), ("phase_bins", _u32), ("_reserved0", _u32),
+        ("ground_radius_km", _f), ("atmosphere_radius_km", _f), ("top_altitude_km", _f),
+        ("sun_direction", _f * 3), ("sun_angular_radius_rad", _f), ("sun_solid_angle_sr", _f),
+        ("ground_albedo", _f), ("_reserved1", _f),
+        ("bands", _vp), ("atmosphere", _vp), ("aerosol", _vp), ("aerosol_optics", _vp),
+        ("majorants_km_inv", _vp), ("phase_values", _vp), ("band_xyz_weights", _vp),
+    ]
+
+
+class SkyRenderConfig(ctypes.Structure):
+    _fields_ = [
+        ("width", _u32), ("height", _u32), ("spp", _u32), ("direct_light_samples", _u32),
+        ("seed", ctypes.c_uint64),
+        ("sun_elevation_deg", _f), ("sun_azimuth_deg", _f), ("observer_altitude_km", _f),
+        ("output_projection", _u32),
+        ("sample_offset", _u32), ("phase_sampling", _u32), ("rr_start_depth", _u32),
+        ("max_orders", _u32), ("watchdog_limit", _u32), ("kernel", _u32), ("flags", _u32),
+        ("tracking", _u32), ("_reserved", _u32 * 2),
+    ]
+
+
+class SkyRenderStats(ctypes.Structure):
+    _fields_ = [
+        ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double), ("chains", ctypes.c_uint64),
+        ("events", ctypes.c_uint64 * EVENT_COUNT), ("watchdog", _u32), ("kernel_used", _u32),
+    ]
+
+
+class SkyDeviceOutputs(ctypes.Structure):
+    _fields_ = [
+        ("cell_sum", _vp), ("cell_sumsq", _vp), ("film", _vp), ("xyz", _vp), ("xyz_var", _vp),
+        ("counters", _vp), ("status", _vp),
+    ]
+
+
+assert ctypes.sizeof(SkySceneDesc) == 120
+assert ctypes.sizeof(SkyRenderConfig) == 80
+assert ctypes.sizeof(SkyRenderStats) == 96
+
+# Every symbol include/sky_cuda.h declares, with its ctypes signature.
+_SIGNATURES = {
+    "sky_cuda_version": (ctypes.c_char_p, []),
+    "sky_cuda_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "sky_cuda_scene_create": (ctypes.c_int, [ctypes.POINTER(SkySceneDesc), ctypes.POINTER(_vp)]),
+    "sky_cuda_scene_destroy": (None, [_vp]),
+    "sky_cuda_render": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t,
+                                       ctypes.POINTER(SkyRenderStats)]),
+    "sky_cuda_render_xyz": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
+    "sky_cuda_render_desc": (ctypes.c_int, [ctypes.POINTER(SkySceneDesc), ctypes.POINTER(SkyRenderConfig), _fp,
+                                            ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
+    "sky_cuda_render_device": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
+                                              ctypes.POINTER(SkyDeviceOutputs), _vp]),
+}
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("SKY_CUDA_LIB", str(LIB_PATH)))
+
+
+def load_library() -> ctypes.CDLL:
+    """Load libsky_cuda.so (built by sky-tracer_gb300/build.py); raises if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise RuntimeError(
+            f"libsky_cuda.so not found at {path}; build it with "
+            "`python sky-tracer_gb300/build.py` (there is no CPU fallback)")
+    lib = ctypes.CDLL(str(path))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def last_error(lib=None) -> str:
+    lib = lib or load_library()
+    buf = ctypes.create_string_buffer(1024)
+    lib.sky_cuda_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+class SkyCudaError(RuntimeError):
+    """A failed C-ABI call; `status` is the SkyStatus code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.message = message
+
+
+class RenderWatchdog(SkyCudaError):
+    """RenderError::Watchdog (integrator.rs:301-304)."""
+
+
+def check(status: int, lib=None) -> None:
+    if status == SKY_OK:
+        return
+    msg = last_error(lib)
+    if status == SKY_ERR_WATCHDOG:
+        raise RenderWatchdog(status, msg)
+    raise SkyCudaError(status, msg)

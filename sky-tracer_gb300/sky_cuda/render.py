@@ -1,0 +1,170 @@
+"""Host-side mirror of the reference integrator API over the C ABI.
+
+    render(scene, config) -> Film          # integrator.rs:125-128
+    RenderConfig                           # config.rs:2-52
+    Film                                   # film.rs:2-62
+    RenderError kinds                      # integrator.rs:18-39 (SkyCudaError.status)
+
+GpuScene keeps the scene's tables resident on the device between renders
+(sky_cuda_scene_create); render() is the one-shot form that uploads, renders
+and frees inside the call, like the reference.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import SkyDeviceOutputs, SkyRenderConfig, SkyRenderStats, check, load_library
+from .scene import Scene
+
+DEFAULT_SEED = 0x5EC7_2026_0430  # config.rs:44
+
+
+@dataclass
+class RenderConfig:
+    """RenderConfig (config.rs:2-12, defaults :38-52) plus the extensions of
+    SkyRenderConfig; the extension defaults reproduce the reference shader."""
+
+    width: int = 1024
+    height: int = 512
+    spp: int = 256
+    seed: int = DEFAULT_SEED
+    sun_elevation_deg: float = 0.0
+    sun_azimuth_deg: float = 0.0
+    observer_altitude_km: float = 0.2
+    direct_light_samples: int = 1
+    output_projection: int = _abi.PROJECTION_PANORAMA
+    sample_offset: int = 0
+    phase_sampling: int = _abi.PHASE_ISOTROPIC
+    rr_start_depth: int = 0
+    max_orders: int = 0
+    watchdog_limit: int = 0
+    kernel: int = _abi.KERNEL_AUTO
+    flags: int = 0
+    tracking: int = _abi.TRACKING_SEGMENT_RESTART
+
+    def to_c(self) -> SkyRenderConfig:
+        c = SkyRenderConfig()
+        for name, _ in SkyRenderConfig._fields_:
+            if name.startswith("_"):
+                continue
+            setattr(c, name, getattr(self, name))
+        return c
+
+    @property
+    def pixels(self) -> int:
+        return self.width * self.height
+
+
+@dataclass
+class Film:
+    """Film (film.rs:2-62): pixel-major, band-minor float32 values."""
+
+    width: int
+    height: int
+    band_count: int
+    values: np.ndarray
+
+    def pixel_spectrum(self, pixel: int) -> np.ndarray:
+        return self.values[pixel * self.band_count:(pixel + 1) * self.band_count]
+
+    def as_array(self) -> np.ndarray:
+        return self.values.reshape(self.height, self.width, self.band_count)
+
+
+@dataclass
+class RenderStats:
+    kernel_ms: float
+    total_ms: float
+    chains: int
+    events: dict
+    watchdog: int
+    kernel_used: int
+
+    @classmethod
+    def from_c(cls, s: SkyRenderStats) -> "RenderStats":
+        return cls(s.kernel_ms, s.total_ms, int(s.chains),
+                   {n: int(s.events[i]) for i, n in enumerate(_abi.EVENT_NAMES)}, int(s.watchdog),
+                   int(s.kernel_used))
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class GpuScene:
+    """A scene uploaded to the current CUDA device (sky_cuda_scene_create)."""
+
+    def __init__(self, scene: Scene):
+        self.lib = load_library()
+        self.scene = scene
+        self.band_count = scene.band_count
+        self._desc = scene.desc()
+        handle = ctypes.c_void_p()
+        check(self.lib.sky_cuda_scene_create(ctypes.byref(self._desc), ctypes.byref(handle)), self.lib)
+        self.handle = handle
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and self.handle.value:
+            self.lib.sky_cuda_scene_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, config: RenderConfig) -> tuple[Film, RenderStats]:
+        film = np.empty(config.pixels * self.band_count, dtype=np.float32)
+        stats = SkyRenderStats()
+        check(self.lib.sky_cuda_render(self.handle, ctypes.byref(config.to_c()), _fptr(film), film.size,
+                                       ctypes.byref(stats)), self.lib)
+        return Film(config.width, config.height, self.band_count, film), RenderStats.from_c(stats)
+
+    def render_xyz(self, config: RenderConfig, with_film: bool = True):
+        """Film, per-pixel XYZ [pixels, 3] (FP64) and its variance, and stats."""
+        film = np.empty(config.pixels * self.band_count, dtype=np.float32) if with_film else None
+        xyz = np.empty((config.pixels, 3), dtype=np.float64)
+        var = np.empty((config.pixels, 3), dtype=np.float64)
+        stats = SkyRenderStats()
+        check(self.lib.sky_cuda_render_xyz(self.handle, ctypes.byref(config.to_c()),
+                                           _fptr(film) if film is not None else None,
+                                           film.size if film is not None else 0, _dptr(xyz), _dptr(var),
+                                           config.pixels, ctypes.byref(stats)), self.lib)
+        f = Film(config.width, config.height, self.band_count, film) if film is not None else None
+        return f, xyz, var, RenderStats.from_c(stats)
+
+    def render_device(self, config: RenderConfig, outputs: dict, stream: int = 0) -> None:
+        """Queue a render into device buffers given as integer device pointers
+        (keys: cell_sum, cell_sumsq, film, xyz, xyz_var, counters, status)."""
+        o = SkyDeviceOutputs()
+        for name, _ in SkyDeviceOutputs._fields_:
+            setattr(o, name, outputs.get(name) or None)
+        check(self.lib.sky_cuda_render_device(self.handle, ctypes.byref(config.to_c()), ctypes.byref(o),
+                                              ctypes.c_void_p(stream)), self.lib)
+
+
+def render(scene: Scene, config: RenderConfig) -> Film:
+    """One-shot render (integrator.rs:125-128): upload, trace, read back, free."""
+    lib = load_library()
+    desc = scene.desc()
+    film = np.empty(config.pixels * scene.band_count, dtype=np.float32)
+    stats = SkyRenderStats()
+    check(lib.sky_cuda_render_desc(ctypes.byref(desc), ctypes.byref(config.to_c()), _fptr(film), film.size,
+                                   ctypes.byref(stats)), lib)
+    return Film(config.width, config.height, scene.band_count, film)

@@ -1,0 +1,198 @@
+"""GPU parity: the CUDA tracer, called through the C ABI, against the oracle
+and against analytic answers.  Runs on the GB300 machine (`-m gpu`)."""
+
+import math
+
+import numpy as np
+import pytest
+
+import analytic
+import sky_oracle as oracle
+from sky_cuda import (FLAG_ACCUMULATE, GpuScene, RenderConfig, RenderWatchdog, SkyCudaError, SyntheticAtmosphere,
+                      render, synthetic_scene, wavelengths)
+from sky_cuda import _abi
+from skystats import parity_report, xyz_from_sums
+
+pytestmark = pytest.mark.gpu
+
+MODES = [(t, p) for t in (_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY)
+         for p in (_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED)]
+
+
+def gpu_sums(gs: GpuScene, cfg: RenderConfig):
+    import torch
+    cells = cfg.pixels * gs.band_count
+    s = torch.zeros(cells, dtype=torch.float64, device="cuda")
+    q = torch.zeros(cells, dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    ctr = torch.zeros(8, dtype=torch.int64, device="cuda")
+    gs.render_device(cfg, {"cell_sum": s.data_ptr(), "cell_sumsq": q.data_ptr(), "status": st.data_ptr(),
+                           "counters": ctr.data_ptr()}, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    shape = (cfg.pixels, gs.band_count)
+    return s.cpu().numpy().reshape(shape), q.cpu().numpy().reshape(shape), ctr.cpu().numpy(), int(st.item())
+
+
+def test_smoke_film(gpu, ref_scene):
+    # smoke.rs:7-24 through the one-shot entry point
+    film = render(ref_scene, RenderConfig(width=32, height=16, spp=2))
+    v = film.values
+    assert v.shape == (32 * 16 * 41,)
+    assert np.all(np.isfinite(v)) and np.all(v >= 0) and np.any(v > 0)
+
+
+@pytest.mark.parametrize("tracking,phase", MODES)
+def test_chains_match_oracle(gpu, cfg0_scene, tracking, phase):
+    """One sample per cell: each GPU chain against the oracle's chain with the
+    same counter-based random stream.  Differences come only from rounding
+    (fast-math intrinsics, the impact-parameter geometry), which flips a
+    decision in a small fraction of chains."""
+    agree = total = 0
+    with GpuScene(cfg0_scene) as gs:
+        for offset in (0, 7, 1000):
+            cfg = RenderConfig(width=16, height=8, spp=1, sample_offset=offset, seed=0x5EC7_2026_0430 + offset,
+                               phase_sampling=phase, tracking=tracking, max_orders=16)
+            g, _, _, st = gpu_sums(gs, cfg)
+            o, _, _, wd = oracle.render(cfg0_scene, cfg)
+            assert st == 0 and wd == 0
+            close = np.abs(g - o) <= 2e-3 * np.maximum(np.abs(g), np.abs(o)) + 1e-9
+            agree += int(close.sum())
+            total += close.size
+    frac = agree / total
+    print(f"chain agreement tracking={tracking} phase={phase}: {frac:.4f} of {total}")
+    assert frac >= 0.95
+
+
+@pytest.mark.parametrize("tracking,phase", [MODES[0], MODES[3]])
+def test_statistical_parity_cfg0(gpu, cfg0_scene, tracking, phase):
+    """The CPU-runnable benchmark scene (64x32, 32 bands, 64 spp): per-pixel
+    XYZ of GPU and oracle within 3 combined standard errors, and no bias."""
+    cfg = RenderConfig(width=64, height=32, spp=64, sun_elevation_deg=10.0, phase_sampling=phase,
+                       tracking=tracking, max_orders=16)
+    with GpuScene(cfg0_scene) as gs:
+        gs_, gq, _, st = gpu_sums(gs, cfg)
+    cfg_o = RenderConfig(**{**cfg.__dict__, "seed": 12345})
+    os_, oq, _, wd = oracle.render(cfg0_scene, cfg_o)
+    assert st == 0 and wd == 0
+    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, cfg0_scene.band_xyz)
+    xo, vo = xyz_from_sums(os_, oq, cfg.spp, cfg0_scene.band_xyz)
+    r = parity_report(xg, vg, xo, vo)
+    print("cfg0 parity", r)
+    assert r["frac_beyond_3se"] <= 0.01
+    bias = abs(float((xg[:, 1] - xo[:, 1]).sum() / xo[:, 1].sum()))
+    assert bias < 0.005
+
+
+def test_high_spp_mean_relative_error(gpu, data_dir):
+    """Matched high sample counts: mean relative XYZ error under 0.5 %."""
+    scene = synthetic_scene(wavelengths(400, 700, 8), data_dir, sun_elevation_deg=10.0)
+    cfg = RenderConfig(width=16, height=8, spp=4096, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_RESIDUAL_CARRY, max_orders=16)
+    with GpuScene(scene) as gs:
+        gs_, gq, _, _ = gpu_sums(gs, cfg)
+    os_, oq, _, _ = oracle.render(scene, RenderConfig(**{**cfg.__dict__, "seed": 4242}))
+    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, scene.band_xyz)
+    xo, vo = xyz_from_sums(os_, oq, cfg.spp, scene.band_xyz)
+    r = parity_report(xg, vg, xo, vo)
+    print("high-spp parity", r)
+    assert r["frac_beyond_3se"] <= 0.02
+    assert abs(float((xg - xo).sum() / xo.sum())) < 0.005
+
+
+def test_vacuum_ground_known_answer(gpu, data_dir):
+    a = SyntheticAtmosphere(rayleigh_ext_km=0.0, mie_ext_km=0.0, ozone_peak_km=0.0)
+    scene = synthetic_scene(wavelengths(450, 650, 3), data_dir, sun_elevation_deg=30.0, atmosphere=a)
+    cfg = RenderConfig(width=1, height=8, spp=2048, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
+    with GpuScene(scene) as gs:
+        s, q, _, st = gpu_sums(gs, cfg)
+    mean = s / cfg.spp
+    se = np.sqrt(np.maximum(q / cfg.spp - mean * mean, 0) / cfg.spp)
+    for y in range(8):
+        d = analytic.lut_direction(1, 8, 0, y, 0.2, scene.ground_radius_km, scene.sun_direction)
+        for band in range(3):
+            if y >= 6:
+                want = analytic.vacuum_ground(scene, band, d)
+                assert abs(mean[y, band] - want) <= 4 * se[y, band] + 1e-4 * want
+            else:
+                assert mean[y, band] == 0.0
+
+
+@pytest.mark.parametrize("tracking", [_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY])
+def test_single_scatter_known_answer(gpu, data_dir, tracking):
+    a = SyntheticAtmosphere(ground_albedo=0.0)
+    scene = synthetic_scene(wavelengths(440, 640, 3), data_dir, sun_elevation_deg=35.0, atmosphere=a)
+    cfg = RenderConfig(width=1, height=8, spp=262144, max_orders=1, output_projection=_abi.PROJECTION_SKY_VIEW_LUT,
+                       tracking=tracking)
+    with GpuScene(scene) as gs:
+        s, q, _, st = gpu_sums(gs, cfg)
+    assert st == 0
+    for y in (0, 3, 5):
+        d = analytic.lut_direction(1, 8, 0, y, 0.2, scene.ground_radius_km, scene.sun_direction)
+        for band in range(3):
+            want = analytic.single_scatter(scene, band, d,
+                                           lambda sp, b, mu: oracle.mie_phase(scene, sp, b, [mu])[0])
+            mean = s[y, band] / cfg.spp
+            se = math.sqrt(max(q[y, band] / cfg.spp - mean * mean, 0) / cfg.spp)
+            assert abs(mean - want) <= 4 * se + 0.002 * want, (y, band, mean, want, se)
+
+
+def test_film_matches_sums_and_progressive_is_exact(gpu, cfg0_scene):
+    cfg = RenderConfig(width=16, height=8, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_RESIDUAL_CARRY)
+    with GpuScene(cfg0_scene) as gs:
+        film, stats = gs.render(cfg)
+        s, q, _, _ = gpu_sums(gs, cfg)
+        np.testing.assert_array_equal(film.values, np.maximum((s / 64).astype(np.float32), 0).ravel())
+        # two progressive halves == one render, bit for bit
+        import torch
+        cells = cfg.pixels * gs.band_count
+        ps = torch.zeros(cells, dtype=torch.float64, device="cuda")
+        pq = torch.zeros(cells, dtype=torch.float64, device="cuda")
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for off in (0, 32):
+            c = RenderConfig(**{**cfg.__dict__, "spp": 32, "sample_offset": off,
+                                "flags": FLAG_ACCUMULATE if off else 0})
+            gs.render_device(c, {"cell_sum": ps.data_ptr(), "cell_sumsq": pq.data_ptr(), "status": st.data_ptr()},
+                             torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(ps.cpu().numpy().reshape(s.shape), s)
+        np.testing.assert_array_equal(pq.cpu().numpy().reshape(q.shape), q)
+    assert stats.chains == cells * 64 and stats.kernel_ms > 0
+    assert stats.events["chain"] == stats.chains
+
+
+def test_xyz_outputs(gpu, cfg0_scene):
+    cfg = RenderConfig(width=16, height=8, spp=64)
+    with GpuScene(cfg0_scene) as gs:
+        film, xyz, var, _ = gs.render_xyz(cfg)
+        s, q, _, _ = gpu_sums(gs, cfg)
+    x_ref, v_ref = xyz_from_sums(s, q, 64, cfg0_scene.band_xyz)
+    np.testing.assert_allclose(xyz, x_ref, rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(var, v_ref, rtol=1e-9, atol=1e-20)
+
+
+def test_watchdog_and_errors(gpu, cfg0_scene):
+    with GpuScene(cfg0_scene) as gs:
+        # a forced one-event watchdog trips on any scattered path (integrator.rs:301-304)
+        with pytest.raises(RenderWatchdog):
+            gs.render(RenderConfig(width=8, height=4, spp=4, watchdog_limit=1))
+        with pytest.raises(SkyCudaError) as e:
+            gs.render(RenderConfig(width=0, height=4, spp=4))
+        assert e.value.status == _abi.SKY_ERR_INVALID_CONFIG
+        # the scene stays usable after both failures
+        film, _ = gs.render(RenderConfig(width=8, height=4, spp=4))
+        assert np.all(np.isfinite(film.values))
+
+
+def test_reference_default_band_count(gpu, ref_scene):
+    """The drop-in scene: 41 bands, 1024-bin phase tables, isotropic sampling,
+    the reference's defaults throughout."""
+    cfg = RenderConfig(width=16, height=8, spp=32)
+    with GpuScene(ref_scene) as gs:
+        s, q, _, st = gpu_sums(gs, cfg)
+    o, oq, _, _ = oracle.render(ref_scene, RenderConfig(**{**cfg.__dict__, "seed": 99}))
+    xg, vg = xyz_from_sums(s, q, 32, ref_scene.band_xyz)
+    xo, vo = xyz_from_sums(o, oq, 32, ref_scene.band_xyz)
+    r = parity_report(xg, vg, xo, vo)
+    print("reference scene parity", r)
+    assert st == 0 and r["frac_beyond_3se"] <= 0.03
