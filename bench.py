@@ -61,7 +61,7 @@ def parse_args():
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
     p.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
-    p.add_argument("--tracking", type=int, default=1, help="SkyTracking (1 = residual carry)")
+    p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -331,8 +331,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "width": cfg.width, "height": cfg.height, "wavelengths": B,
                        "spp": cfg.spp, "chains_per_step": chains, "sun_elevation_deg": w["sun"],
-                       "tracking": "residual-carry" if cfg.tracking else "segment-restart",
-                       "phase_sampling": "tabulated", "kernel": cfg.kernel,
+                       "tracking": ("segment-restart", "residual-carry", "merged-layers")[cfg.tracking],
+                       "phase_sampling": "tabulated", "kernel": ("persistent", "plain", "persistent")[cfg.kernel],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}"},
             "e2e": {"value": world * chains / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(desc_bytes),
                     "d2h_bytes_per_step": int(cells * 4 + 8 * 8 + 4)},
@@ -344,7 +344,7 @@ def main():
                          "flops_per_step": flops_per_step, "events_per_step": ev},
             "cpu_baseline": cpu,
             "clocks": clocks.summary(),
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": (2 if cfg.kernel == 1 else 1) * args.steps,
         }
         print(json.dumps(out))
     gs.close()

@@ -138,7 +138,12 @@ typedef enum SkyTracking {
     /* Same collision distribution, one exponential draw per tentative
      * collision: the residual optical depth is carried across segment
      * boundaries instead of being re-drawn. */
-    SKY_TRACKING_RESIDUAL_CARRY = 1
+    SKY_TRACKING_RESIDUAL_CARRY = 1,
+    /* Residual carry over a coarser tracking grid: adjacent majorant layers
+     * of each band are merged (majorant = max of the merged layers, so still
+     * a bound) where the extra null collisions cost less than the saved
+     * layer crossings.  Same collision distribution again. */
+    SKY_TRACKING_MERGED_LAYERS = 2
 } SkyTracking;
 
 typedef enum SkyKernel {

@@ -111,7 +111,31 @@ void build_phase_sampling_tables(const float* values, uint32_t band_count, uint3
     }
 }
 
-int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err) {
+std::vector<uint32_t> merge_majorant_layers(const float* maj, uint32_t L, float dz, double crossing_cost) {
+    std::vector<double> best(L + 1, 0.0);
+    std::vector<uint32_t> from(L + 1, 0);
+    for (uint32_t j = 1; j <= L; ++j) {
+        best[j] = 1e300;
+        double mx = 0.0, sum = 0.0;
+        for (uint32_t i = j; i-- > 0;) {  // group [i, j)
+            double m = std::max(double(maj[i]), 1e-8);
+            mx = std::max(mx, m);
+            sum += m;
+            double excess = (mx * double(j - i) - sum) * double(dz);
+            double c = best[i] + crossing_cost + excess;
+            if (c < best[j]) {
+                best[j] = c;
+                from[j] = i;
+            }
+        }
+    }
+    std::vector<uint32_t> starts;
+    for (uint32_t j = L; j > 0; j = from[j]) starts.push_back(from[j]);
+    std::reverse(starts.begin(), starts.end());
+    return starts;
+}
+
+int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, double crossing_cost) {
     auto fail = [&err](const std::string& msg) {
         err = msg;
         return int(SKY_ERR_INVALID_CONFIG);
@@ -230,6 +254,36 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err) 
     out.knot_z = z;
     out.majorants.assign(d->majorants_km_inv, d->majorants_km_inv + nmaj);
 
+    // Merged tracking grid per band (compact rows: count + 1 radii, count majorants).
+    {
+        const uint32_t L = d->majorant_layers;
+        const float dzl = top / float(L);
+        out.trk_radius.clear();
+        out.trk_maj.clear();
+        out.trk_map.assign(size_t(B) * L, 0);
+        out.trk_count.assign(B, 0);
+        out.trk_off.assign(B, 0);
+        for (uint32_t b = 0; b < B; ++b) {
+            const float* maj = d->majorants_km_inv + size_t(b) * L;
+            std::vector<uint32_t> starts = merge_majorant_layers(maj, L, dzl, crossing_cost);
+            const uint32_t M = uint32_t(starts.size());
+            out.trk_count[b] = M;
+            out.trk_off[b] = uint32_t(out.trk_radius.size());
+            for (uint32_t m = 0; m < M; ++m) {
+                uint32_t k0 = starts[m], k1 = m + 1 < M ? starts[m + 1] : L;
+                float mx = 0.0f;
+                for (uint32_t k = k0; k < k1; ++k) {
+                    mx = std::max(mx, std::max(maj[k], 0.00000001f));
+                    out.trk_map[size_t(b) * L + k] = uint16_t(m);
+                }
+                out.trk_maj.push_back(mx);
+                out.trk_radius.push_back(d->ground_radius_km + float(k0) * dzl);
+            }
+            out.trk_maj.push_back(0.0f);  // keeps both arrays the same length
+            out.trk_radius.push_back(d->ground_radius_km + top);
+        }
+    }
+
     // Phase tables and their sampling CDFs.
     out.phase_values.assign(d->phase_values, d->phase_values + nphase);
     build_phase_sampling_tables(d->phase_values, B, d->phase_bins, out.phase_cdf, out.phase_bin_pdf);
@@ -244,6 +298,8 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err) 
     S.atmosphere_radius = d->atmosphere_radius_km;
     S.top_altitude = top;
     S.layer_dz = top / float(d->majorant_layers);
+    S.inv_layer_dz = float(d->majorant_layers) / top;
+    S.trk_total = uint32_t(out.trk_radius.size());
     S.finder_scale = float(kFinderCells) / top;
     S.ground_albedo = d->ground_albedo;
     float sl = std::sqrt(d->sun_direction[0] * d->sun_direction[0] + d->sun_direction[1] * d->sun_direction[1] +

@@ -20,13 +20,27 @@ struct HostTables {
     std::vector<DevProfileKnot> profile;
     std::vector<SkyAerosolOptics> optics;
     std::vector<float> phase_values, phase_cdf, phase_bin_pdf;
+    std::vector<float> trk_radius, trk_maj;
+    std::vector<uint16_t> trk_map;
+    std::vector<uint32_t> trk_count, trk_off;
     bool has_xyz = false;
 };
+
+// Relative cost of one layer crossing against one null collision, used to
+// merge majorant layers for SKY_TRACKING_MERGED_LAYERS.
+constexpr double kDefaultCrossingCost = 0.25;
+
+// Partition the `layers` uniform majorant layers of one band into contiguous
+// groups minimising  sum_groups [crossing_cost + dz * sum_k (max_group - maj_k)],
+// i.e. crossings plus the extra null collisions of a vertical ray.  Returns
+// the first uniform layer of each group (ascending, starting at 0).
+std::vector<uint32_t> merge_majorant_layers(const float* maj, uint32_t layers, float dz, double crossing_cost);
 
 // Validates `desc` (the checks of integrator.rs:130-163 and :401-407, with
 // the band and bin counts as run-time values) and fills `out`.  Returns
 // SKY_OK or SKY_ERR_INVALID_CONFIG with a message in `err`.
-int build_host_tables(const SkySceneDesc* desc, HostTables& out, std::string& err);
+int build_host_tables(const SkySceneDesc* desc, HostTables& out, std::string& err,
+                      double crossing_cost = kDefaultCrossingCost);
 
 // MiePhaseTable sampling tables (phase.rs:105-135): per (species, band) the
 // CDF over the cube-root mu bins and the per-bin pdf.

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -36,6 +37,10 @@ struct SkyScene {
     unsigned long long* ws_counters = nullptr;
     uint32_t* ws_status = nullptr;
     uint64_t ws_cells = 0, ws_pixels = 0;
+    // persistent-kernel job table and work counter (one job per render call)
+    DevJob* jobs = nullptr;
+    uint32_t* work_counter = nullptr;
+    int smem_optin = 0;
 };
 
 namespace {
@@ -108,7 +113,7 @@ int validate_config(const SkyScene* scene, const SkyRenderConfig* c) {
         return set_error(SKY_ERR_INVALID_CONFIG, "unknown output projection");
     if (c->phase_sampling > SKY_PHASE_TABULATED)
         return set_error(SKY_ERR_INVALID_CONFIG, "unknown phase sampling mode");
-    if (c->tracking > SKY_TRACKING_RESIDUAL_CARRY)
+    if (c->tracking > SKY_TRACKING_MERGED_LAYERS)
         return set_error(SKY_ERR_INVALID_CONFIG, "unknown tracking mode");
     if (c->kernel > SKY_KERNEL_WAVEFRONT) return set_error(SKY_ERR_INVALID_CONFIG, "unknown kernel");
     if (!std::isfinite(c->observer_altitude_km))
@@ -163,23 +168,70 @@ DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
     return L;
 }
 
+// Pixels per work group of the persistent kernel: enough chains per group
+// (>= 1024) to amortise the group epilogue, at most 256 cells per group.
+uint32_t pixels_per_group(uint32_t bands, uint32_t spp) {
+    uint32_t p = (1024u + bands * spp - 1u) / (bands * spp);
+    p = std::max(1u, std::min(p, 256u / bands));
+    return p;
+}
+
 int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs* o, cudaStream_t stream,
                   bool timed) {
     DevLaunch L = make_launch(s, c);
     const uint64_t pixels = uint64_t(c->width) * c->height;
-    const uint64_t cells = pixels * s->dev.band_count;
-    (void)cells;
     cudaError_t e;
     const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
-    if (timed) cudaEventRecord(s->ev_start, stream);
-    e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "tracing kernel launch", e);
-    if (timed) cudaEventRecord(s->ev_stop, stream);
-    const uint32_t total_spp = (c->flags & SKY_FLAG_ACCUMULATE) ? c->sample_offset + c->spp : c->spp;
+    const uint32_t total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
     double* xyz = s->has_xyz ? o->xyz : nullptr;
     double* xyz_var = s->has_xyz ? o->xyz_var : nullptr;
-    e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
+    if (c->kernel == SKY_KERNEL_PLAIN) {
+        if (timed) cudaEventRecord(s->ev_start, stream);
+        e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate, stream);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "tracing kernel launch", e);
+        if (timed) cudaEventRecord(s->ev_stop, stream);
+        e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, stream);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
+        return SKY_OK;
+    }
+    const uint32_t B = s->dev.band_count;
+    DevJob job{};
+    job.S = s->dev;
+    job.L = L;
+    job.cell_sum = o->cell_sum;
+    job.cell_sumsq = o->cell_sumsq;
+    job.film = o->film;
+    job.xyz = xyz;
+    job.xyz_var = xyz_var;
+    job.accumulate = accumulate ? 1u : 0u;
+    job.total_spp = total_spp;
+    job.pixels_per_group = pixels_per_group(B, c->spp);
+    job.group_begin = 0;
+    job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
+    WaveLaunch w{};
+    w.jobs = s->jobs;
+    w.num_jobs = 1;
+    w.total_groups = job.group_count;
+    w.block_threads = kWaveBlockThreads;
+    w.tracking = c->tracking;
+    w.phase_sampling = c->phase_sampling;
+    w.work_counter = s->work_counter;
+    w.counters = o->counters;
+    w.status = o->status;
+    const uint32_t warps = kWaveBlockThreads / 32u;
+    const bool with_maj = c->tracking != SKY_TRACKING_MERGED_LAYERS;
+    w.layout = plan_stage_layout(s->dev, warps, job.pixels_per_group * B, with_maj, true);
+    w.staged = w.layout.total <= uint32_t(s->smem_optin);
+    if (!w.staged) w.layout = plan_stage_layout(s->dev, warps, job.pixels_per_group * B, with_maj, false);
+    w.smem_bytes = w.layout.total;
+    if ((e = cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return cuda_fail(SKY_ERR_COPY, "job upload", e);
+    if ((e = cudaMemsetAsync(s->work_counter, 0, sizeof(uint32_t), stream)) != cudaSuccess)
+        return cuda_fail(SKY_ERR_LAUNCH, "work counter reset", e);
+    if (timed) cudaEventRecord(s->ev_start, stream);
+    e = launch_trace_wavefront(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "persistent tracing kernel launch", e);
+    if (timed) cudaEventRecord(s->ev_stop, stream);
     return SKY_OK;
 }
 
@@ -228,7 +280,7 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
         stats->chains = uint64_t(cells) * c->spp;
         for (int i = 0; i < SKY_EVENT_COUNT; ++i) stats->events[i] = counters[i];
         stats->watchdog = status;
-        stats->kernel_used = SKY_KERNEL_PLAIN;
+        stats->kernel_used = c->kernel == SKY_KERNEL_PLAIN ? SKY_KERNEL_PLAIN : SKY_KERNEL_WAVEFRONT;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     if (status) return set_error(SKY_ERR_WATCHDOG, "GPU path watchdog was reached");
@@ -279,6 +331,11 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     size_t o_pv = reserve(h.phase_values.size() * sizeof(float));
     size_t o_pc = reserve(h.phase_cdf.size() * sizeof(float));
     size_t o_pp = reserve(h.phase_bin_pdf.size() * sizeof(float));
+    size_t o_tr = reserve(h.trk_radius.size() * sizeof(float));
+    size_t o_tm = reserve(h.trk_maj.size() * sizeof(float));
+    size_t o_tp = reserve(h.trk_map.size() * sizeof(uint16_t));
+    size_t o_tc = reserve(h.trk_count.size() * sizeof(uint32_t));
+    size_t o_to = reserve(h.trk_off.size() * sizeof(uint32_t));
     std::vector<unsigned char> host(off, 0);
     auto put = [&](size_t at, const void* src, size_t bytes) { std::memcpy(host.data() + at, src, bytes); };
     put(o_knot, h.knot_z.data(), h.knot_z.size() * sizeof(float));
@@ -291,6 +348,11 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     put(o_pv, h.phase_values.data(), h.phase_values.size() * sizeof(float));
     put(o_pc, h.phase_cdf.data(), h.phase_cdf.size() * sizeof(float));
     put(o_pp, h.phase_bin_pdf.data(), h.phase_bin_pdf.size() * sizeof(float));
+    put(o_tr, h.trk_radius.data(), h.trk_radius.size() * sizeof(float));
+    put(o_tm, h.trk_maj.data(), h.trk_maj.size() * sizeof(float));
+    put(o_tp, h.trk_map.data(), h.trk_map.size() * sizeof(uint16_t));
+    put(o_tc, h.trk_count.data(), h.trk_count.size() * sizeof(uint32_t));
+    put(o_to, h.trk_off.data(), h.trk_off.size() * sizeof(uint32_t));
     if ((e = cudaMalloc(&s->blob, off)) != cudaSuccess) {
         delete s;
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "scene table allocation", e);
@@ -312,7 +374,18 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->dev.phase_values = reinterpret_cast<const float*>(base + o_pv);
     s->dev.phase_cdf = reinterpret_cast<const float*>(base + o_pc);
     s->dev.phase_bin_pdf = reinterpret_cast<const float*>(base + o_pp);
+    s->dev.trk_radius = reinterpret_cast<const float*>(base + o_tr);
+    s->dev.trk_maj = reinterpret_cast<const float*>(base + o_tm);
+    s->dev.trk_map = reinterpret_cast<const uint16_t*>(base + o_tp);
+    s->dev.trk_count = reinterpret_cast<const uint32_t*>(base + o_tc);
+    s->dev.trk_off = reinterpret_cast<const uint32_t*>(base + o_to);
     s->has_xyz = h.has_xyz;
+    cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
+    if ((e = cudaMalloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
+        (e = cudaMalloc(&s->work_counter, sizeof(uint32_t))) != cudaSuccess) {
+        sky_cuda_scene_destroy(s);
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "job table allocation", e);
+    }
     if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&s->ev_start)) != cudaSuccess || (e = cudaEventCreate(&s->ev_stop)) != cudaSuccess) {
         sky_cuda_scene_destroy(s);
@@ -327,6 +400,8 @@ void sky_cuda_scene_destroy(SkyScene* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_workspace(s);
+    cudaFree(s->jobs);
+    cudaFree(s->work_counter);
     cudaFree(s->blob);
     if (s->ev_start) cudaEventDestroy(s->ev_start);
     if (s->ev_stop) cudaEventDestroy(s->ev_stop);

@@ -181,6 +181,57 @@ __device__ __forceinline__ float next_segment_end(const DevScene& S, const RayGe
     return next_t;
 }
 
+// ---- merged tracking grid (SKY_TRACKING_MERGED_LAYERS) -------------------------------
+
+struct MergedGrid {
+    const float* radius;    // [count + 1] shell radii
+    const float* maj;       // [count]
+    const uint16_t* map;    // [layers] uniform layer -> merged layer
+    int count;
+};
+
+__device__ __forceinline__ MergedGrid merged_grid(const DevScene& S, uint32_t band) {
+    MergedGrid G;
+    const uint32_t off = S.trk_off[band];
+    G.radius = S.trk_radius + off;
+    G.maj = S.trk_maj + off;
+    G.map = S.trk_map + band * S.layer_count;
+    G.count = int(S.trk_count[band]);
+    return G;
+}
+
+__device__ __forceinline__ int merged_layer_at(const DevScene& S, const MergedGrid& G, float alt) {
+    int k = min(max(int(alt * S.inv_layer_dz), 0), int(S.layer_count) - 1);
+    return int(G.map[k]);
+}
+
+// The next shell crossing of merged layer m after t: inbound rays (s = t + b
+// < 0) that reach the lower shell leave through it (dir -1); otherwise the
+// ray leaves through the upper shell (dir +1); dir 0 when the boundary
+// (ground / top, t_max) comes first.  One square root per crossing.
+__device__ __forceinline__ float merged_crossing(const MergedGrid& G, const RayGeo& g, int m, float t, float t_max,
+                                                 int& dir) {
+    dir = 0;
+    float tn = t_max;
+    if (t + g.b < 0.0f && m > 0) {
+        float r = G.radius[m];
+        if (g.p < r) {
+            tn = -sqrtf((r - g.p) * (r + g.p)) - g.b;
+            dir = -1;
+        }
+    }
+    if (dir == 0 && m + 1 < G.count) {
+        float r = G.radius[m + 1];
+        tn = sqrtf(fmaxf((r - g.p) * (r + g.p), 0.0f)) - g.b;
+        dir = 1;
+    }
+    if (tn >= t_max) {
+        tn = t_max;
+        dir = 0;
+    }
+    return fmaxf(tn, t);
+}
+
 // ---- medium ---------------------------------------------------------------------------
 
 // Knot interval containing `alt` (alt in [0, top]).

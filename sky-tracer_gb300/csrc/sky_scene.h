@@ -81,6 +81,16 @@ struct DevScene {
     const float* phase_values;         // [species][B][bins]
     const float* phase_cdf;            // [species][B][bins]
     const float* phase_bin_pdf;        // [species][B][bins]
+    // Merged tracking grid (SKY_TRACKING_MERGED_LAYERS): per band, the
+    // merged layers' shell radii, majorants, and the map from a uniform
+    // majorant layer to the merged layer that contains it.
+    const float* trk_radius;           // [trk_off[b] + m], m <= count: lower shell radius of merged layer m
+    const float* trk_maj;              // [trk_off[b] + m], m < count: majorant of merged layer m
+    const uint16_t* trk_map;           // [B][L]: uniform layer -> merged layer
+    const uint32_t* trk_count;         // [B]: merged layers of the band
+    const uint32_t* trk_off;           // [B]: row offset of the band in trk_radius / trk_maj
+    uint32_t trk_total;                // entries in trk_radius / trk_maj
+    float inv_layer_dz;                // layers / top
 };
 
 // Per-launch constants.
@@ -102,6 +112,26 @@ struct DevLaunch {
     float lut_forward[3];
     float lut_side[3];
     float inv_width, inv_height;
+};
+
+// One render inside a persistent launch: its scene (tables may be shared
+// with other jobs; only the sun differs across an elevation sweep), its
+// launch constants, its outputs and its range of work groups.  A work group
+// is `pixels_per_group` consecutive pixels x all bands x all samples.
+struct DevJob {
+    DevScene S;
+    DevLaunch L;
+    double* cell_sum;
+    double* cell_sumsq;
+    float* film;
+    double* xyz;
+    double* xyz_var;
+    uint32_t accumulate;
+    uint32_t total_spp;         // samples behind the sums after this launch
+    uint32_t pixels_per_group;
+    uint32_t group_begin;       // first global group index of the job
+    uint32_t group_count;
+    uint32_t _pad;
 };
 
 }  // namespace sky

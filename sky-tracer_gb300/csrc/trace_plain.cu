@@ -19,9 +19,50 @@ namespace {
 // delta_transmittance, sky_trace.wgsl:405-475).  Returns true at a real
 // collision (t_hit set).  kTracking selects the reference's per-segment
 // restart or the residual carry (same distribution, fewer draws).
+// Residual-carry delta tracking over the band's merged tracking grid.
+__device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo& g, float t_max, uint32_t band,
+                                                 Rng& rng, float& t_hit, Counters& n, bool& watchdog) {
+    const MergedGrid G = merged_grid(S, band);
+    const float2* sig_row = S.sigma_t + band * S.knot_count;
+    float t = 0.0f;
+    int m = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_max), S.ground_radius));
+    int dir;
+    float t_seg = merged_crossing(G, g, m, t, t_max, dir);
+    float maj = __ldg(G.maj + m);
+    ++n.e[SKY_EVENT_SEGMENT];
+    float tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+    uint32_t guard = 0;
+    for (;;) {
+        float dt = tau / maj;
+        if (t + dt < t_seg) {
+            t = t + dt;
+            ++n.e[SKY_EVENT_TRACK_STEP];
+            float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
+            if (rng.next() * maj < sig) {
+                t_hit = t;
+                return true;
+            }
+            tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+        } else {
+            if (dir == 0) return false;
+            if (++guard > 100000u) {
+                watchdog = true;
+                return false;
+            }
+            tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
+            t = t_seg;
+            m += dir;
+            t_seg = merged_crossing(G, g, m, t, t_max, dir);
+            maj = __ldg(G.maj + m);
+            ++n.e[SKY_EVENT_SEGMENT];
+        }
+    }
+}
+
 template <int kTracking>
 __device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, float t_max, uint32_t band, Rng& rng,
                                           float& t_hit, Counters& n, bool& watchdog) {
+    if (kTracking == SKY_TRACKING_MERGED_LAYERS) return track_ray_merged(S, g, t_max, band, rng, t_hit, n, watchdog);
     const float* maj_row = S.majorants + band * S.layer_count;
     const float2* sig_row = S.sigma_t + band * S.knot_count;
     float t = 0.0f;
@@ -264,6 +305,8 @@ cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* ce
     SKY_PLAIN_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_TABULATED)
     SKY_PLAIN_CASE(SKY_TRACKING_RESIDUAL_CARRY, SKY_PHASE_ISOTROPIC)
     SKY_PLAIN_CASE(SKY_TRACKING_RESIDUAL_CARRY, SKY_PHASE_TABULATED)
+    SKY_PLAIN_CASE(SKY_TRACKING_MERGED_LAYERS, SKY_PHASE_ISOTROPIC)
+    SKY_PLAIN_CASE(SKY_TRACKING_MERGED_LAYERS, SKY_PHASE_TABULATED)
 #undef SKY_PLAIN_CASE
     return cudaErrorInvalidValue;
 }

@@ -6,15 +6,15 @@ include/sky_cuda.h; this package mirrors the reference's host interface
 """
 
 from ._abi import (FLAG_ACCUMULATE, KERNEL_AUTO, KERNEL_PLAIN, KERNEL_WAVEFRONT, PHASE_ISOTROPIC, PHASE_TABULATED,
-                   PROJECTION_PANORAMA, PROJECTION_SKY_VIEW_LUT, TRACKING_RESIDUAL_CARRY, TRACKING_SEGMENT_RESTART,
-                   RenderWatchdog, SkyCudaError, load_library)
+                   PROJECTION_PANORAMA, PROJECTION_SKY_VIEW_LUT, TRACKING_MERGED_LAYERS, TRACKING_RESIDUAL_CARRY,
+                   TRACKING_SEGMENT_RESTART, RenderWatchdog, SkyCudaError, load_library)
 from .render import Film, GpuScene, RenderConfig, RenderStats, render
 from .scene import (Scene, SceneError, SyntheticAtmosphere, compute_majorant_grid, load_scene_data,
                     sun_from_degrees, synthetic_scene, wavelengths)
 
 __all__ = [
     "FLAG_ACCUMULATE", "KERNEL_AUTO", "KERNEL_PLAIN", "KERNEL_WAVEFRONT", "PHASE_ISOTROPIC", "PHASE_TABULATED",
-    "PROJECTION_PANORAMA", "PROJECTION_SKY_VIEW_LUT", "TRACKING_RESIDUAL_CARRY", "TRACKING_SEGMENT_RESTART",
+    "PROJECTION_PANORAMA", "PROJECTION_SKY_VIEW_LUT", "TRACKING_MERGED_LAYERS", "TRACKING_RESIDUAL_CARRY", "TRACKING_SEGMENT_RESTART",
     "RenderWatchdog", "SkyCudaError", "load_library", "Film", "GpuScene", "RenderConfig", "RenderStats", "render",
     "Scene", "SceneError", "SyntheticAtmosphere", "compute_majorant_grid", "load_scene_data", "sun_from_degrees",
     "synthetic_scene", "wavelengths",

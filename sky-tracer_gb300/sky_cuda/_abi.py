@@ -36,6 +36,7 @@ PHASE_ISOTROPIC = 0
 PHASE_TABULATED = 1
 TRACKING_SEGMENT_RESTART = 0
 TRACKING_RESIDUAL_CARRY = 1
+TRACKING_MERGED_LAYERS = 2
 KERNEL_AUTO = 0
 KERNEL_PLAIN = 1
 KERNEL_WAVEFRONT = 2

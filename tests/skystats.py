@@ -24,6 +24,24 @@ def zscores(xyz_a, var_a, xyz_b, var_b, floor=1e-30):
     return (xyz_a - xyz_b) / np.sqrt(np.maximum(var_a + var_b, floor))
 
 
+def regular_pixels(xyz, var, factor=10.0):
+    """Pixels whose relative standard error of Y is at most `factor` times the
+    median: excludes the sun disc, where a rare hit of the 0.27-degree sun
+    (radiance ~1e5 times the sky) dominates both the mean and the variance."""
+    rel = np.sqrt(np.maximum(var[:, 1], 0)) / np.maximum(np.abs(xyz[:, 1]), 1e-30)
+    return rel <= factor * np.median(rel)
+
+
+def relative_bias(xyz_a, var_a, xyz_b, var_b):
+    """Signed relative difference of the summed XYZ over regular pixels of
+    both images, and its standard error."""
+    keep = regular_pixels(xyz_a, var_a) & regular_pixels(xyz_b, var_b)
+    d = (xyz_a[keep] - xyz_b[keep]).sum(axis=0)
+    ref = xyz_b[keep].sum(axis=0)
+    se = np.sqrt((var_a[keep] + var_b[keep]).sum(axis=0))
+    return d / ref, se / np.abs(ref)
+
+
 def parity_report(xyz_a, var_a, xyz_b, var_b, bright_fraction=1e-3):
     """z-scores on pixels whose Y is not below bright_fraction * p99(Y)
     (the exclusion rule of the 1 % error metric), and the mean relative
@@ -33,7 +51,10 @@ def parity_report(xyz_a, var_a, xyz_b, var_b, bright_fraction=1e-3):
     z = zscores(xyz_a[keep], var_a[keep], xyz_b[keep], var_b[keep])
     rel = np.abs(xyz_a[keep] - xyz_b[keep]) / np.maximum(np.abs(xyz_b[keep]), 1e-30)
     mean_rel = float(np.abs(xyz_a[keep] - xyz_b[keep]).sum() / np.abs(xyz_b[keep]).sum())
+    bias, bias_se = relative_bias(xyz_a, var_a, xyz_b, var_b)
     return {
+        "bias_xyz": [float(v) for v in bias],
+        "bias_se_xyz": [float(v) for v in bias_se],
         "pixels": int(keep.sum()),
         "frac_beyond_3se": float(np.mean(np.abs(z) > 3.0)),
         "max_abs_z": float(np.max(np.abs(z))) if z.size else 0.0,
