@@ -175,7 +175,8 @@ def cpu_baseline_run(w, args, budget_s):
     from sky_cuda import RenderConfig
     sky_oracle.load()
     scene = make_scene(w, 0)
-    cfg = make_config(w, args, 0)
+    # the reference algorithm: layered delta tracking restarted per segment
+    cfg = RenderConfig(**{**make_config(w, args, 0).__dict__, "tracking": 0})
     threads = os.cpu_count() or 1
     # pilot: one row at 1/8 of the samples to size the sample
     pilot = RenderConfig(**{**cfg.__dict__, "spp": max(1, cfg.spp // 8)})
