@@ -49,6 +49,9 @@ WORKLOADS = {
                                       rr_start_depth=8, max_orders=0),
     "plain-64x32-32wl-64spp": dict(width=64, height=32, lam=(380.0, 780.0, 32), spp=64, sun=10.0,
                                    rr_start_depth=0, max_orders=16),
+    # the production workload at 1/16 of the pixels and 1/4 of the samples: profiling case
+    "profile-128x64-81wl-64spp": dict(width=128, height=64, lam=(380.0, 780.0, 81), spp=64, sun=5.0,
+                                      rr_start_depth=8, max_orders=0),
 }
 DEFAULT_WORKLOAD = "plain-512x256-81wl-256spp"
 
@@ -63,6 +66,7 @@ def parse_args():
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-peak", action="store_true", help="skip the SGEMM FP32-peak measurement")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -304,20 +308,20 @@ def main():
     # end to end through the one-shot C ABI: host tables in, host film out
     desc_bytes = sum(a.nbytes for a in scene._keep) if scene._keep else 0
     e2e_times = []
-    for i in range(args.e2e_steps + 1):
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         t0 = time.perf_counter()
         render(scene, cfg)
         dt = time.perf_counter() - t0
         if i > 0:
             e2e_times.append(dt)
     desc_bytes = sum(a.nbytes for a in scene._keep)
-    e2e_s = statistics.median(e2e_times)
+    e2e_s = statistics.median(e2e_times) if e2e_times else float("nan")
     if world > 1:
         t = torch.tensor([e2e_s], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
 
-    peak = measure_fp32_peak(torch, dev) if rank == 0 else None
+    peak = measure_fp32_peak(torch, dev) if rank == 0 and not args.no_peak else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample = cpu_baseline_run(w, args, args.cpu_seconds)
@@ -335,7 +339,8 @@ def main():
                        "tracking": ("segment-restart", "residual-carry", "merged-layers")[cfg.tracking],
                        "phase_sampling": "tabulated", "kernel": ("persistent", "plain", "persistent")[cfg.kernel],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}"},
-            "e2e": {"value": world * chains / e2e_s, "unit": "chains/s", "h2d_bytes_per_step": int(desc_bytes),
+            "e2e": {"value": world * chains / e2e_s if e2e_times else None, "unit": "chains/s",
+                    "h2d_bytes_per_step": int(desc_bytes),
                     "d2h_bytes_per_step": int(cells * 4 + 8 * 8 + 4)},
             "time_to_1pct_xyz_s": t1pct, "p95_rel_se_at_spp": p95,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

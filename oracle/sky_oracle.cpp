@@ -133,7 +133,38 @@ struct Ctx {
     V3 sun;
     float sun_angular_radius_rad, ground_albedo;
     std::vector<float> cdf, bin_pdf;  // phase.rs:105-126 layout [species][band][bin]
+    // merged tracking grid (tracking mode 2): per band, merged-layer bounds
+    // (altitudes of the first uniform layer of each group, then top), majorant
+    // of each group, and the group of every uniform layer
+    std::vector<std::vector<float>> merged_lo, merged_maj;
+    std::vector<std::vector<uint32_t>> merged_of;
 };
+
+// Grouping of uniform majorant layers for tracking mode 2: contiguous groups
+// minimising sum_groups [0.25 + dz * sum_k (max_group - maj_k)] (the cost of a
+// layer crossing against the expected extra null collisions of a vertical ray).
+std::vector<uint32_t> merge_groups(const float* maj, uint32_t L, float dz) {
+    std::vector<double> best(L + 1, 0.0);
+    std::vector<uint32_t> from(L + 1, 0);
+    for (uint32_t j = 1; j <= L; ++j) {
+        best[j] = 1e300;
+        double mx = 0.0, sum = 0.0;
+        for (uint32_t i = j; i-- > 0;) {
+            double m = std::max(double(maj[i]), 1e-8);
+            mx = std::max(mx, m);
+            sum += m;
+            double c = best[i] + 0.25 + (mx * double(j - i) - sum) * double(dz);
+            if (c < best[j]) {
+                best[j] = c;
+                from[j] = i;
+            }
+        }
+    }
+    std::vector<uint32_t> starts;
+    for (uint32_t j = L; j > 0; j = from[j]) starts.push_back(from[j]);
+    std::reverse(starts.begin(), starts.end());
+    return starts;
+}
 
 // ---- phase.rs sampling tables: phase.rs:105-146 ----------------------------
 
@@ -245,6 +276,21 @@ inline float next_majorant_segment_end(const Ctx& c, const Ray& ray, float t,
     return next_t;
 }
 
+// Tracking mode 2: next_majorant_segment_end over the merged grid, with the
+// reference's candidate rule (both roots of both shells beyond t + epsilon).
+inline float merged_segment_end(const Ctx& c, const Ray& ray, uint32_t band, float t, float t_max, float& majorant) {
+    float probe_t = std::min(t + RAY_EPSILON_KM, t_max);
+    uint32_t k = layer_for_altitude(c, altitude_km(c, ray_at(ray, probe_t)));
+    uint32_t g = c.merged_of[band][k];
+    float next_t = t_max;
+    next_t = boundary_candidate(c, ray, t, next_t, c.merged_lo[band][g]);
+    next_t = boundary_candidate(c, ray, t, next_t, c.merged_lo[band][g + 1]);
+    float probe2 = std::min(t + RAY_EPSILON_KM, next_t);
+    uint32_t k2 = layer_for_altitude(c, altitude_km(c, ray_at(ray, probe2)));
+    majorant = c.merged_maj[band][c.merged_of[band][k2]];
+    return next_t;
+}
+
 // ---- medium: sky_trace.wgsl:296-403 ----------------------------------------
 
 inline float lerp(float a, float b, float t) { return a * (1.0f - t) + b * t; }  // :296-298
@@ -337,12 +383,17 @@ CollisionSample sample_real_collision(const Ctx& c, const Ray& ray, float t_max,
             return CollisionSample{false, 0.0f, Coeffs{}};
         }
         guard++;
-        float segment_end = next_majorant_segment_end(c, ray, t, t_max);
+        float segment_end, majorant;
+        if (c.tracking == SKY_TRACKING_MERGED_LAYERS) {
+            segment_end = merged_segment_end(c, ray, band, t, t_max, majorant);
+        } else {
+            segment_end = next_majorant_segment_end(c, ray, t, t_max);
+            uint32_t layer = layer_for_altitude(
+                c, altitude_km(c, ray_at(ray, std::min(t + RAY_EPSILON_KM, segment_end))));
+            majorant = majorant_for_layer(c, band, layer);
+        }
         n.e[SKY_EVENT_SEGMENT]++;
-        uint32_t layer = layer_for_altitude(
-            c, altitude_km(c, ray_at(ray, std::min(t + RAY_EPSILON_KM, segment_end))));
-        float majorant = majorant_for_layer(c, band, layer);
-        if (c.tracking == SKY_TRACKING_RESIDUAL_CARRY) {
+        if (c.tracking != SKY_TRACKING_SEGMENT_RESTART) {
             for (;;) {
                 if (need_draw) {
                     tau = -std::log(std::max(1.0f - rng_f32(rng), 0.0000001f));
@@ -391,12 +442,17 @@ float delta_transmittance(const Ctx& c, const Ray& ray, float t_max, uint32_t ba
             return 0.0f;
         }
         guard++;
-        float segment_end = next_majorant_segment_end(c, ray, t, t_max);
+        float segment_end, majorant;
+        if (c.tracking == SKY_TRACKING_MERGED_LAYERS) {
+            segment_end = merged_segment_end(c, ray, band, t, t_max, majorant);
+        } else {
+            segment_end = next_majorant_segment_end(c, ray, t, t_max);
+            uint32_t layer = layer_for_altitude(
+                c, altitude_km(c, ray_at(ray, std::min(t + RAY_EPSILON_KM, segment_end))));
+            majorant = majorant_for_layer(c, band, layer);
+        }
         n.e[SKY_EVENT_SEGMENT]++;
-        uint32_t layer = layer_for_altitude(
-            c, altitude_km(c, ray_at(ray, std::min(t + RAY_EPSILON_KM, segment_end))));
-        float majorant = majorant_for_layer(c, band, layer);
-        if (c.tracking == SKY_TRACKING_RESIDUAL_CARRY) {
+        if (c.tracking != SKY_TRACKING_SEGMENT_RESTART) {
             for (;;) {
                 if (need_draw) {
                     tau = -std::log(std::max(1.0f - rng_f32(rng), 0.0000001f));
@@ -808,6 +864,29 @@ bool make_ctx(const SkySceneDesc* s, const SkyRenderConfig* cfg, Ctx& c) {
     c.ground_albedo = s->ground_albedo;
     if (c.phase_sampling == SKY_PHASE_TABULATED)
         build_sampling_tables(s->phase_values, s->band_count, s->phase_bins, c.cdf, c.bin_pdf);
+    if (c.tracking == SKY_TRACKING_MERGED_LAYERS) {
+        const uint32_t L = s->majorant_layers;
+        const float dz = c.top_altitude_km / float(L);
+        c.merged_lo.resize(s->band_count);
+        c.merged_maj.resize(s->band_count);
+        c.merged_of.resize(s->band_count);
+        for (uint32_t b = 0; b < s->band_count; ++b) {
+            const float* maj = s->majorants_km_inv + size_t(b) * L;
+            std::vector<uint32_t> starts = merge_groups(maj, L, dz);
+            c.merged_of[b].assign(L, 0);
+            for (uint32_t g = 0; g < starts.size(); ++g) {
+                uint32_t k1 = g + 1 < starts.size() ? starts[g + 1] : L;
+                float mx = 0.0f;
+                for (uint32_t k = starts[g]; k < k1; ++k) {
+                    mx = std::max(mx, std::max(maj[k], 0.00000001f));
+                    c.merged_of[b][k] = g;
+                }
+                c.merged_lo[b].push_back(float(starts[g]) * dz);
+                c.merged_maj[b].push_back(mx);
+            }
+            c.merged_lo[b].push_back(c.top_altitude_km);
+        }
+    }
     return true;
 }
 

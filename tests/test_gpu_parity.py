@@ -15,7 +15,8 @@ from skystats import parity_report, xyz_from_sums
 
 pytestmark = pytest.mark.gpu
 
-MODES = [(t, p) for t in (_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY)
+MODES = [(t, p) for t in (_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY,
+                          _abi.TRACKING_MERGED_LAYERS)
          for p in (_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED)]
 
 
@@ -83,7 +84,7 @@ def test_wavefront_matches_plain_chains(gpu, cfg0_scene, tracking, phase):
     np.testing.assert_allclose(ca[:7], cb[:7], rtol=2e-3)
 
 
-@pytest.mark.parametrize("tracking,phase", [MODES[0], MODES[3], (_abi.TRACKING_MERGED_LAYERS, _abi.PHASE_TABULATED)])
+@pytest.mark.parametrize("tracking,phase", [MODES[0], MODES[3], MODES[5]])
 def test_statistical_parity_cfg0(gpu, cfg0_scene, tracking, phase):
     """The CPU-runnable benchmark scene (64x32, 32 bands, 64 spp): per-pixel
     XYZ of GPU and oracle within 3 combined standard errors, and no bias."""
@@ -91,7 +92,7 @@ def test_statistical_parity_cfg0(gpu, cfg0_scene, tracking, phase):
                        tracking=tracking, max_orders=16)
     with GpuScene(cfg0_scene) as gs:
         gs_, gq, _, st = gpu_sums(gs, cfg)
-    cfg_o = RenderConfig(**{**cfg.__dict__, "seed": 12345, "tracking": min(tracking, 1)})
+    cfg_o = RenderConfig(**{**cfg.__dict__, "seed": 12345})
     os_, oq, _, wd = oracle.render(cfg0_scene, cfg_o)
     assert st == 0 and wd == 0
     xg, vg = xyz_from_sums(gs_, gq, cfg.spp, cfg0_scene.band_xyz)
@@ -107,12 +108,11 @@ def test_statistical_parity_cfg0(gpu, cfg0_scene, tracking, phase):
 def test_high_spp_mean_relative_error(gpu, data_dir):
     """Matched high sample counts: mean relative XYZ error under 0.5 %."""
     scene = synthetic_scene(wavelengths(400, 700, 8), data_dir, sun_elevation_deg=10.0)
-    cfg = RenderConfig(width=32, height=16, spp=4096, phase_sampling=_abi.PHASE_TABULATED,
+    cfg = RenderConfig(width=64, height=32, spp=4096, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS, max_orders=16)
     with GpuScene(scene) as gs:
         gs_, gq, _, _ = gpu_sums(gs, cfg)
-    os_, oq, _, _ = oracle.render(scene, RenderConfig(**{**cfg.__dict__, "seed": 4242,
-                                                         "tracking": _abi.TRACKING_RESIDUAL_CARRY}))
+    os_, oq, _, _ = oracle.render(scene, RenderConfig(**{**cfg.__dict__, "seed": 4242}))
     xg, vg = xyz_from_sums(gs_, gq, cfg.spp, scene.band_xyz)
     xo, vo = xyz_from_sums(os_, oq, cfg.spp, scene.band_xyz)
     r = parity_report(xg, vg, xo, vo)
