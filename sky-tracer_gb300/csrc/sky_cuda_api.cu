@@ -41,6 +41,8 @@ struct SkyScene {
     DevJob* jobs = nullptr;
     uint32_t* work_counter = nullptr;
     int smem_optin = 0;
+    bool stage_tables = false;        // stage the scene tables in shared memory
+    uint32_t max_blocks_per_sm = 0;   // 0 = occupancy limit
 };
 
 namespace {
@@ -169,10 +171,11 @@ DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
 }
 
 // Pixels per work group of the persistent kernel: enough chains per group
-// (>= 1024) to amortise the group epilogue, at most 256 cells per group.
+// (>= 4 pools) to keep the ring short, at most kPoolMaxCells cells.
 uint32_t pixels_per_group(uint32_t bands, uint32_t spp) {
-    uint32_t p = (1024u + bands * spp - 1u) / (bands * spp);
-    p = std::max(1u, std::min(p, 256u / bands));
+    const uint32_t want = 4u * kPoolSlots;
+    uint32_t p = (want + bands * spp - 1u) / (bands * spp);
+    p = std::max(1u, std::min(p, kPoolMaxCells / bands));
     return p;
 }
 
@@ -208,28 +211,25 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     job.pixels_per_group = pixels_per_group(B, c->spp);
     job.group_begin = 0;
     job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
-    WaveLaunch w{};
+    PoolLaunch w{};
     w.jobs = s->jobs;
     w.num_jobs = 1;
     w.total_groups = job.group_count;
-    w.block_threads = kWaveBlockThreads;
     w.tracking = c->tracking;
     w.phase_sampling = c->phase_sampling;
     w.work_counter = s->work_counter;
     w.counters = o->counters;
     w.status = o->status;
-    const uint32_t warps = kWaveBlockThreads / 32u;
     const bool with_maj = c->tracking != SKY_TRACKING_MERGED_LAYERS;
-    w.layout = plan_stage_layout(s->dev, warps, job.pixels_per_group * B, with_maj, true);
-    w.staged = w.layout.total <= uint32_t(s->smem_optin);
-    if (!w.staged) w.layout = plan_stage_layout(s->dev, warps, job.pixels_per_group * B, with_maj, false);
-    w.smem_bytes = w.layout.total;
+    w.layout = plan_pool_layout(s->dev, with_maj, s->stage_tables);
+    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false);
+    w.max_blocks_per_sm = s->max_blocks_per_sm;
     if ((e = cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
         return cuda_fail(SKY_ERR_COPY, "job upload", e);
     if ((e = cudaMemsetAsync(s->work_counter, 0, sizeof(uint32_t), stream)) != cudaSuccess)
         return cuda_fail(SKY_ERR_LAUNCH, "work counter reset", e);
     if (timed) cudaEventRecord(s->ev_start, stream);
-    e = launch_trace_wavefront(w, stream);
+    e = launch_trace_pool(w, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "persistent tracing kernel launch", e);
     if (timed) cudaEventRecord(s->ev_stop, stream);
     return SKY_OK;

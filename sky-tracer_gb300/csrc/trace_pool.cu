@@ -1,0 +1,862 @@
+// trace_pool.cu — persistent wavefront tracer: a pool of paths per block,
+// regrouped by the work they need next.
+//
+// The plain kernel runs every chain to completion inside one lane, so the
+// warp executes the union of 32 different paths (profiled: ~5 of 32 lanes
+// active per instruction).  Here each block keeps kPoolSlots paths in shared
+// memory (structure of arrays) and advances all of them in lock-step phases:
+//
+//   generate  free slots take the next chains of the block's work groups and
+//             build camera rays (sky_trace.wgsl:795-807);
+//   trace     every ray that needs delta tracking (camera/continuation rays
+//             and sun shadow rays alike) is put on one compacted list, and
+//             lanes drain the list with per-lane refill, so the tracking loop
+//             (sky_trace.wgsl:405-475) runs with nearly full warps;
+//   shade     finished rays are split into three lists — shadow results,
+//             real collisions, ground/escape — and each list is processed by
+//             all threads: NEE accumulation, scattering, phase sampling,
+//             Russian roulette and the next ray (sky_trace.wgsl:566-776).
+//
+// Each chain's random stream is consumed in exactly the order of the plain
+// kernel (and of the reference shader), so both kernels trace the same paths.
+//
+// Work groups: `pixels_per_group` pixels x all bands x all samples of one
+// job, taken from a global counter; up to kRing groups are in flight per
+// block, each with FP64 per-cell sums in shared memory.  When a group's last
+// chain finishes the block writes its cell sums, mean film and per-pixel CIE
+// XYZ with its variance (warp-shuffle reductions over the bands).
+
+#include <algorithm>
+
+#include "sky_device.cuh"
+#include "trace_kernels.h"
+
+namespace sky {
+namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kThreads = kPoolThreads;
+constexpr uint32_t kWarps = kThreads / 32u;
+constexpr uint32_t kSlots = kPoolSlots;
+constexpr uint32_t kRing = kPoolRing;
+constexpr uint32_t kMaxCells = kPoolMaxCells;
+// Upper bound on block iterations for one launch-lifetime of a block without
+// progress; exceeding it sets status bit 2 instead of running on.
+constexpr uint32_t kMaxIdleIterations = 1u << 24;
+
+// slot meta word
+constexpr uint32_t M_STATE = 0x3u;  // 0 free, 1 needs tracking, 2 tracked
+constexpr uint32_t S_FREE = 0u, S_TRACE = 1u, S_TRACED = 2u;
+constexpr uint32_t M_HIT = 1u << 2;
+constexpr uint32_t M_SHADOW = 1u << 3;
+constexpr uint32_t M_GROUND = 1u << 4;
+constexpr uint32_t M_EXIT = 1u << 5;
+constexpr uint32_t M_LIGHT_SHIFT = 8u;
+constexpr uint32_t M_DEPTH_SHIFT = 16u;
+
+enum SlotField : uint32_t {
+    F_CELL, F_K0, F_K1, F_K2, F_DIM, F_META,
+    F_OX, F_OY, F_OZ, F_DX, F_DY, F_DZ, F_THR, F_RAD,
+    F_PX, F_PY, F_PZ, F_LX, F_LY, F_LZ, F_ALT, F_NEE,
+    F_GB, F_GP, F_GR, F_TMAX, F_T, F_COUNT
+};
+
+struct RingEntry {
+    unsigned long long pixel0;
+    uint32_t job, total, issued, done, cells, npix, active, _pad;
+};
+
+struct PoolHeader {
+    RingEntry ring[kRing];
+    uint32_t order[kRing];  // active ring entries, oldest first
+    uint32_t ring_count, no_more_work, fetch, _pad;
+    uint32_t list_count[4];
+    uint32_t warp_totals[kWarps];
+};
+
+struct PoolSmem {
+    PoolHeader* hdr;
+    DevJob* jobs;       // [kRing] job constants of the ring entries
+    double* acc;        // [kRing][kMaxCells][2]
+    uint32_t* slots;    // [F_COUNT][kSlots]
+    uint16_t* lists;    // [4][kSlots]
+    __device__ __forceinline__ uint32_t& u(uint32_t f, uint32_t s) const { return slots[f * kSlots + s]; }
+    __device__ __forceinline__ float& f(uint32_t fld, uint32_t s) const {
+        return reinterpret_cast<float*>(slots)[fld * kSlots + s];
+    }
+};
+
+// Registers of one path while a thread works on it.
+struct Path {
+    uint32_t slot, cell, ring, meta;
+    Rng rng;
+    V3 org, dir, pos, ldir;
+    float thr, rad, alt, nee, tmax, t;
+    RayGeo g;
+};
+
+__device__ __forceinline__ void load_path(const PoolSmem& P, uint32_t s, Path& p) {
+    p.slot = s;
+    const uint32_t c = P.u(F_CELL, s);
+    p.cell = c & 0xffffu;
+    p.ring = c >> 16;
+    p.rng.k0 = P.u(F_K0, s);
+    p.rng.k1 = P.u(F_K1, s);
+    p.rng.k2 = P.u(F_K2, s);
+    p.rng.dim = P.u(F_DIM, s);
+    p.meta = P.u(F_META, s);
+    p.org = mk(P.f(F_OX, s), P.f(F_OY, s), P.f(F_OZ, s));
+    p.dir = mk(P.f(F_DX, s), P.f(F_DY, s), P.f(F_DZ, s));
+    p.thr = P.f(F_THR, s);
+    p.rad = P.f(F_RAD, s);
+    p.pos = mk(P.f(F_PX, s), P.f(F_PY, s), P.f(F_PZ, s));
+    p.ldir = mk(P.f(F_LX, s), P.f(F_LY, s), P.f(F_LZ, s));
+    p.alt = P.f(F_ALT, s);
+    p.nee = P.f(F_NEE, s);
+    p.g.b = P.f(F_GB, s);
+    p.g.p = P.f(F_GP, s);
+    p.g.r0sq = P.f(F_GR, s);
+    p.tmax = P.f(F_TMAX, s);
+    p.t = P.f(F_T, s);
+}
+
+__device__ __forceinline__ void store_path(const PoolSmem& P, const Path& p) {
+    const uint32_t s = p.slot;
+    P.u(F_CELL, s) = p.cell | (p.ring << 16);
+    P.u(F_K0, s) = p.rng.k0;
+    P.u(F_K1, s) = p.rng.k1;
+    P.u(F_K2, s) = p.rng.k2;
+    P.u(F_DIM, s) = p.rng.dim;
+    P.u(F_META, s) = p.meta;
+    P.f(F_OX, s) = p.org.x;
+    P.f(F_OY, s) = p.org.y;
+    P.f(F_OZ, s) = p.org.z;
+    P.f(F_DX, s) = p.dir.x;
+    P.f(F_DY, s) = p.dir.y;
+    P.f(F_DZ, s) = p.dir.z;
+    P.f(F_THR, s) = p.thr;
+    P.f(F_RAD, s) = p.rad;
+    P.f(F_PX, s) = p.pos.x;
+    P.f(F_PY, s) = p.pos.y;
+    P.f(F_PZ, s) = p.pos.z;
+    P.f(F_LX, s) = p.ldir.x;
+    P.f(F_LY, s) = p.ldir.y;
+    P.f(F_LZ, s) = p.ldir.z;
+    P.f(F_ALT, s) = p.alt;
+    P.f(F_NEE, s) = p.nee;
+    P.f(F_GB, s) = p.g.b;
+    P.f(F_GP, s) = p.g.p;
+    P.f(F_GR, s) = p.g.r0sq;
+    P.f(F_TMAX, s) = p.tmax;
+    P.f(F_T, s) = p.t;
+}
+
+__device__ __forceinline__ uint32_t depth_of(uint32_t meta) { return meta >> M_DEPTH_SHIFT; }
+__device__ __forceinline__ uint32_t light_of(uint32_t meta) { return (meta >> M_LIGHT_SHIFT) & 0xffu; }
+__device__ __forceinline__ uint32_t with_light(uint32_t meta, uint32_t l) {
+    return (meta & ~(0xffu << M_LIGHT_SHIFT)) | (min(l, 255u) << M_LIGHT_SHIFT);
+}
+__device__ __forceinline__ uint32_t with_state(uint32_t meta, uint32_t st) { return (meta & ~M_STATE) | st; }
+
+// Delta tracking state along one ray (camera/continuation or shadow).
+struct Tracker {
+    RayGeo g;
+    float t, t_max, t_seg, tau, maj;
+    int m, mdir;
+    uint32_t guard;
+    bool need_draw;
+};
+
+template <int kTracking>
+__device__ __forceinline__ void track_begin(const DevScene& S, uint32_t band, Tracker& k, Rng& rng, Counters& n) {
+    k.t = 0.0f;
+    k.guard = 0;
+    k.need_draw = true;
+    k.mdir = 0;
+    k.m = 0;
+    k.t_seg = 0.0f;
+    k.tau = 0.0f;
+    k.maj = 1.0f;
+    if (kTracking == SKY_TRACKING_MERGED_LAYERS) {
+        const MergedGrid G = merged_grid(S, band);
+        k.m = merged_layer_at(S, G, altitude_at(k.g, fminf(kRayEpsilonKm, k.t_max), S.ground_radius));
+        k.t_seg = merged_crossing(G, k.g, k.m, 0.0f, k.t_max, k.mdir);
+        k.maj = G.maj[k.m];
+        ++n.e[SKY_EVENT_SEGMENT];
+        k.tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+        k.need_draw = false;
+    }
+}
+
+// One tracking action: 0 continue, 1 real collision at k.t, 2 reached
+// k.t_max.  Draw order identical to the plain kernel's track_ray().
+template <int kTracking>
+__device__ __forceinline__ int track_action(const DevScene& S, uint32_t band, Tracker& k, Rng& rng, Counters& n,
+                                           bool& watchdog) {
+    const float2* sig_row = S.sigma_t + band * S.knot_count;
+    if (kTracking == SKY_TRACKING_MERGED_LAYERS) {
+        const float dt = k.tau / k.maj;
+        if (k.t + dt < k.t_seg) {
+            k.t = k.t + dt;
+            ++n.e[SKY_EVENT_TRACK_STEP];
+            const float sig =
+                sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, altitude_at(k.g, k.t, S.ground_radius));
+            if (rng.next() * k.maj < sig) return 1;
+            k.tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+            return 0;
+        }
+        if (k.mdir == 0) return 2;
+        if (++k.guard > 100000u) {
+            watchdog = true;
+            return 2;
+        }
+        k.tau = fmaxf(k.tau - (k.t_seg - k.t) * k.maj, 0.0f);
+        k.t = k.t_seg;
+        k.m += k.mdir;
+        const MergedGrid G = merged_grid(S, band);
+        k.t_seg = merged_crossing(G, k.g, k.m, k.t, k.t_max, k.mdir);
+        k.maj = G.maj[k.m];
+        ++n.e[SKY_EVENT_SEGMENT];
+        return 0;
+    }
+    if (k.mdir == 0) {  // set up the next reference segment (sky_trace.wgsl:409-420)
+        if (k.t >= k.t_max) return 2;
+        if (k.guard > 100000u) {
+            watchdog = true;
+            return 2;
+        }
+        ++k.guard;
+        uint32_t layer;
+        k.t_seg = next_segment_end(S, k.g, k.t, k.t_max, layer);
+        k.maj = fmaxf(S.majorants[band * S.layer_count + layer], 0.00000001f);
+        ++n.e[SKY_EVENT_SEGMENT];
+        k.mdir = 1;
+        return 0;
+    }
+    if (kTracking == SKY_TRACKING_RESIDUAL_CARRY) {
+        if (k.need_draw) {
+            k.tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+            k.need_draw = false;
+        }
+        const float dt = k.tau / k.maj;
+        if (k.t + dt >= k.t_seg) {
+            k.tau = fmaxf(k.tau - (k.t_seg - k.t) * k.maj, 0.0f);
+            k.t = k.t_seg;
+            k.mdir = 0;
+            return 0;
+        }
+        k.t = k.t + dt;
+        k.need_draw = true;
+    } else {
+        if (k.t >= k.t_seg) {
+            k.t = k.t_seg;
+            k.mdir = 0;
+            return 0;
+        }
+        const float u = fmaxf(1.0f - rng.next(), 0.0000001f);
+        const float tn = k.t - __logf(u) / k.maj;
+        if (tn >= k.t_seg) {
+            k.t = k.t_seg;
+            k.mdir = 0;
+            return 0;
+        }
+        k.t = tn;
+    }
+    ++n.e[SKY_EVENT_TRACK_STEP];
+    const float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, altitude_at(k.g, k.t, S.ground_radius));
+    return rng.next() * k.maj < sig ? 1 : 0;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void copy_words(void* dst, const void* src, uint32_t bytes, uint32_t tid, uint32_t n) {
+    const uint32_t* s = static_cast<const uint32_t*>(src);
+    uint32_t* d = static_cast<uint32_t*>(dst);
+    for (uint32_t i = tid; i < bytes / 4u; i += n) d[i] = s[i];
+}
+
+// A path ends: its radiance joins its cell's FP64 sums and the slot frees.
+__device__ __forceinline__ void finish(const PoolSmem& P, Path& p, float result) {
+    const double rd = double(result);
+    double* a = P.acc + (size_t(p.ring) * kMaxCells + p.cell) * 2u;
+    atomicAdd(a, rd);
+    atomicAdd(a + 1, rd * rd);
+    atomicAdd(&P.hdr->ring[p.ring].done, 1u);
+    p.meta = S_FREE;
+}
+
+// Depth checks and the boundary of a new camera/continuation ray
+// (sky_trace.wgsl:709-717); leaves the path waiting for tracking or ends it.
+__device__ __forceinline__ void start_ray(const PoolSmem& P, const DevScene& S, const DevLaunch& L, Path& p,
+                                          Counters& n, bool& watchdog) {
+    const uint32_t depth = depth_of(p.meta);
+    if (depth >= L.watchdog_limit) {
+        watchdog = true;
+        finish(P, p, p.rad);
+        return;
+    }
+    if (L.max_orders != 0u && depth >= L.max_orders) {
+        finish(P, p, fmaxf(p.rad, 0.0f));
+        return;
+    }
+    p.g = ray_geo(p.org, p.dir);
+    ++n.e[SKY_EVENT_BOUNDARY];
+    float tb;
+    uint32_t kind;
+    if (!next_boundary(S, p.g, tb, kind)) {
+        finish(P, p, fmaxf(p.rad, 0.0f));
+        return;
+    }
+    p.tmax = tb;
+    p.meta = (p.meta & ~(M_STATE | M_SHADOW | M_HIT | M_EXIT)) | S_TRACE | (kind == 1u ? M_EXIT : 0u);
+}
+
+// Light samples of the current event (sky_trace.wgsl:566-608) until one needs
+// a shadow ray traced; then the continuation (:728-767) and the next ray.
+template <int kPhase>
+__device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const DevLaunch& L, Path& p, Counters& n,
+                                    bool& watchdog) {
+    const uint32_t band = p.cell % L.band_count;
+    const bool ground = (p.meta & M_GROUND) != 0u;
+    uint32_t light = light_of(p.meta);
+    while (light < L.direct_light_samples) {
+        p.ldir = sample_sun_cone(S, p.rng);
+        ++n.e[SKY_EVENT_NEE];
+        bool go = true;
+        if (ground) go = fmaxf(dot3(normalize_or_y(p.pos), p.ldir), 0.0f) > 0.0f;
+        if (go) {
+            p.g = ray_geo(madd(p.pos, p.ldir, kRayEpsilonKm), p.ldir);
+            ++n.e[SKY_EVENT_BOUNDARY];
+            float tb;
+            uint32_t kind;
+            if (next_boundary(S, p.g, tb, kind) && kind == 1u) {
+                p.tmax = tb;
+                p.meta = (with_light(p.meta, light) & ~(M_STATE | M_HIT)) | S_TRACE | M_SHADOW;
+                return;
+            }
+        }
+        ++light;
+    }
+    // continuation
+    const float l_sun = S.bands[band].solar_radiance;
+    (void)l_sun;
+    p.rad += p.thr * (p.nee * (1.0f / float(L.direct_light_samples)));
+    const uint32_t depth = depth_of(p.meta);
+    V3 nd;
+    if (!ground) {
+        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, p.alt);
+        if (kPhase == SKY_PHASE_TABULATED) {
+            p.thr *= sample_tabulated(S, c, band, p.dir, p.rng, nd);
+        } else {
+            nd = sample_isotropic(p.rng);
+            p.thr *= mixed_phase(S, c, band, dot3(p.dir, nd)) / kIsotropicPdf;
+        }
+    } else {
+        const V3 normal = normalize_or_y(p.pos);
+        float pdf;
+        nd = sample_cosine_hemisphere(normal, p.rng, pdf);
+        const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+        if (pdf <= 0.0f || cos_out <= 0.0f) {
+            finish(P, p, fmaxf(p.rad, 0.0f));
+            return;
+        }
+        p.thr *= S.ground_albedo * kInvPi * cos_out / pdf;
+    }
+    if (depth >= L.rr_start_depth) {
+        const float q = fminf(fmaxf(p.thr, 0.05f), 0.95f);
+        if (p.rng.next() > q) {
+            finish(P, p, fmaxf(p.rad, 0.0f));
+            return;
+        }
+        p.thr = p.thr / q;
+    }
+    p.org = madd(p.pos, nd, kRayEpsilonKm);
+    p.dir = nd;
+    if (p.rad < 0.0f || p.rad != p.rad || p.thr < 0.0f || p.thr != p.thr) {
+        finish(P, p, 0.0f);
+        return;
+    }
+    p.meta = (p.meta & 0xffffu & ~(0xffu << M_LIGHT_SHIFT) & ~M_GROUND) | ((depth + 1u) << M_DEPTH_SHIFT);
+    start_ray(P, S, L, p, n, watchdog);
+}
+
+// Build a compacted list of the slots satisfying pred (any order).
+template <class Pred>
+__device__ __forceinline__ void build_list(const PoolSmem& P, uint32_t which, Pred pred) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = 0; base < kSlots; base += kThreads) {
+        const uint32_t s = base + threadIdx.x;
+        const bool take = pred(s);
+        const uint32_t mask = __ballot_sync(kFull, take);
+        uint32_t at = 0;
+        if (lane == 0 && mask) at = atomicAdd(&P.hdr->list_count[which], __popc(mask));
+        at = __shfl_sync(kFull, at, 0);
+        if (take) P.lists[which * kSlots + at + __popc(mask & ((1u << lane) - 1u))] = uint16_t(s);
+    }
+}
+
+template <int kTracking, int kPhase>
+__global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict__ jobs, uint32_t num_jobs,
+                                                        uint32_t total_groups, PoolLayout lay,
+                                                        uint32_t* __restrict__ work_counter,
+                                                        unsigned long long* __restrict__ counters,
+                                                        uint32_t* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u;
+    const uint32_t warp = tid >> 5;
+    PoolSmem P;
+    P.hdr = reinterpret_cast<PoolHeader*>(smem + lay.header);
+    P.jobs = reinterpret_cast<DevJob*>(smem + lay.jobs);
+    P.acc = reinterpret_cast<double*>(smem + lay.acc);
+    P.slots = reinterpret_cast<uint32_t*>(smem + lay.slots);
+    P.lists = reinterpret_cast<uint16_t*>(smem + lay.lists);
+
+    if (lay.staged) {
+        const DevScene& S0 = jobs[0].S;
+        copy_words(smem + lay.knot_z, S0.knot_z, lay.knot_z_bytes, tid, kThreads);
+        copy_words(smem + lay.finder, S0.finder, lay.finder_bytes, tid, kThreads);
+        copy_words(smem + lay.sigma_t, S0.sigma_t, lay.sigma_t_bytes, tid, kThreads);
+        copy_words(smem + lay.bands, S0.bands, lay.bands_bytes, tid, kThreads);
+        copy_words(smem + lay.trk_radius, S0.trk_radius, lay.trk_bytes, tid, kThreads);
+        copy_words(smem + lay.trk_maj, S0.trk_maj, lay.trk_bytes, tid, kThreads);
+        copy_words(smem + lay.trk_map, S0.trk_map, lay.trk_map_bytes, tid, kThreads);
+        copy_words(smem + lay.trk_count, S0.trk_count, lay.trk_count_bytes, tid, kThreads);
+        copy_words(smem + lay.trk_off, S0.trk_off, lay.trk_count_bytes, tid, kThreads);
+        if (lay.majorants_bytes) copy_words(smem + lay.majorants, S0.majorants, lay.majorants_bytes, tid, kThreads);
+    }
+    for (uint32_t s = tid; s < kSlots; s += kThreads) P.u(F_META, s) = S_FREE;
+    if (tid == 0) {
+        for (uint32_t r = 0; r < kRing; ++r) P.hdr->ring[r].active = 0;
+        P.hdr->ring_count = 0;
+        P.hdr->no_more_work = 0;
+    }
+    __syncthreads();
+
+    Counters n;
+    n.clear();
+    bool watchdog = false;
+    bool stalled = false;
+    uint32_t idle_iterations = 0;
+
+    for (;;) {
+        // ---- ring maintenance: epilogues of finished groups, then refill ----
+        for (uint32_t q = 0; q < kRing; ++q) {
+            RingEntry& R = P.hdr->ring[q];
+            if (!(R.active && R.done == R.total)) continue;  // block-uniform
+            const DevJob& J = P.jobs[q];
+            const uint32_t B = J.L.band_count;
+            const double n_total = double(J.total_spp);
+            const double inv_n = 1.0 / n_total;
+            for (uint32_t px = warp; px < R.npix; px += kWarps) {
+                double xyz[3] = {0.0, 0.0, 0.0}, var[3] = {0.0, 0.0, 0.0};
+                const unsigned long long cell0 = (R.pixel0 + px) * B;
+                for (uint32_t b = lane; b < B; b += 32u) {
+                    const uint32_t c = px * B + b;
+                    double s = P.acc[(size_t(q) * kMaxCells + c) * 2u];
+                    double sq = P.acc[(size_t(q) * kMaxCells + c) * 2u + 1u];
+                    if (J.accumulate) {
+                        s += J.cell_sum[cell0 + b];
+                        if (J.cell_sumsq) sq += J.cell_sumsq[cell0 + b];
+                    }
+                    J.cell_sum[cell0 + b] = s;
+                    if (J.cell_sumsq) J.cell_sumsq[cell0 + b] = sq;
+                    const double mean = s * inv_n;
+                    if (J.film) J.film[cell0 + b] = fmaxf(float(mean), 0.0f);
+                    double var_mean = 0.0;
+                    if (J.total_spp > 1u) var_mean = fmax((sq - s * mean) / (n_total - 1.0), 0.0) * inv_n;
+                    const DevBand& bd = J.S.bands[b];
+#pragma unroll
+                    for (int ch = 0; ch < 3; ++ch) {
+                        const double w = double(bd.xyz[ch]);
+                        xyz[ch] += mean * w;
+                        var[ch] += var_mean * w * w;
+                    }
+                }
+                if (J.xyz || J.xyz_var) {
+#pragma unroll
+                    for (int ch = 0; ch < 3; ++ch) {
+                        xyz[ch] = warp_sum_d(xyz[ch]);
+                        var[ch] = warp_sum_d(var[ch]);
+                    }
+                    if (lane < 3u) {
+                        const double vx = lane == 0 ? xyz[0] : (lane == 1 ? xyz[1] : xyz[2]);
+                        const double vv = lane == 0 ? var[0] : (lane == 1 ? var[1] : var[2]);
+                        const unsigned long long pix = R.pixel0 + px;
+                        if (J.xyz) J.xyz[pix * 3 + lane] = vx;
+                        if (J.xyz_var) J.xyz_var[pix * 3 + lane] = vv;
+                    }
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                R.active = 0;
+                uint32_t w = 0;
+                for (uint32_t i = 0; i < P.hdr->ring_count; ++i)
+                    if (P.hdr->order[i] != q) P.hdr->order[w++] = P.hdr->order[i];
+                P.hdr->ring_count = w;
+            }
+            __syncthreads();
+        }
+        if (warp == 0) {
+            // fetch groups until the unissued chains cover the pool or the ring is full
+            for (;;) {
+                uint32_t pending = 0, count = P.hdr->ring_count;
+                for (uint32_t q = 0; q < kRing; ++q) {
+                    const RingEntry& R = P.hdr->ring[q];
+                    if (R.active) pending += R.total - R.issued;
+                }
+                if (pending >= kSlots || count >= kRing || P.hdr->no_more_work) break;
+                uint32_t group = 0;
+                if (lane == 0) group = atomicAdd(work_counter, 1u);
+                group = __shfl_sync(kFull, group, 0);
+                if (group >= total_groups) {
+                    if (lane == 0) P.hdr->no_more_work = 1;
+                    __syncwarp();
+                    break;
+                }
+                uint32_t ji = 0;
+                while (ji + 1 < num_jobs && jobs[ji + 1].group_begin <= group) ++ji;
+                uint32_t q = 0;
+                while (P.hdr->ring[q].active) ++q;  // count < kRing: a free entry exists
+                copy_words(&P.jobs[q], &jobs[ji], sizeof(DevJob), lane, 32u);
+                __syncwarp();
+                if (lane == 0) {
+                    DevJob& J = P.jobs[q];
+                    if (lay.staged) {
+                        J.S.knot_z = reinterpret_cast<const float*>(smem + lay.knot_z);
+                        J.S.finder = reinterpret_cast<const uint16_t*>(smem + lay.finder);
+                        J.S.sigma_t = reinterpret_cast<const float2*>(smem + lay.sigma_t);
+                        J.S.bands = reinterpret_cast<const DevBand*>(smem + lay.bands);
+                        J.S.trk_radius = reinterpret_cast<const float*>(smem + lay.trk_radius);
+                        J.S.trk_maj = reinterpret_cast<const float*>(smem + lay.trk_maj);
+                        J.S.trk_map = reinterpret_cast<const uint16_t*>(smem + lay.trk_map);
+                        J.S.trk_count = reinterpret_cast<const uint32_t*>(smem + lay.trk_count);
+                        J.S.trk_off = reinterpret_cast<const uint32_t*>(smem + lay.trk_off);
+                        if (lay.majorants_bytes) J.S.majorants = reinterpret_cast<const float*>(smem + lay.majorants);
+                    }
+                    const unsigned long long pixels = (unsigned long long)J.L.width * J.L.height;
+                    const unsigned long long pixel0 =
+                        (unsigned long long)(group - J.group_begin) * J.pixels_per_group;
+                    const uint32_t npix = uint32_t(min((unsigned long long)J.pixels_per_group, pixels - pixel0));
+                    RingEntry& R = P.hdr->ring[q];
+                    R.pixel0 = pixel0;
+                    R.job = ji;
+                    R.npix = npix;
+                    R.cells = npix * J.L.band_count;
+                    R.total = R.cells * J.L.spp;
+                    R.issued = 0;
+                    R.done = 0;
+                    R.active = 1;
+                    P.hdr->order[count] = q;
+                    P.hdr->ring_count = count + 1u;
+                }
+                __syncwarp();
+                const uint32_t cells = P.hdr->ring[q].cells;
+                for (uint32_t c = lane; c < cells * 2u; c += 32u) P.acc[size_t(q) * kMaxCells * 2u + c] = 0.0;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        if (P.hdr->no_more_work && P.hdr->ring_count == 0) break;  // every slot is free here
+
+        // ---- generate: free slots take the next chains, in ring order ----
+        {
+            const uint32_t s0 = tid, s1 = tid + kThreads;
+            const bool f0 = (P.u(F_META, s0) & M_STATE) == S_FREE;
+            const bool f1 = kSlots > kThreads && (P.u(F_META, s1) & M_STATE) == S_FREE;
+            const uint32_t cnt = uint32_t(f0) + uint32_t(f1);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(kFull, incl, o);
+                if (int(lane) >= o) incl += v;
+            }
+            if (lane == 31) P.hdr->warp_totals[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0, all_free = 0;
+            for (uint32_t w = 0; w < kWarps; ++w) {
+                const uint32_t v = P.hdr->warp_totals[w];
+                if (w < warp) before += v;
+                all_free += v;
+            }
+            uint32_t rank = before + incl - cnt;
+            for (int which = 0; which < 2; ++which) {
+                const bool fr = which == 0 ? f0 : f1;
+                if (!fr) continue;
+                const uint32_t slot = which == 0 ? s0 : s1;
+                // map the rank to (ring entry, chain) in ring order
+                uint32_t q = 0xffffffffu, j = 0, cum = 0;
+                for (uint32_t i = 0; i < P.hdr->ring_count; ++i) {
+                    const uint32_t e = P.hdr->order[i];
+                    const RingEntry& R = P.hdr->ring[e];
+                    const uint32_t rem = R.total - R.issued;
+                    if (rank < cum + rem) {
+                        q = e;
+                        j = R.issued + (rank - cum);
+                        break;
+                    }
+                    cum += rem;
+                }
+                ++rank;
+                if (q == 0xffffffffu) continue;
+                const DevJob& J = P.jobs[q];
+                const DevScene& S = J.S;
+                const DevLaunch& L = J.L;
+                const RingEntry& R = P.hdr->ring[q];
+                Path p;
+                p.slot = slot;
+                p.ring = q;
+                p.cell = j % R.cells;
+                const uint32_t sample = L.sample_offset + j / R.cells;
+                const uint32_t band = p.cell % L.band_count;
+                const unsigned long long pixel = R.pixel0 + p.cell / L.band_count;
+                const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
+                p.rng.init(uint32_t(pixel), sample, band, L.seed_lo, L.seed_hi);
+                p.dir = camera_dir(L, x, y, p.rng);
+                p.org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
+                p.thr = 1.0f;
+                p.rad = 0.0f;
+                p.meta = 0u;
+                p.pos = p.ldir = mk(0.0f, 0.0f, 0.0f);
+                p.alt = p.nee = p.t = p.tmax = 0.0f;
+                ++n.e[SKY_EVENT_CHAIN];
+                start_ray(P, S, L, p, n, watchdog);
+                store_path(P, p);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                uint32_t left = all_free;
+                for (uint32_t i = 0; i < P.hdr->ring_count && left; ++i) {
+                    RingEntry& R = P.hdr->ring[P.hdr->order[i]];
+                    const uint32_t take = min(left, R.total - R.issued);
+                    R.issued += take;
+                    left -= take;
+                }
+                P.hdr->list_count[0] = P.hdr->list_count[1] = P.hdr->list_count[2] = P.hdr->list_count[3] = 0;
+                P.hdr->fetch = 0;
+            }
+            __syncthreads();
+        }
+
+        // ---- trace: every ray that needs tracking, lanes refilled from one list ----
+        build_list(P, 0, [&](uint32_t s) { return (P.u(F_META, s) & M_STATE) == S_TRACE; });
+        __syncthreads();
+        {
+            const uint32_t total = P.hdr->list_count[0];
+            uint32_t slot = 0, band = 0;
+            const DevScene* S = nullptr;
+            Tracker k;
+            Rng rng;
+            bool have = false, exhausted = false;
+            for (;;) {
+                const uint32_t need = __ballot_sync(kFull, !have && !exhausted);
+                if (need) {
+                    uint32_t base = 0;
+                    if (lane == __ffs(need) - 1u) base = atomicAdd(&P.hdr->fetch, __popc(need));
+                    base = __shfl_sync(kFull, base, __ffs(need) - 1u);
+                    if (!have && !exhausted) {
+                        const uint32_t idx = base + __popc(need & ((1u << lane) - 1u));
+                        if (idx < total) {
+                            slot = P.lists[idx];
+                            const uint32_t c = P.u(F_CELL, slot);
+                            const uint32_t q = c >> 16;
+                            S = &P.jobs[q].S;
+                            band = (c & 0xffffu) % P.jobs[q].L.band_count;
+                            rng.k0 = P.u(F_K0, slot);
+                            rng.k1 = P.u(F_K1, slot);
+                            rng.k2 = P.u(F_K2, slot);
+                            rng.dim = P.u(F_DIM, slot);
+                            k.g.b = P.f(F_GB, slot);
+                            k.g.p = P.f(F_GP, slot);
+                            k.g.r0sq = P.f(F_GR, slot);
+                            k.t_max = P.f(F_TMAX, slot);
+                            track_begin<kTracking>(*S, band, k, rng, n);
+                            have = true;
+                        } else {
+                            exhausted = true;
+                        }
+                    }
+                }
+                if (__ballot_sync(kFull, have) == 0u) break;
+                if (have) {
+                    const int r = track_action<kTracking>(*S, band, k, rng, n, watchdog);
+                    if (r != 0) {
+                        P.f(F_T, slot) = k.t;
+                        P.u(F_DIM, slot) = rng.dim;
+                        const uint32_t meta = P.u(F_META, slot);
+                        P.u(F_META, slot) = (meta & ~(M_STATE | M_HIT)) | S_TRACED | (r == 1 ? M_HIT : 0u);
+                        have = false;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- shade: shadow results, real collisions, ground / escape ----
+        build_list(P, 1, [&](uint32_t s) {
+            const uint32_t m = P.u(F_META, s);
+            return (m & M_STATE) == S_TRACED && (m & M_SHADOW);
+        });
+        build_list(P, 2, [&](uint32_t s) {
+            const uint32_t m = P.u(F_META, s);
+            return (m & M_STATE) == S_TRACED && !(m & M_SHADOW) && (m & M_HIT);
+        });
+        build_list(P, 3, [&](uint32_t s) {
+            const uint32_t m = P.u(F_META, s);
+            return (m & M_STATE) == S_TRACED && !(m & M_SHADOW) && !(m & M_HIT);
+        });
+        __syncthreads();
+        for (uint32_t which = 1; which <= 3; ++which) {
+            const uint32_t cnt = P.hdr->list_count[which];
+            for (uint32_t i = tid; i < cnt; i += kThreads) {
+                Path p;
+                load_path(P, P.lists[which * kSlots + i], p);
+                const DevJob& J = P.jobs[p.ring];
+                const DevScene& S = J.S;
+                const DevLaunch& L = J.L;
+                const uint32_t band = p.cell % L.band_count;
+                const float l_sun = S.bands[band].solar_radiance;
+                if (which == 1) {
+                    // shadow result (sky_trace.wgsl:576-581, :600-603)
+                    if (!(p.meta & M_HIT)) {
+                        if (p.meta & M_GROUND) {
+                            const float cos_sun = fmaxf(dot3(normalize_or_y(p.pos), p.ldir), 0.0f);
+                            p.nee += S.ground_albedo * kInvPi * l_sun * 1.0f * cos_sun / S.light_pdf;
+                        } else {
+                            const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, p.alt);
+                            p.nee += l_sun * 1.0f * mixed_phase(S, c, band, dot3(p.dir, p.ldir)) / S.light_pdf;
+                        }
+                    }
+                    p.meta = with_light(p.meta & ~M_SHADOW, light_of(p.meta) + 1u);
+                    lights_and_continue<kPhase>(P, S, L, p, n, watchdog);
+                } else if (which == 2) {
+                    // real collision (sky_trace.wgsl:720-733)
+                    ++n.e[SKY_EVENT_SCATTER];
+                    p.pos = madd(p.org, p.dir, p.t);
+                    p.alt = altitude_at(p.g, p.t, S.ground_radius);
+                    const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, p.alt);
+                    if (c.extinction <= 0.0f || c.scattering <= 0.0f) {
+                        finish(P, p, fmaxf(p.rad, 0.0f));
+                    } else {
+                        p.thr *= fminf(fmaxf(c.scattering / c.extinction, 0.0f), 1.0f);
+                        if (p.thr <= 0.0f) {
+                            finish(P, p, fmaxf(p.rad, 0.0f));
+                        } else {
+                            p.nee = 0.0f;
+                            p.meta = with_light(p.meta & ~M_GROUND, 0u);
+                            lights_and_continue<kPhase>(P, S, L, p, n, watchdog);
+                        }
+                    }
+                } else {
+                    if (p.meta & M_EXIT) {  // escape (sky_trace.wgsl:745-749)
+                        if (depth_of(p.meta) == 0u && dot3(p.dir, load3(S.sun)) >= S.cos_max) p.rad += p.thr * l_sun;
+                        finish(P, p, fmaxf(p.rad, 0.0f));
+                    } else {  // ground (sky_trace.wgsl:750-752)
+                        ++n.e[SKY_EVENT_GROUND];
+                        p.pos = madd(p.org, p.dir, p.tmax);
+                        p.nee = 0.0f;
+                        p.meta = with_light(p.meta | M_GROUND, 0u);
+                        lights_and_continue<kPhase>(P, S, L, p, n, watchdog);
+                    }
+                }
+                store_path(P, p);
+            }
+        }
+        __syncthreads();
+        if (++idle_iterations > kMaxIdleIterations) {  // never expected: give up, report it
+            stalled = true;
+            break;
+        }
+    }
+
+    if (counters) {
+#pragma unroll
+        for (int e = 0; e < SKY_EVENT_COUNT; ++e) {
+            uint32_t v = n.e[e];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+            if (lane == 0 && v) atomicAdd(counters + e, (unsigned long long)v);
+        }
+    }
+    if (__any_sync(kFull, watchdog) && lane == 0) atomicOr(status, 1u);
+    if (__any_sync(kFull, stalled) && lane == 0) atomicOr(status, 2u);
+}
+
+template <int kTracking, int kPhase>
+cudaError_t launch_one(const PoolLaunch& w, cudaStream_t stream) {
+    auto fn = pool_kernel<kTracking, kPhase>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(w.layout.total));
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, int(kThreads), w.layout.total);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (w.max_blocks_per_sm > 0) per_sm = std::min(per_sm, int(w.max_blocks_per_sm));
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    uint32_t blocks = std::max(1u, std::min(uint32_t(sms) * uint32_t(per_sm), w.total_groups));
+    fn<<<blocks, kThreads, w.layout.total, stream>>>(w.jobs, w.num_jobs, w.total_groups, w.layout, w.work_counter,
+                                                     w.counters, w.status);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream) {
+#define SKY_POOL_CASE(TR, PH) \
+    if (w.tracking == TR && w.phase_sampling == PH) return launch_one<TR, PH>(w, stream);
+    SKY_POOL_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_ISOTROPIC)
+    SKY_POOL_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_TABULATED)
+    SKY_POOL_CASE(SKY_TRACKING_RESIDUAL_CARRY, SKY_PHASE_ISOTROPIC)
+    SKY_POOL_CASE(SKY_TRACKING_RESIDUAL_CARRY, SKY_PHASE_TABULATED)
+    SKY_POOL_CASE(SKY_TRACKING_MERGED_LAYERS, SKY_PHASE_ISOTROPIC)
+    SKY_POOL_CASE(SKY_TRACKING_MERGED_LAYERS, SKY_PHASE_TABULATED)
+#undef SKY_POOL_CASE
+    return cudaErrorInvalidValue;
+}
+
+PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables) {
+    PoolLayout l{};
+    size_t off = 0;
+    auto take = [&off](size_t bytes) {
+        const size_t at = off;
+        off = (off + bytes + 15) / 16 * 16;
+        return uint32_t(at);
+    };
+    l.header = take(sizeof(PoolHeader));
+    l.jobs = take(kRing * sizeof(DevJob));
+    l.acc = take(size_t(kRing) * kMaxCells * 2u * sizeof(double));
+    l.slots = take(size_t(F_COUNT) * kSlots * 4u);
+    l.lists = take(4u * kSlots * 2u);
+    l.staged = stage_tables ? 1u : 0u;
+    if (stage_tables) {
+        l.knot_z_bytes = S.knot_count * 4u;
+        l.finder_bytes = kFinderCells * 2u;
+        l.sigma_t_bytes = S.band_count * S.knot_count * 8u;
+        l.bands_bytes = S.band_count * uint32_t(sizeof(DevBand));
+        l.trk_bytes = S.trk_total * 4u;
+        l.trk_map_bytes = (S.band_count * S.layer_count * 2u + 3u) / 4u * 4u;
+        l.trk_count_bytes = S.band_count * 4u;
+        l.majorants_bytes = with_majorants ? S.band_count * S.layer_count * 4u : 0u;
+        l.knot_z = take(l.knot_z_bytes);
+        l.finder = take(l.finder_bytes);
+        l.sigma_t = take(l.sigma_t_bytes);
+        l.bands = take(l.bands_bytes);
+        l.trk_radius = take(l.trk_bytes);
+        l.trk_maj = take(l.trk_bytes);
+        l.trk_map = take(l.trk_map_bytes);
+        l.trk_count = take(l.trk_count_bytes);
+        l.trk_off = take(l.trk_count_bytes);
+        l.majorants = take(l.majorants_bytes);
+    }
+    l.total = uint32_t(off);
+    return l;
+}
+
+}  // namespace sky
