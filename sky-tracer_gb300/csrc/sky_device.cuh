@@ -298,6 +298,11 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float
 
 // ---- phase functions ----------------------------------------------------------------
 
+// Cube root of x >= 0 as 2^(log2(x)/3) on the special-function unit (relative
+// error ~1e-6; only used to place mu on the cube-root phase grid and in the
+// Rayleigh inverse CDF).
+__device__ __forceinline__ float cbrt_pos(float x) { return x > 0.0f ? exp2f(__log2f(x) * (1.0f / 3.0f)) : 0.0f; }
+
 __device__ __forceinline__ float rayleigh_phase(float mu) { return kRayleighNorm * (1.0f + mu * mu); }
 
 // mie_phase (sky_trace.wgsl:485-494): lerp between bin centres on the
@@ -305,7 +310,7 @@ __device__ __forceinline__ float rayleigh_phase(float mu) { return kRayleighNorm
 __device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, uint32_t band, float mu) {
     uint32_t bins = S.phase_bins;
     float x = (1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f;
-    float u = cbrtf(x);
+    float u = cbrt_pos(x);
     float f = u * float(bins) - 0.5f;
     uint32_t i0 = min(uint32_t(fminf(fmaxf(floorf(f), 0.0f), float(bins - 1u))), bins - 1u);
     uint32_t i1 = min(i0 + 1u, bins - 1u);
@@ -353,7 +358,7 @@ __device__ __forceinline__ float sample_mie_mu(const DevScene& S, uint32_t speci
 // MiePhaseTable::sampling_pdf (phase.rs:71-75, mu_to_bin :142-146)
 __device__ __forceinline__ float mie_sampling_pdf(const DevScene& S, uint32_t species, uint32_t band, float mu) {
     uint32_t bins = S.phase_bins;
-    float u = cbrtf((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
+    float u = cbrt_pos((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
     uint32_t bin = min(uint32_t(floorf(u * float(bins))), bins - 1u);
     return fmaxf(__ldg(S.phase_bin_pdf + (size_t(species) * S.band_count + band) * bins + bin), 1.0e-12f);
 }
@@ -362,7 +367,7 @@ __device__ __forceinline__ float mie_sampling_pdf(const DevScene& S, uint32_t sp
 // with u = cbrt(y + sqrt(y^2 + 1)), y = 4 xi - 2.
 __device__ __forceinline__ float invert_rayleigh_cdf(float xi) {
     float y = 4.0f * fminf(fmaxf(xi, 0.0f), 1.0f) - 2.0f;
-    float u = cbrtf(y + sqrtf(fmaf(y, y, 1.0f)));
+    float u = cbrt_pos(y + sqrtf(fmaf(y, y, 1.0f)));
     return fminf(fmaxf(u - 1.0f / u, -1.0f), 1.0f);
 }
 

@@ -17,7 +17,7 @@ cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* ce
 
 // Block path pool of the persistent wavefront kernel (trace_pool.cu).
 constexpr uint32_t kPoolThreads = 256;
-constexpr uint32_t kPoolSlots = 512;      // paths resident per block
+constexpr uint32_t kPoolSlots = 1024;     // paths resident per block (a multiple of kPoolThreads)
 constexpr uint32_t kPoolRing = 4;         // work groups in flight per block
 constexpr uint32_t kPoolMaxCells = 256;   // (pixel, band) cells per work group
 

@@ -40,9 +40,10 @@ constexpr uint32_t kWarps = kThreads / 32u;
 constexpr uint32_t kSlots = kPoolSlots;
 constexpr uint32_t kRing = kPoolRing;
 constexpr uint32_t kMaxCells = kPoolMaxCells;
-// Upper bound on block iterations for one launch-lifetime of a block without
-// progress; exceeding it sets status bit 2 instead of running on.
-constexpr uint32_t kMaxIdleIterations = 1u << 24;
+// Upper bound on the phase iterations of one block in one launch (a block
+// needs ~3 per chain / kSlots); exceeding it sets status bit 2 and the block
+// returns instead of running on.
+constexpr uint32_t kMaxIterations = 1u << 24;
 
 // slot meta word
 constexpr uint32_t M_STATE = 0x3u;  // 0 free, 1 needs tracking, 2 tracked
@@ -54,11 +55,14 @@ constexpr uint32_t M_EXIT = 1u << 5;
 constexpr uint32_t M_LIGHT_SHIFT = 8u;
 constexpr uint32_t M_DEPTH_SHIFT = 16u;
 
+// Slot fields (one u32 word each, structure of arrays).  O holds the origin
+// of the camera/continuation ray or, after an event, the event position; T
+// holds the distance to the boundary while a ray waits for tracking and the
+// collision distance after it.
 enum SlotField : uint32_t {
     F_CELL, F_K0, F_K1, F_K2, F_DIM, F_META,
-    F_OX, F_OY, F_OZ, F_DX, F_DY, F_DZ, F_THR, F_RAD,
-    F_PX, F_PY, F_PZ, F_LX, F_LY, F_LZ, F_ALT, F_NEE,
-    F_GB, F_GP, F_GR, F_TMAX, F_T, F_COUNT
+    F_OX, F_OY, F_OZ, F_DX, F_DY, F_DZ, F_LX, F_LY, F_LZ,
+    F_THR, F_RAD, F_NEE, F_ALT, F_T, F_COUNT
 };
 
 struct RingEntry {
@@ -86,13 +90,12 @@ struct PoolSmem {
     }
 };
 
-// Registers of one path while a thread works on it.
+// Registers of one path while a thread shades it.
 struct Path {
     uint32_t slot, cell, ring, meta;
     Rng rng;
-    V3 org, dir, pos, ldir;
-    float thr, rad, alt, nee, tmax, t;
-    RayGeo g;
+    V3 o, dir, ldir;
+    float thr, rad, nee, alt, t;
 };
 
 __device__ __forceinline__ void load_path(const PoolSmem& P, uint32_t s, Path& p) {
@@ -105,18 +108,13 @@ __device__ __forceinline__ void load_path(const PoolSmem& P, uint32_t s, Path& p
     p.rng.k2 = P.u(F_K2, s);
     p.rng.dim = P.u(F_DIM, s);
     p.meta = P.u(F_META, s);
-    p.org = mk(P.f(F_OX, s), P.f(F_OY, s), P.f(F_OZ, s));
+    p.o = mk(P.f(F_OX, s), P.f(F_OY, s), P.f(F_OZ, s));
     p.dir = mk(P.f(F_DX, s), P.f(F_DY, s), P.f(F_DZ, s));
+    p.ldir = mk(P.f(F_LX, s), P.f(F_LY, s), P.f(F_LZ, s));
     p.thr = P.f(F_THR, s);
     p.rad = P.f(F_RAD, s);
-    p.pos = mk(P.f(F_PX, s), P.f(F_PY, s), P.f(F_PZ, s));
-    p.ldir = mk(P.f(F_LX, s), P.f(F_LY, s), P.f(F_LZ, s));
-    p.alt = P.f(F_ALT, s);
     p.nee = P.f(F_NEE, s);
-    p.g.b = P.f(F_GB, s);
-    p.g.p = P.f(F_GP, s);
-    p.g.r0sq = P.f(F_GR, s);
-    p.tmax = P.f(F_TMAX, s);
+    p.alt = P.f(F_ALT, s);
     p.t = P.f(F_T, s);
 }
 
@@ -128,26 +126,19 @@ __device__ __forceinline__ void store_path(const PoolSmem& P, const Path& p) {
     P.u(F_K2, s) = p.rng.k2;
     P.u(F_DIM, s) = p.rng.dim;
     P.u(F_META, s) = p.meta;
-    P.f(F_OX, s) = p.org.x;
-    P.f(F_OY, s) = p.org.y;
-    P.f(F_OZ, s) = p.org.z;
+    P.f(F_OX, s) = p.o.x;
+    P.f(F_OY, s) = p.o.y;
+    P.f(F_OZ, s) = p.o.z;
     P.f(F_DX, s) = p.dir.x;
     P.f(F_DY, s) = p.dir.y;
     P.f(F_DZ, s) = p.dir.z;
-    P.f(F_THR, s) = p.thr;
-    P.f(F_RAD, s) = p.rad;
-    P.f(F_PX, s) = p.pos.x;
-    P.f(F_PY, s) = p.pos.y;
-    P.f(F_PZ, s) = p.pos.z;
     P.f(F_LX, s) = p.ldir.x;
     P.f(F_LY, s) = p.ldir.y;
     P.f(F_LZ, s) = p.ldir.z;
-    P.f(F_ALT, s) = p.alt;
+    P.f(F_THR, s) = p.thr;
+    P.f(F_RAD, s) = p.rad;
     P.f(F_NEE, s) = p.nee;
-    P.f(F_GB, s) = p.g.b;
-    P.f(F_GP, s) = p.g.p;
-    P.f(F_GR, s) = p.g.r0sq;
-    P.f(F_TMAX, s) = p.tmax;
+    P.f(F_ALT, s) = p.alt;
     P.f(F_T, s) = p.t;
 }
 
@@ -303,20 +294,21 @@ __device__ __forceinline__ void start_ray(const PoolSmem& P, const DevScene& S, 
         finish(P, p, fmaxf(p.rad, 0.0f));
         return;
     }
-    p.g = ray_geo(p.org, p.dir);
+    const RayGeo g = ray_geo(p.o, p.dir);
     ++n.e[SKY_EVENT_BOUNDARY];
     float tb;
     uint32_t kind;
-    if (!next_boundary(S, p.g, tb, kind)) {
+    if (!next_boundary(S, g, tb, kind)) {
         finish(P, p, fmaxf(p.rad, 0.0f));
         return;
     }
-    p.tmax = tb;
+    p.t = tb;
     p.meta = (p.meta & ~(M_STATE | M_SHADOW | M_HIT | M_EXIT)) | S_TRACE | (kind == 1u ? M_EXIT : 0u);
 }
 
 // Light samples of the current event (sky_trace.wgsl:566-608) until one needs
 // a shadow ray traced; then the continuation (:728-767) and the next ray.
+// p.o is the event position here.
 template <int kPhase>
 __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const DevLaunch& L, Path& p, Counters& n,
                                     bool& watchdog) {
@@ -327,14 +319,14 @@ __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const 
         p.ldir = sample_sun_cone(S, p.rng);
         ++n.e[SKY_EVENT_NEE];
         bool go = true;
-        if (ground) go = fmaxf(dot3(normalize_or_y(p.pos), p.ldir), 0.0f) > 0.0f;
+        if (ground) go = fmaxf(dot3(normalize_or_y(p.o), p.ldir), 0.0f) > 0.0f;
         if (go) {
-            p.g = ray_geo(madd(p.pos, p.ldir, kRayEpsilonKm), p.ldir);
+            const RayGeo g = ray_geo(madd(p.o, p.ldir, kRayEpsilonKm), p.ldir);
             ++n.e[SKY_EVENT_BOUNDARY];
             float tb;
             uint32_t kind;
-            if (next_boundary(S, p.g, tb, kind) && kind == 1u) {
-                p.tmax = tb;
+            if (next_boundary(S, g, tb, kind) && kind == 1u) {
+                p.t = tb;
                 p.meta = (with_light(p.meta, light) & ~(M_STATE | M_HIT)) | S_TRACE | M_SHADOW;
                 return;
             }
@@ -342,8 +334,6 @@ __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const 
         ++light;
     }
     // continuation
-    const float l_sun = S.bands[band].solar_radiance;
-    (void)l_sun;
     p.rad += p.thr * (p.nee * (1.0f / float(L.direct_light_samples)));
     const uint32_t depth = depth_of(p.meta);
     V3 nd;
@@ -356,7 +346,7 @@ __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const 
             p.thr *= mixed_phase(S, c, band, dot3(p.dir, nd)) / kIsotropicPdf;
         }
     } else {
-        const V3 normal = normalize_or_y(p.pos);
+        const V3 normal = normalize_or_y(p.o);
         float pdf;
         nd = sample_cosine_hemisphere(normal, p.rng, pdf);
         const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
@@ -374,7 +364,7 @@ __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const 
         }
         p.thr = p.thr / q;
     }
-    p.org = madd(p.pos, nd, kRayEpsilonKm);
+    p.o = madd(p.o, nd, kRayEpsilonKm);
     p.dir = nd;
     if (p.rad < 0.0f || p.rad != p.rad || p.thr < 0.0f || p.thr != p.thr) {
         finish(P, p, 0.0f);
@@ -399,8 +389,29 @@ __device__ __forceinline__ void build_list(const PoolSmem& P, uint32_t which, Pr
     }
 }
 
+// One pass over the slots: tracked rays go to list 1 (shadow results),
+// 2 (real collisions) or 3 (ground / escape).
+__device__ __forceinline__ void build_shade_lists(const PoolSmem& P) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (uint32_t base = 0; base < kSlots; base += kThreads) {
+        const uint32_t s = base + threadIdx.x;
+        const uint32_t m = P.u(F_META, s);
+        const bool traced = (m & M_STATE) == S_TRACED;
+        const uint32_t cls = !traced ? 0u : ((m & M_SHADOW) ? 1u : ((m & M_HIT) ? 2u : 3u));
+#pragma unroll
+        for (uint32_t w = 1; w <= 3; ++w) {
+            const uint32_t mask = __ballot_sync(kFull, cls == w);
+            uint32_t at = 0;
+            if (lane == 0 && mask) at = atomicAdd(&P.hdr->list_count[w], __popc(mask));
+            at = __shfl_sync(kFull, at, 0);
+            if (cls == w) P.lists[w * kSlots + at + __popc(mask & lt)] = uint16_t(s);
+        }
+    }
+}
+
 template <int kTracking, int kPhase>
-__global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict__ jobs, uint32_t num_jobs,
+__global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restrict__ jobs, uint32_t num_jobs,
                                                         uint32_t total_groups, PoolLayout lay,
                                                         uint32_t* __restrict__ work_counter,
                                                         unsigned long long* __restrict__ counters,
@@ -441,7 +452,7 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
     n.clear();
     bool watchdog = false;
     bool stalled = false;
-    uint32_t idle_iterations = 0;
+    uint32_t iterations = 0;
 
     for (;;) {
         // ---- ring maintenance: epilogues of finished groups, then refill ----
@@ -566,10 +577,15 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
 
         // ---- generate: free slots take the next chains, in ring order ----
         {
-            const uint32_t s0 = tid, s1 = tid + kThreads;
-            const bool f0 = (P.u(F_META, s0) & M_STATE) == S_FREE;
-            const bool f1 = kSlots > kThreads && (P.u(F_META, s1) & M_STATE) == S_FREE;
-            const uint32_t cnt = uint32_t(f0) + uint32_t(f1);
+            constexpr uint32_t kPer = kSlots / kThreads;
+            uint32_t free_mask = 0, cnt = 0;
+#pragma unroll
+            for (uint32_t i = 0; i < kPer; ++i) {
+                if ((P.u(F_META, tid + i * kThreads) & M_STATE) == S_FREE) {
+                    free_mask |= 1u << i;
+                    ++cnt;
+                }
+            }
             uint32_t incl = cnt;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -585,25 +601,24 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                 all_free += v;
             }
             uint32_t rank = before + incl - cnt;
-            for (int which = 0; which < 2; ++which) {
-                const bool fr = which == 0 ? f0 : f1;
-                if (!fr) continue;
-                const uint32_t slot = which == 0 ? s0 : s1;
+            for (uint32_t i = 0; i < kPer; ++i) {
+                if (!(free_mask & (1u << i))) continue;
+                const uint32_t slot = tid + i * kThreads;
                 // map the rank to (ring entry, chain) in ring order
                 uint32_t q = 0xffffffffu, j = 0, cum = 0;
-                for (uint32_t i = 0; i < P.hdr->ring_count; ++i) {
-                    const uint32_t e = P.hdr->order[i];
-                    const RingEntry& R = P.hdr->ring[e];
+                for (uint32_t e = 0; e < P.hdr->ring_count; ++e) {
+                    const uint32_t id = P.hdr->order[e];
+                    const RingEntry& R = P.hdr->ring[id];
                     const uint32_t rem = R.total - R.issued;
                     if (rank < cum + rem) {
-                        q = e;
+                        q = id;
                         j = R.issued + (rank - cum);
                         break;
                     }
                     cum += rem;
                 }
                 ++rank;
-                if (q == 0xffffffffu) continue;
+                if (q == 0xffffffffu) break;  // later ranks find no chain either
                 const DevJob& J = P.jobs[q];
                 const DevScene& S = J.S;
                 const DevLaunch& L = J.L;
@@ -618,12 +633,12 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                 const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
                 p.rng.init(uint32_t(pixel), sample, band, L.seed_lo, L.seed_hi);
                 p.dir = camera_dir(L, x, y, p.rng);
-                p.org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
+                p.o = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
                 p.thr = 1.0f;
                 p.rad = 0.0f;
                 p.meta = 0u;
-                p.pos = p.ldir = mk(0.0f, 0.0f, 0.0f);
-                p.alt = p.nee = p.t = p.tmax = 0.0f;
+                p.ldir = mk(0.0f, 0.0f, 0.0f);
+                p.alt = p.nee = p.t = 0.0f;
                 ++n.e[SKY_EVENT_CHAIN];
                 start_ray(P, S, L, p, n, watchdog);
                 store_path(P, p);
@@ -631,8 +646,8 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
             __syncthreads();
             if (tid == 0) {
                 uint32_t left = all_free;
-                for (uint32_t i = 0; i < P.hdr->ring_count && left; ++i) {
-                    RingEntry& R = P.hdr->ring[P.hdr->order[i]];
+                for (uint32_t e = 0; e < P.hdr->ring_count && left; ++e) {
+                    RingEntry& R = P.hdr->ring[P.hdr->order[e]];
                     const uint32_t take = min(left, R.total - R.issued);
                     R.issued += take;
                     left -= take;
@@ -652,13 +667,14 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
             const DevScene* S = nullptr;
             Tracker k;
             Rng rng;
-            bool have = false, exhausted = false;
+            bool have = false, exhausted = false, shadow = false;
             for (;;) {
                 const uint32_t need = __ballot_sync(kFull, !have && !exhausted);
                 if (need) {
+                    const uint32_t leader = __ffs(need) - 1u;
                     uint32_t base = 0;
-                    if (lane == __ffs(need) - 1u) base = atomicAdd(&P.hdr->fetch, __popc(need));
-                    base = __shfl_sync(kFull, base, __ffs(need) - 1u);
+                    if (lane == leader) base = atomicAdd(&P.hdr->fetch, __popc(need));
+                    base = __shfl_sync(kFull, base, leader);
                     if (!have && !exhausted) {
                         const uint32_t idx = base + __popc(need & ((1u << lane) - 1u));
                         if (idx < total) {
@@ -671,10 +687,15 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                             rng.k1 = P.u(F_K1, slot);
                             rng.k2 = P.u(F_K2, slot);
                             rng.dim = P.u(F_DIM, slot);
-                            k.g.b = P.f(F_GB, slot);
-                            k.g.p = P.f(F_GP, slot);
-                            k.g.r0sq = P.f(F_GR, slot);
-                            k.t_max = P.f(F_TMAX, slot);
+                            shadow = (P.u(F_META, slot) & M_SHADOW) != 0u;
+                            const V3 o = mk(P.f(F_OX, slot), P.f(F_OY, slot), P.f(F_OZ, slot));
+                            if (shadow) {
+                                const V3 l = mk(P.f(F_LX, slot), P.f(F_LY, slot), P.f(F_LZ, slot));
+                                k.g = ray_geo(madd(o, l, kRayEpsilonKm), l);
+                            } else {
+                                k.g = ray_geo(o, mk(P.f(F_DX, slot), P.f(F_DY, slot), P.f(F_DZ, slot)));
+                            }
+                            k.t_max = P.f(F_T, slot);
                             track_begin<kTracking>(*S, band, k, rng, n);
                             have = true;
                         } else {
@@ -686,7 +707,10 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                 if (have) {
                     const int r = track_action<kTracking>(*S, band, k, rng, n, watchdog);
                     if (r != 0) {
-                        P.f(F_T, slot) = k.t;
+                        if (r == 1 && !shadow) {
+                            P.f(F_T, slot) = k.t;
+                            P.f(F_ALT, slot) = altitude_at(k.g, k.t, S->ground_radius);
+                        }
                         P.u(F_DIM, slot) = rng.dim;
                         const uint32_t meta = P.u(F_META, slot);
                         P.u(F_META, slot) = (meta & ~(M_STATE | M_HIT)) | S_TRACED | (r == 1 ? M_HIT : 0u);
@@ -698,18 +722,7 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
         __syncthreads();
 
         // ---- shade: shadow results, real collisions, ground / escape ----
-        build_list(P, 1, [&](uint32_t s) {
-            const uint32_t m = P.u(F_META, s);
-            return (m & M_STATE) == S_TRACED && (m & M_SHADOW);
-        });
-        build_list(P, 2, [&](uint32_t s) {
-            const uint32_t m = P.u(F_META, s);
-            return (m & M_STATE) == S_TRACED && !(m & M_SHADOW) && (m & M_HIT);
-        });
-        build_list(P, 3, [&](uint32_t s) {
-            const uint32_t m = P.u(F_META, s);
-            return (m & M_STATE) == S_TRACED && !(m & M_SHADOW) && !(m & M_HIT);
-        });
+        build_shade_lists(P);
         __syncthreads();
         for (uint32_t which = 1; which <= 3; ++which) {
             const uint32_t cnt = P.hdr->list_count[which];
@@ -722,10 +735,10 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                 const uint32_t band = p.cell % L.band_count;
                 const float l_sun = S.bands[band].solar_radiance;
                 if (which == 1) {
-                    // shadow result (sky_trace.wgsl:576-581, :600-603)
+                    // shadow result (sky_trace.wgsl:576-581, :600-603); p.o is the event position
                     if (!(p.meta & M_HIT)) {
                         if (p.meta & M_GROUND) {
-                            const float cos_sun = fmaxf(dot3(normalize_or_y(p.pos), p.ldir), 0.0f);
+                            const float cos_sun = fmaxf(dot3(normalize_or_y(p.o), p.ldir), 0.0f);
                             p.nee += S.ground_albedo * kInvPi * l_sun * 1.0f * cos_sun / S.light_pdf;
                         } else {
                             const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, p.alt);
@@ -735,10 +748,9 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                     p.meta = with_light(p.meta & ~M_SHADOW, light_of(p.meta) + 1u);
                     lights_and_continue<kPhase>(P, S, L, p, n, watchdog);
                 } else if (which == 2) {
-                    // real collision (sky_trace.wgsl:720-733)
+                    // real collision (sky_trace.wgsl:720-733); p.alt was set by the tracker
                     ++n.e[SKY_EVENT_SCATTER];
-                    p.pos = madd(p.org, p.dir, p.t);
-                    p.alt = altitude_at(p.g, p.t, S.ground_radius);
+                    p.o = madd(p.o, p.dir, p.t);
                     const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, p.alt);
                     if (c.extinction <= 0.0f || c.scattering <= 0.0f) {
                         finish(P, p, fmaxf(p.rad, 0.0f));
@@ -756,9 +768,9 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
                     if (p.meta & M_EXIT) {  // escape (sky_trace.wgsl:745-749)
                         if (depth_of(p.meta) == 0u && dot3(p.dir, load3(S.sun)) >= S.cos_max) p.rad += p.thr * l_sun;
                         finish(P, p, fmaxf(p.rad, 0.0f));
-                    } else {  // ground (sky_trace.wgsl:750-752)
+                    } else {  // ground (sky_trace.wgsl:750-752): T still holds the ground distance
                         ++n.e[SKY_EVENT_GROUND];
-                        p.pos = madd(p.org, p.dir, p.tmax);
+                        p.o = madd(p.o, p.dir, p.t);
                         p.nee = 0.0f;
                         p.meta = with_light(p.meta | M_GROUND, 0u);
                         lights_and_continue<kPhase>(P, S, L, p, n, watchdog);
@@ -768,7 +780,7 @@ __global__ void __launch_bounds__(kThreads) pool_kernel(const DevJob* __restrict
             }
         }
         __syncthreads();
-        if (++idle_iterations > kMaxIdleIterations) {  // never expected: give up, report it
+        if (++iterations > kMaxIterations) {  // never expected: give up, report it
             stalled = true;
             break;
         }
