@@ -69,6 +69,7 @@ def parse_args():
     p.add_argument("--no-peak", action="store_true", help="skip the SGEMM FP32-peak measurement")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     return p.parse_args()
 
 
@@ -252,6 +253,14 @@ def main():
     chains = cells * cfg.spp
 
     gs = GpuScene(scene)
+    tuning_log = None
+    if not args.no_autotune and cfg.kernel != 1:
+        from sky_cuda.autotune import autotune
+        t0 = time.perf_counter()
+        best, trials = autotune(gs, cfg)
+        tuning_log = {"chosen": best, "seconds": round(time.perf_counter() - t0, 2),
+                      "trials": [[t["pool_variant"], t["stage_tables"], round(t["crossing_cost"], 3), round(ms, 3)]
+                                 for t, ms in trials]}
     stream = torch.cuda.current_stream(dev)
     s = torch.zeros(cells, dtype=torch.float64, device=dev)
     q = torch.zeros(cells, dtype=torch.float64, device=dev)
@@ -338,7 +347,8 @@ def main():
                        "spp": cfg.spp, "chains_per_step": chains, "sun_elevation_deg": w["sun"],
                        "tracking": ("segment-restart", "residual-carry", "merged-layers")[cfg.tracking],
                        "phase_sampling": "tabulated", "kernel": ("persistent", "plain", "persistent")[cfg.kernel],
-                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}"},
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}",
+                       "tuning": gs.get_tuning(), "autotune": tuning_log},
             "e2e": {"value": world * chains / e2e_s if e2e_times else None, "unit": "chains/s",
                     "h2d_bytes_per_step": int(desc_bytes),
                     "d2h_bytes_per_step": int(cells * 4 + 8 * 8 + 4)},

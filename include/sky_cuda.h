@@ -227,6 +227,22 @@ typedef struct SkyDeviceOutputs {
     uint32_t* status;
 } SkyDeviceOutputs;
 
+/*
+ * Launch shape of the persistent tracer, per scene.  No counterpart in the
+ * reference, whose dispatch shape is fixed (workgroup 8x8x1, one dispatch per
+ * 2 samples, integrator.rs:254-283).  The Python package's autotuner times
+ * candidates of these on the caller's workload and keeps the fastest.
+ */
+typedef struct SkyTuning {
+    uint32_t pool_variant;       /* 0: 1024 resident paths, 2 blocks/SM; 1: 512 paths, 3 blocks/SM */
+    uint32_t max_blocks_per_sm;  /* 0 = occupancy limit                                          */
+    uint32_t stage_tables;       /* 1 = stage the scene tables in shared memory when they fit     */
+    uint32_t pixels_per_group;   /* pixels per work group; 0 = automatic                          */
+    float crossing_cost;         /* merged tracking grid: cost of a layer crossing relative to a
+                                    null collision; <= 0 leaves the grid as it is              */
+    uint32_t _reserved[3];
+} SkyTuning;
+
 /* ---- Entry points ------------------------------------------------------ */
 
 /* Library version string, e.g. "sky_cuda 0.1.0 (abi 1, sm_103a)". */
@@ -242,6 +258,12 @@ int sky_cuda_last_error(char* buf, size_t buf_len);
 int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene);
 
 void sky_cuda_scene_destroy(SkyScene* scene);
+
+/* Set / read the scene's launch shape (SkyTuning).  Setting a positive
+ * crossing_cost rebuilds the merged tracking grid (SKY_TRACKING_MERGED_LAYERS)
+ * from the scene's majorant grid.  No counterpart in the reference. */
+int sky_cuda_scene_set_tuning(SkyScene* scene, const SkyTuning* tuning);
+int sky_cuda_scene_get_tuning(const SkyScene* scene, SkyTuning* tuning);
 
 /*
  * Render the spectral film into host memory: `film_out` receives

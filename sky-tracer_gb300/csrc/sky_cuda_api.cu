@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/sky_cuda.h"
 #include "scene_build.h"
@@ -41,8 +42,12 @@ struct SkyScene {
     DevJob* jobs = nullptr;
     uint32_t* work_counter = nullptr;
     int smem_optin = 0;
-    bool stage_tables = false;        // stage the scene tables in shared memory
-    uint32_t max_blocks_per_sm = 0;   // 0 = occupancy limit
+    SkyTuning tuning{};
+    // merged tracking grid in its own allocation (rebuilt by set_tuning)
+    void* trk_blob = nullptr;
+    std::vector<float> host_majorants;
+    float host_ground_radius = 0.0f, host_top = 0.0f;
+    uint32_t host_layers = 0;
 };
 
 namespace {
@@ -172,8 +177,8 @@ DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
 
 // Pixels per work group of the persistent kernel: enough chains per group
 // (>= 4 pools) to keep the ring short, at most kPoolMaxCells cells.
-uint32_t pixels_per_group(uint32_t bands, uint32_t spp) {
-    const uint32_t want = 4u * kPoolSlots;
+uint32_t pixels_per_group(uint32_t bands, uint32_t spp, uint32_t variant) {
+    const uint32_t want = 4u * kPoolThreads * pool_slots_per_thread(variant);
     uint32_t p = (want + bands * spp - 1u) / (bands * spp);
     p = std::max(1u, std::min(p, kPoolMaxCells / bands));
     return p;
@@ -208,7 +213,10 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     job.xyz_var = xyz_var;
     job.accumulate = accumulate ? 1u : 0u;
     job.total_spp = total_spp;
-    job.pixels_per_group = pixels_per_group(B, c->spp);
+    job.pixels_per_group = s->tuning.pixels_per_group
+                               ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
+                               : pixels_per_group(B, c->spp, s->tuning.pool_variant);
+    job.pixels_per_group = std::max(1u, job.pixels_per_group);
     job.group_begin = 0;
     job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
     PoolLaunch w{};
@@ -221,9 +229,10 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     w.counters = o->counters;
     w.status = o->status;
     const bool with_maj = c->tracking != SKY_TRACKING_MERGED_LAYERS;
-    w.layout = plan_pool_layout(s->dev, with_maj, s->stage_tables);
-    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false);
-    w.max_blocks_per_sm = s->max_blocks_per_sm;
+    w.variant = s->tuning.pool_variant;
+    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
+    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
+    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
     if ((e = cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
         return cuda_fail(SKY_ERR_COPY, "job upload", e);
     if ((e = cudaMemsetAsync(s->work_counter, 0, sizeof(uint32_t), stream)) != cudaSuccess)
@@ -287,9 +296,106 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
     return SKY_OK;
 }
 
+// Upload the merged tracking grid of `h` into its own device allocation.
+int upload_tracking_grid(SkyScene* s, const HostTables& h) {
+    size_t off = 0;
+    auto reserve = [&off](size_t bytes) {
+        size_t at = off;
+        off = align_up(off + bytes, 256);
+        return at;
+    };
+    const size_t o_tr = reserve(h.trk_radius.size() * sizeof(float));
+    const size_t o_tm = reserve(h.trk_maj.size() * sizeof(float));
+    const size_t o_tp = reserve(h.trk_map.size() * sizeof(uint16_t));
+    const size_t o_tc = reserve(h.trk_count.size() * sizeof(uint32_t));
+    const size_t o_to = reserve(h.trk_off.size() * sizeof(uint32_t));
+    std::vector<unsigned char> host(off, 0);
+    std::memcpy(host.data() + o_tr, h.trk_radius.data(), h.trk_radius.size() * sizeof(float));
+    std::memcpy(host.data() + o_tm, h.trk_maj.data(), h.trk_maj.size() * sizeof(float));
+    std::memcpy(host.data() + o_tp, h.trk_map.data(), h.trk_map.size() * sizeof(uint16_t));
+    std::memcpy(host.data() + o_tc, h.trk_count.data(), h.trk_count.size() * sizeof(uint32_t));
+    std::memcpy(host.data() + o_to, h.trk_off.data(), h.trk_off.size() * sizeof(uint32_t));
+    void* blob = nullptr;
+    cudaError_t e = cudaMalloc(&blob, off);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "tracking grid allocation", e);
+    if ((e = cudaMemcpy(blob, host.data(), off, cudaMemcpyHostToDevice)) != cudaSuccess) {
+        cudaFree(blob);
+        return cuda_fail(SKY_ERR_COPY, "tracking grid upload", e);
+    }
+    if (s->trk_blob) {
+        if (s->stream) cudaStreamSynchronize(s->stream);
+        cudaFree(s->trk_blob);
+    }
+    s->trk_blob = blob;
+    unsigned char* base = static_cast<unsigned char*>(blob);
+    s->dev.trk_radius = reinterpret_cast<const float*>(base + o_tr);
+    s->dev.trk_maj = reinterpret_cast<const float*>(base + o_tm);
+    s->dev.trk_map = reinterpret_cast<const uint16_t*>(base + o_tp);
+    s->dev.trk_count = reinterpret_cast<const uint32_t*>(base + o_tc);
+    s->dev.trk_off = reinterpret_cast<const uint32_t*>(base + o_to);
+    s->dev.trk_total = uint32_t(h.trk_radius.size());
+    return SKY_OK;
+}
+
+// Rebuild the merged grid for a new crossing cost from the stored majorants.
+int rebuild_tracking_grid(SkyScene* s, double crossing_cost) {
+    HostTables h;
+    const uint32_t B = s->dev.band_count, L = s->host_layers;
+    const float dzl = s->host_top / float(L);
+    h.trk_map.assign(size_t(B) * L, 0);
+    h.trk_count.assign(B, 0);
+    h.trk_off.assign(B, 0);
+    for (uint32_t b = 0; b < B; ++b) {
+        const float* maj = s->host_majorants.data() + size_t(b) * L;
+        std::vector<uint32_t> starts = merge_majorant_layers(maj, L, dzl, crossing_cost);
+        const uint32_t M = uint32_t(starts.size());
+        h.trk_count[b] = M;
+        h.trk_off[b] = uint32_t(h.trk_radius.size());
+        for (uint32_t m = 0; m < M; ++m) {
+            const uint32_t k0 = starts[m], k1 = m + 1 < M ? starts[m + 1] : L;
+            float mx = 0.0f;
+            for (uint32_t k = k0; k < k1; ++k) {
+                mx = std::max(mx, std::max(maj[k], 0.00000001f));
+                h.trk_map[size_t(b) * L + k] = uint16_t(m);
+            }
+            h.trk_maj.push_back(mx);
+            h.trk_radius.push_back(s->host_ground_radius + float(k0) * dzl);
+        }
+        h.trk_maj.push_back(0.0f);
+        h.trk_radius.push_back(s->host_ground_radius + s->host_top);
+    }
+    return upload_tracking_grid(s, h);
+}
+
 }  // namespace
 
 extern "C" {
+
+int sky_cuda_scene_set_tuning(SkyScene* s, const SkyTuning* t) {
+    if (!s || !t) return set_error(SKY_ERR_INVALID_CONFIG, "scene and tuning must not be null");
+    if (t->pool_variant > 1) return set_error(SKY_ERR_INVALID_CONFIG, "unknown pool variant");
+    if (t->max_blocks_per_sm > 64) return set_error(SKY_ERR_INVALID_CONFIG, "max_blocks_per_sm out of range");
+    if (t->pixels_per_group > kPoolMaxCells)
+        return set_error(SKY_ERR_INVALID_CONFIG, "pixels_per_group out of range");
+    if (!(t->crossing_cost <= 0.0f) && !(t->crossing_cost < 1e6f))
+        return set_error(SKY_ERR_INVALID_CONFIG, "crossing_cost out of range");
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    if (t->crossing_cost > 0.0f && t->crossing_cost != s->tuning.crossing_cost) {
+        int st = rebuild_tracking_grid(s, double(t->crossing_cost));
+        if (st) return st;
+    }
+    const float keep = s->tuning.crossing_cost;
+    s->tuning = *t;
+    if (!(t->crossing_cost > 0.0f)) s->tuning.crossing_cost = keep;
+    return SKY_OK;
+}
+
+int sky_cuda_scene_get_tuning(const SkyScene* s, SkyTuning* t) {
+    if (!s || !t) return set_error(SKY_ERR_INVALID_CONFIG, "scene and tuning must not be null");
+    *t = s->tuning;
+    return SKY_OK;
+}
+
 
 const char* sky_cuda_version(void) { return "sky_cuda 0.1.0 (abi 1, sm_103a)"; }
 
@@ -331,11 +437,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     size_t o_pv = reserve(h.phase_values.size() * sizeof(float));
     size_t o_pc = reserve(h.phase_cdf.size() * sizeof(float));
     size_t o_pp = reserve(h.phase_bin_pdf.size() * sizeof(float));
-    size_t o_tr = reserve(h.trk_radius.size() * sizeof(float));
-    size_t o_tm = reserve(h.trk_maj.size() * sizeof(float));
-    size_t o_tp = reserve(h.trk_map.size() * sizeof(uint16_t));
-    size_t o_tc = reserve(h.trk_count.size() * sizeof(uint32_t));
-    size_t o_to = reserve(h.trk_off.size() * sizeof(uint32_t));
+
     std::vector<unsigned char> host(off, 0);
     auto put = [&](size_t at, const void* src, size_t bytes) { std::memcpy(host.data() + at, src, bytes); };
     put(o_knot, h.knot_z.data(), h.knot_z.size() * sizeof(float));
@@ -348,11 +450,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     put(o_pv, h.phase_values.data(), h.phase_values.size() * sizeof(float));
     put(o_pc, h.phase_cdf.data(), h.phase_cdf.size() * sizeof(float));
     put(o_pp, h.phase_bin_pdf.data(), h.phase_bin_pdf.size() * sizeof(float));
-    put(o_tr, h.trk_radius.data(), h.trk_radius.size() * sizeof(float));
-    put(o_tm, h.trk_maj.data(), h.trk_maj.size() * sizeof(float));
-    put(o_tp, h.trk_map.data(), h.trk_map.size() * sizeof(uint16_t));
-    put(o_tc, h.trk_count.data(), h.trk_count.size() * sizeof(uint32_t));
-    put(o_to, h.trk_off.data(), h.trk_off.size() * sizeof(uint32_t));
+
     if ((e = cudaMalloc(&s->blob, off)) != cudaSuccess) {
         delete s;
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "scene table allocation", e);
@@ -374,11 +472,15 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->dev.phase_values = reinterpret_cast<const float*>(base + o_pv);
     s->dev.phase_cdf = reinterpret_cast<const float*>(base + o_pc);
     s->dev.phase_bin_pdf = reinterpret_cast<const float*>(base + o_pp);
-    s->dev.trk_radius = reinterpret_cast<const float*>(base + o_tr);
-    s->dev.trk_maj = reinterpret_cast<const float*>(base + o_tm);
-    s->dev.trk_map = reinterpret_cast<const uint16_t*>(base + o_tp);
-    s->dev.trk_count = reinterpret_cast<const uint32_t*>(base + o_tc);
-    s->dev.trk_off = reinterpret_cast<const uint32_t*>(base + o_to);
+    s->host_majorants = h.majorants;
+    s->host_layers = desc->majorant_layers;
+    s->host_ground_radius = desc->ground_radius_km;
+    s->host_top = desc->top_altitude_km;
+    s->tuning.crossing_cost = float(kDefaultCrossingCost);
+    if ((st = upload_tracking_grid(s, h))) {
+        sky_cuda_scene_destroy(s);
+        return st;
+    }
     s->has_xyz = h.has_xyz;
     cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
     if ((e = cudaMalloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
@@ -400,6 +502,7 @@ void sky_cuda_scene_destroy(SkyScene* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_workspace(s);
+    cudaFree(s->trk_blob);
     cudaFree(s->jobs);
     cudaFree(s->work_counter);
     cudaFree(s->blob);

@@ -17,7 +17,7 @@ cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* ce
 
 // Block path pool of the persistent wavefront kernel (trace_pool.cu).
 constexpr uint32_t kPoolThreads = 256;
-constexpr uint32_t kPoolSlots = 1024;     // paths resident per block (a multiple of kPoolThreads)
+constexpr uint32_t kPoolMaxSlotsPerThread = 4;  // variant 0: 4 slots/thread, 2 blocks/SM; 1: 2 and 3
 constexpr uint32_t kPoolRing = 4;         // work groups in flight per block
 constexpr uint32_t kPoolMaxCells = 256;   // (pixel, band) cells per work group
 
@@ -35,6 +35,7 @@ struct PoolLaunch {
     uint32_t total_groups;
     PoolLayout layout;
     uint32_t max_blocks_per_sm;    // 0 = as many as fit
+    uint32_t variant;              // pool shape (slots per thread, blocks per SM)
     uint32_t tracking, phase_sampling;
     uint32_t* work_counter;        // zeroed before the launch
     unsigned long long* counters;  // may be null
@@ -44,7 +45,8 @@ struct PoolLaunch {
 // Persistent wavefront tracer over a job table.  Writes the cell sums, film
 // and XYZ of every job directly (no finalize launch needed).
 cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream);
-PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables);
+PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables, uint32_t variant);
+uint32_t pool_slots_per_thread(uint32_t variant);
 
 // Mean film, XYZ and XYZ variance from the per-cell sums (any output may be
 // null; xyz_var needs cell_sumsq).

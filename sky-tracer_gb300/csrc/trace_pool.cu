@@ -37,7 +37,7 @@ namespace {
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr uint32_t kThreads = kPoolThreads;
 constexpr uint32_t kWarps = kThreads / 32u;
-constexpr uint32_t kSlots = kPoolSlots;
+constexpr uint32_t kMaxSlots = kPoolThreads * kPoolMaxSlotsPerThread;
 constexpr uint32_t kRing = kPoolRing;
 constexpr uint32_t kMaxCells = kPoolMaxCells;
 // Upper bound on the phase iterations of one block in one launch (a block
@@ -74,35 +74,48 @@ struct PoolHeader {
     RingEntry ring[kRing];
     uint32_t order[kRing];  // active ring entries, oldest first
     uint32_t ring_count, no_more_work, fetch, _pad;
-    uint32_t list_count[4];
+    uint32_t list_count[5];
     uint32_t warp_totals[kWarps];
 };
 
+template <uint32_t kSlots>
 struct PoolSmem {
+    static constexpr uint32_t slots_n = kSlots;
     PoolHeader* hdr;
     DevJob* jobs;       // [kRing] job constants of the ring entries
     double* acc;        // [kRing][kMaxCells][2]
     uint32_t* slots;    // [F_COUNT][kSlots]
-    uint16_t* lists;    // [4][kSlots]
+    uint16_t* lists;    // [5][kSlots]: 0 trace, 1-3 shade, 4 free
     __device__ __forceinline__ uint32_t& u(uint32_t f, uint32_t s) const { return slots[f * kSlots + s]; }
     __device__ __forceinline__ float& f(uint32_t fld, uint32_t s) const {
         return reinterpret_cast<float*>(slots)[fld * kSlots + s];
     }
 };
 
+// F_CELL packs the cell within the work group (9 bits), the band (8 bits) and
+// the ring entry (3 bits), so the hot phases need no integer division.
+__device__ __forceinline__ uint32_t pack_cell(uint32_t cell, uint32_t band, uint32_t ring) {
+    return cell | (band << 9) | (ring << 17);
+}
+__device__ __forceinline__ uint32_t cell_of(uint32_t c) { return c & 0x1ffu; }
+__device__ __forceinline__ uint32_t band_of(uint32_t c) { return (c >> 9) & 0xffu; }
+__device__ __forceinline__ uint32_t ring_of(uint32_t c) { return c >> 17; }
+
 // Registers of one path while a thread shades it.
 struct Path {
-    uint32_t slot, cell, ring, meta;
+    uint32_t slot, cell, band, ring, meta;
     Rng rng;
     V3 o, dir, ldir;
     float thr, rad, nee, alt, t;
 };
 
-__device__ __forceinline__ void load_path(const PoolSmem& P, uint32_t s, Path& p) {
+template <class PS>
+__device__ __forceinline__ void load_path(const PS& P, uint32_t s, Path& p) {
     p.slot = s;
     const uint32_t c = P.u(F_CELL, s);
-    p.cell = c & 0xffffu;
-    p.ring = c >> 16;
+    p.cell = cell_of(c);
+    p.band = band_of(c);
+    p.ring = ring_of(c);
     p.rng.k0 = P.u(F_K0, s);
     p.rng.k1 = P.u(F_K1, s);
     p.rng.k2 = P.u(F_K2, s);
@@ -118,9 +131,10 @@ __device__ __forceinline__ void load_path(const PoolSmem& P, uint32_t s, Path& p
     p.t = P.f(F_T, s);
 }
 
-__device__ __forceinline__ void store_path(const PoolSmem& P, const Path& p) {
+template <class PS>
+__device__ __forceinline__ void store_path(const PS& P, const Path& p) {
     const uint32_t s = p.slot;
-    P.u(F_CELL, s) = p.cell | (p.ring << 16);
+    P.u(F_CELL, s) = pack_cell(p.cell, p.band, p.ring);
     P.u(F_K0, s) = p.rng.k0;
     P.u(F_K1, s) = p.rng.k1;
     P.u(F_K2, s) = p.rng.k2;
@@ -271,7 +285,8 @@ __device__ __forceinline__ void copy_words(void* dst, const void* src, uint32_t 
 }
 
 // A path ends: its radiance joins its cell's FP64 sums and the slot frees.
-__device__ __forceinline__ void finish(const PoolSmem& P, Path& p, float result) {
+template <class PS>
+__device__ __forceinline__ void finish(const PS& P, Path& p, float result) {
     const double rd = double(result);
     double* a = P.acc + (size_t(p.ring) * kMaxCells + p.cell) * 2u;
     atomicAdd(a, rd);
@@ -282,7 +297,8 @@ __device__ __forceinline__ void finish(const PoolSmem& P, Path& p, float result)
 
 // Depth checks and the boundary of a new camera/continuation ray
 // (sky_trace.wgsl:709-717); leaves the path waiting for tracking or ends it.
-__device__ __forceinline__ void start_ray(const PoolSmem& P, const DevScene& S, const DevLaunch& L, Path& p,
+template <class PS>
+__device__ __forceinline__ void start_ray(const PS& P, const DevScene& S, const DevLaunch& L, Path& p,
                                           Counters& n, bool& watchdog) {
     const uint32_t depth = depth_of(p.meta);
     if (depth >= L.watchdog_limit) {
@@ -309,10 +325,10 @@ __device__ __forceinline__ void start_ray(const PoolSmem& P, const DevScene& S, 
 // Light samples of the current event (sky_trace.wgsl:566-608) until one needs
 // a shadow ray traced; then the continuation (:728-767) and the next ray.
 // p.o is the event position here.
-template <int kPhase>
-__device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const DevLaunch& L, Path& p, Counters& n,
+template <int kPhase, class PS>
+__device__ void lights_and_continue(const PS& P, const DevScene& S, const DevLaunch& L, Path& p, Counters& n,
                                     bool& watchdog) {
-    const uint32_t band = p.cell % L.band_count;
+    const uint32_t band = p.band;
     const bool ground = (p.meta & M_GROUND) != 0u;
     uint32_t light = light_of(p.meta);
     while (light < L.direct_light_samples) {
@@ -375,8 +391,9 @@ __device__ void lights_and_continue(const PoolSmem& P, const DevScene& S, const 
 }
 
 // Build a compacted list of the slots satisfying pred (any order).
-template <class Pred>
-__device__ __forceinline__ void build_list(const PoolSmem& P, uint32_t which, Pred pred) {
+template <class PS, class Pred>
+__device__ __forceinline__ void build_list(const PS& P, uint32_t which, Pred pred) {
+    constexpr uint32_t kSlots = PS::slots_n;
     const uint32_t lane = threadIdx.x & 31u;
     for (uint32_t base = 0; base < kSlots; base += kThreads) {
         const uint32_t s = base + threadIdx.x;
@@ -391,7 +408,9 @@ __device__ __forceinline__ void build_list(const PoolSmem& P, uint32_t which, Pr
 
 // One pass over the slots: tracked rays go to list 1 (shadow results),
 // 2 (real collisions) or 3 (ground / escape).
-__device__ __forceinline__ void build_shade_lists(const PoolSmem& P) {
+template <class PS>
+__device__ __forceinline__ void build_shade_lists(const PS& P) {
+    constexpr uint32_t kSlots = PS::slots_n;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = (1u << lane) - 1u;
     for (uint32_t base = 0; base < kSlots; base += kThreads) {
@@ -410,8 +429,8 @@ __device__ __forceinline__ void build_shade_lists(const PoolSmem& P) {
     }
 }
 
-template <int kTracking, int kPhase>
-__global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restrict__ jobs, uint32_t num_jobs,
+template <int kTracking, int kPhase, uint32_t kPer, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) pool_kernel(const DevJob* __restrict__ jobs, uint32_t num_jobs,
                                                         uint32_t total_groups, PoolLayout lay,
                                                         uint32_t* __restrict__ work_counter,
                                                         unsigned long long* __restrict__ counters,
@@ -420,7 +439,8 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
     const uint32_t tid = threadIdx.x;
     const uint32_t lane = tid & 31u;
     const uint32_t warp = tid >> 5;
-    PoolSmem P;
+    constexpr uint32_t kSlots = kPer * kThreads;
+    PoolSmem<kSlots> P;
     P.hdr = reinterpret_cast<PoolHeader*>(smem + lay.header);
     P.jobs = reinterpret_cast<DevJob*>(smem + lay.jobs);
     P.acc = reinterpret_cast<double*>(smem + lay.acc);
@@ -445,6 +465,8 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
         for (uint32_t r = 0; r < kRing; ++r) P.hdr->ring[r].active = 0;
         P.hdr->ring_count = 0;
         P.hdr->no_more_work = 0;
+        for (uint32_t i = 0; i < 5; ++i) P.hdr->list_count[i] = 0;
+        P.hdr->fetch = 0;
     }
     __syncthreads();
 
@@ -576,62 +598,39 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
         if (P.hdr->no_more_work && P.hdr->ring_count == 0) break;  // every slot is free here
 
         // ---- generate: free slots take the next chains, in ring order ----
+        build_list(P, 4, [&](uint32_t s) { return (P.u(F_META, s) & M_STATE) == S_FREE; });
+        __syncthreads();
         {
-            constexpr uint32_t kPer = kSlots / kThreads;
-            uint32_t free_mask = 0, cnt = 0;
-#pragma unroll
-            for (uint32_t i = 0; i < kPer; ++i) {
-                if ((P.u(F_META, tid + i * kThreads) & M_STATE) == S_FREE) {
-                    free_mask |= 1u << i;
-                    ++cnt;
-                }
-            }
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(kFull, incl, o);
-                if (int(lane) >= o) incl += v;
-            }
-            if (lane == 31) P.hdr->warp_totals[warp] = incl;
-            __syncthreads();
-            uint32_t before = 0, all_free = 0;
-            for (uint32_t w = 0; w < kWarps; ++w) {
-                const uint32_t v = P.hdr->warp_totals[w];
-                if (w < warp) before += v;
-                all_free += v;
-            }
-            uint32_t rank = before + incl - cnt;
-            for (uint32_t i = 0; i < kPer; ++i) {
-                if (!(free_mask & (1u << i))) continue;
-                const uint32_t slot = tid + i * kThreads;
-                // map the rank to (ring entry, chain) in ring order
-                uint32_t q = 0xffffffffu, j = 0, cum = 0;
-                for (uint32_t e = 0; e < P.hdr->ring_count; ++e) {
-                    const uint32_t id = P.hdr->order[e];
-                    const RingEntry& R = P.hdr->ring[id];
+            const uint32_t nfree = P.hdr->list_count[4];
+            uint32_t e = 0, cum = 0;  // ring cursor, advanced monotonically over the ranks
+            for (uint32_t rank = tid; rank < nfree; rank += kThreads) {
+                uint32_t q = 0xffffffffu, j = 0;
+                while (e < P.hdr->ring_count) {
+                    const RingEntry& R = P.hdr->ring[P.hdr->order[e]];
                     const uint32_t rem = R.total - R.issued;
                     if (rank < cum + rem) {
-                        q = id;
+                        q = P.hdr->order[e];
                         j = R.issued + (rank - cum);
                         break;
                     }
                     cum += rem;
+                    ++e;
                 }
-                ++rank;
                 if (q == 0xffffffffu) break;  // later ranks find no chain either
                 const DevJob& J = P.jobs[q];
                 const DevScene& S = J.S;
                 const DevLaunch& L = J.L;
                 const RingEntry& R = P.hdr->ring[q];
                 Path p;
-                p.slot = slot;
+                p.slot = P.lists[4 * kSlots + rank];
                 p.ring = q;
-                p.cell = j % R.cells;
-                const uint32_t sample = L.sample_offset + j / R.cells;
-                const uint32_t band = p.cell % L.band_count;
-                const unsigned long long pixel = R.pixel0 + p.cell / L.band_count;
-                const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
-                p.rng.init(uint32_t(pixel), sample, band, L.seed_lo, L.seed_hi);
+                const uint32_t sample_local = j / R.cells;
+                p.cell = j - sample_local * R.cells;
+                const uint32_t pix_local = p.cell / L.band_count;
+                p.band = p.cell - pix_local * L.band_count;
+                const uint32_t pixel = uint32_t(R.pixel0) + pix_local;
+                const uint32_t y = pixel / L.width, x = pixel - y * L.width;
+                p.rng.init(pixel, L.sample_offset + sample_local, p.band, L.seed_lo, L.seed_hi);
                 p.dir = camera_dir(L, x, y, p.rng);
                 p.o = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
                 p.thr = 1.0f;
@@ -645,14 +644,14 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
             }
             __syncthreads();
             if (tid == 0) {
-                uint32_t left = all_free;
-                for (uint32_t e = 0; e < P.hdr->ring_count && left; ++e) {
-                    RingEntry& R = P.hdr->ring[P.hdr->order[e]];
+                uint32_t left = nfree;
+                for (uint32_t i = 0; i < P.hdr->ring_count && left; ++i) {
+                    RingEntry& R = P.hdr->ring[P.hdr->order[i]];
                     const uint32_t take = min(left, R.total - R.issued);
                     R.issued += take;
                     left -= take;
                 }
-                P.hdr->list_count[0] = P.hdr->list_count[1] = P.hdr->list_count[2] = P.hdr->list_count[3] = 0;
+                for (uint32_t i = 0; i < 5; ++i) P.hdr->list_count[i] = 0;
                 P.hdr->fetch = 0;
             }
             __syncthreads();
@@ -680,9 +679,8 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
                         if (idx < total) {
                             slot = P.lists[idx];
                             const uint32_t c = P.u(F_CELL, slot);
-                            const uint32_t q = c >> 16;
-                            S = &P.jobs[q].S;
-                            band = (c & 0xffffu) % P.jobs[q].L.band_count;
+                            S = &P.jobs[ring_of(c)].S;
+                            band = band_of(c);
                             rng.k0 = P.u(F_K0, slot);
                             rng.k1 = P.u(F_K1, slot);
                             rng.k2 = P.u(F_K2, slot);
@@ -732,7 +730,7 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
                 const DevJob& J = P.jobs[p.ring];
                 const DevScene& S = J.S;
                 const DevLaunch& L = J.L;
-                const uint32_t band = p.cell % L.band_count;
+                const uint32_t band = p.band;
                 const float l_sun = S.bands[band].solar_radiance;
                 if (which == 1) {
                     // shadow result (sky_trace.wgsl:576-581, :600-603); p.o is the event position
@@ -799,9 +797,9 @@ __global__ void __launch_bounds__(kThreads, 2) pool_kernel(const DevJob* __restr
     if (__any_sync(kFull, stalled) && lane == 0) atomicOr(status, 2u);
 }
 
-template <int kTracking, int kPhase>
+template <int kTracking, int kPhase, uint32_t kPer, int kMinBlocks>
 cudaError_t launch_one(const PoolLaunch& w, cudaStream_t stream) {
-    auto fn = pool_kernel<kTracking, kPhase>;
+    auto fn = pool_kernel<kTracking, kPhase, kPer, kMinBlocks>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(w.layout.total));
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -818,11 +816,19 @@ cudaError_t launch_one(const PoolLaunch& w, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+template <int kTracking, int kPhase>
+cudaError_t launch_variant(const PoolLaunch& w, cudaStream_t stream) {
+    if (w.variant == 1) return launch_one<kTracking, kPhase, 2u, 3>(w, stream);
+    return launch_one<kTracking, kPhase, 4u, 2>(w, stream);
+}
+
 }  // namespace
+
+uint32_t pool_slots_per_thread(uint32_t variant) { return variant == 1 ? 2u : 4u; }
 
 cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream) {
 #define SKY_POOL_CASE(TR, PH) \
-    if (w.tracking == TR && w.phase_sampling == PH) return launch_one<TR, PH>(w, stream);
+    if (w.tracking == TR && w.phase_sampling == PH) return launch_variant<TR, PH>(w, stream);
     SKY_POOL_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_ISOTROPIC)
     SKY_POOL_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_TABULATED)
     SKY_POOL_CASE(SKY_TRACKING_RESIDUAL_CARRY, SKY_PHASE_ISOTROPIC)
@@ -833,7 +839,8 @@ cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream) {
     return cudaErrorInvalidValue;
 }
 
-PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables) {
+PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables, uint32_t variant) {
+    const uint32_t kSlots = kThreads * pool_slots_per_thread(variant);
     PoolLayout l{};
     size_t off = 0;
     auto take = [&off](size_t bytes) {
@@ -845,7 +852,7 @@ PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_t
     l.jobs = take(kRing * sizeof(DevJob));
     l.acc = take(size_t(kRing) * kMaxCells * 2u * sizeof(double));
     l.slots = take(size_t(F_COUNT) * kSlots * 4u);
-    l.lists = take(4u * kSlots * 2u);
+    l.lists = take(5u * kSlots * 2u);
     l.staged = stage_tables ? 1u : 0u;
     if (stage_tables) {
         l.knot_z_bytes = S.knot_count * 4u;

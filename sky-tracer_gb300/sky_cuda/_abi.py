@@ -103,6 +103,13 @@ class SkyDeviceOutputs(ctypes.Structure):
     ]
 
 
+class SkyTuning(ctypes.Structure):
+    _fields_ = [
+        ("pool_variant", _u32), ("max_blocks_per_sm", _u32), ("stage_tables", _u32), ("pixels_per_group", _u32),
+        ("crossing_cost", _f), ("_reserved", _u32 * 3),
+    ]
+
+
 assert ctypes.sizeof(SkySceneDesc) == 120
 assert ctypes.sizeof(SkyRenderConfig) == 80
 assert ctypes.sizeof(SkyRenderStats) == 96
@@ -113,6 +120,8 @@ _SIGNATURES = {
     "sky_cuda_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "sky_cuda_scene_create": (ctypes.c_int, [ctypes.POINTER(SkySceneDesc), ctypes.POINTER(_vp)]),
     "sky_cuda_scene_destroy": (None, [_vp]),
+    "sky_cuda_scene_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(SkyTuning)]),
+    "sky_cuda_scene_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(SkyTuning)]),
     "sky_cuda_render": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t,
                                        ctypes.POINTER(SkyRenderStats)]),
     "sky_cuda_render_xyz": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t,

@@ -18,7 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import SkyDeviceOutputs, SkyRenderConfig, SkyRenderStats, check, load_library
+from ._abi import SkyDeviceOutputs, SkyRenderConfig, SkyRenderStats, SkyTuning, check, load_library
 from .scene import Scene
 
 DEFAULT_SEED = 0x5EC7_2026_0430  # config.rs:44
@@ -128,6 +128,22 @@ class GpuScene:
             self.close()
         except Exception:
             pass
+
+    def get_tuning(self) -> dict:
+        t = SkyTuning()
+        check(self.lib.sky_cuda_scene_get_tuning(self.handle, ctypes.byref(t)), self.lib)
+        return {"pool_variant": t.pool_variant, "max_blocks_per_sm": t.max_blocks_per_sm,
+                "stage_tables": t.stage_tables, "pixels_per_group": t.pixels_per_group,
+                "crossing_cost": float(t.crossing_cost)}
+
+    def set_tuning(self, **kw) -> None:
+        """Set launch-shape fields of SkyTuning (unnamed fields keep their value)."""
+        cur = self.get_tuning()
+        cur.update(kw)
+        t = SkyTuning()
+        for k, v in cur.items():
+            setattr(t, k, v)
+        check(self.lib.sky_cuda_scene_set_tuning(self.handle, ctypes.byref(t)), self.lib)
 
     def render(self, config: RenderConfig) -> tuple[Film, RenderStats]:
         film = np.empty(config.pixels * self.band_count, dtype=np.float32)

@@ -229,3 +229,32 @@ def test_reference_default_band_count(gpu, ref_scene):
     r = parity_report(xg, vg, xo, vo)
     print("reference scene parity", r)
     assert st == 0 and r["frac_beyond_3se"] <= 0.03
+
+
+@pytest.mark.parametrize("variant,stage,cost", [(0, 0, 0.25), (0, 1, 0.5), (1, 0, 0.1), (1, 1, 1.0)])
+def test_pool_shapes_trace_the_same_chains(gpu, cfg0_scene, variant, stage, cost):
+    """Every launch shape the autotuner can pick traces the plain kernel's
+    paths (the crossing cost changes the tracking grid for both kernels)."""
+    with GpuScene(cfg0_scene) as gs:
+        gs.set_tuning(pool_variant=variant, stage_tables=stage, crossing_cost=cost)
+        t = gs.get_tuning()
+        assert t["pool_variant"] == variant and t["stage_tables"] == stage and abs(t["crossing_cost"] - cost) < 1e-6
+        cfg = RenderConfig(width=32, height=16, spp=2, sample_offset=5, phase_sampling=_abi.PHASE_TABULATED,
+                           tracking=_abi.TRACKING_MERGED_LAYERS, max_orders=16)
+        a, _, _, _ = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_PLAIN}))
+        b, _, _, _ = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_WAVEFRONT}))
+    close = np.abs(a - b) <= 1e-5 * np.maximum(np.abs(a), np.abs(b)) + 1e-12
+    assert close.mean() >= 0.999
+
+
+def test_autotuner_picks_a_measured_shape(gpu, cfg0_scene):
+    from sky_cuda.autotune import autotune
+    cfg = RenderConfig(width=64, height=32, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    with GpuScene(cfg0_scene) as gs:
+        best, results = autotune(gs, cfg, space={"pool_variant": (0, 1), "crossing_cost": (0.25, 0.5)})
+        assert len(results) == 4 and all(ms > 0 for _, ms in results)
+        assert best == min(results, key=lambda r: r[1])[0]
+        assert gs.get_tuning() == best
+        film, _ = gs.render(cfg)
+        assert np.all(np.isfinite(film.values))
