@@ -477,6 +477,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->host_ground_radius = desc->ground_radius_km;
     s->host_top = desc->top_altitude_km;
     s->tuning.crossing_cost = float(kDefaultCrossingCost);
+    s->tuning.pool_variant = 1;  // 512 resident paths, 3 blocks per SM: the autotuner's usual pick
     if ((st = upload_tracking_grid(s, h))) {
         sky_cuda_scene_destroy(s);
         return st;
