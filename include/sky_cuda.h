@@ -300,6 +300,36 @@ int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config
 int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
                            const SkyDeviceOutputs* outputs, void* cuda_stream);
 
+/*
+ * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
+ * single launch of the persistent tracer.  No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while rendering: engines
+ * that reserve all device memory up front through their own allocator, or
+ * that forbid allocations on their render path.  Such a caller creates the
+ * scene once at start-up, owns every output buffer, and renders through this
+ * call, which calls no cudaMalloc, cudaFree or allocating library routine.
+ *
+ * configs[i] / outputs[i] describe job i exactly as in
+ * sky_cuda_render_device(); every job must use the same tracking mode and
+ * phase sampling.  outputs[0].status is required and receives the watchdog
+ * bits of the whole batch (OR-ed in; the caller clears it); outputs[0].counters
+ * receives the batch's event counts.  More than SKY_NOALLOC_MAX_JOBS jobs are
+ * rejected with SKY_ERR_INVALID_CONFIG.
+ *
+ * The kernel's job table and work counter live in one fixed scratch area of
+ * the library (SKY_NOALLOC_SCRATCH_BYTES of device memory on every GPU that
+ * loads it, held until the process exits).  The first call on a device looks
+ * up that area's address (set-up once per device), so make it before any
+ * stream capture.  All calls share the area and it keeps the last call's
+ * contents: calls that overlap on the GPU (different streams without
+ * ordering, or different host threads) race on it, so order them.
+ */
+#define SKY_NOALLOC_MAX_JOBS 16u
+#define SKY_NOALLOC_SCRATCH_BYTES 16384u
+int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* configs,
+                                  const SkyDeviceOutputs* outputs, uint32_t job_count, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

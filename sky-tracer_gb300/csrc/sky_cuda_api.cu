@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstddef>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -551,3 +553,111 @@ int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
 }
 
 }  // extern "C"
+
+// ---- allocation-free batch render -------------------------------------------------
+
+namespace {
+
+struct NoAllocScratch {
+    DevJob jobs[SKY_NOALLOC_MAX_JOBS];
+    uint32_t work_counter;
+};
+static_assert(sizeof(NoAllocScratch) <= SKY_NOALLOC_SCRATCH_BYTES, "scratch area too small");
+
+// The job table and work counter of sky_cuda_render_batch_noalloc().  Host
+// code may not use this name as a device address: it is resolved per device
+// with cudaGetSymbolAddress() below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SKY_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch area on `device` (which must be current).
+int noalloc_scratch(int device, void** out) {
+    if (device < 0 || device >= kNoAllocMaxDevices)
+        return set_error(SKY_ERR_DEVICE_INIT, "device ordinal beyond the allocation-free scratch table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_DEVICE_INIT, "locating the allocation-free scratch area", e);
+        g_noalloc_address[device] = ptr;
+    }
+    *out = g_noalloc_address[device];
+    return SKY_OK;
+}
+
+}  // namespace
+
+extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* configs,
+                                             const SkyDeviceOutputs* outputs, uint32_t job_count,
+                                             void* cuda_stream) {
+    if (!scene || !configs || !outputs) return set_error(SKY_ERR_INVALID_CONFIG, "scene, configs and outputs are required");
+    if (job_count == 0) return set_error(SKY_ERR_INVALID_CONFIG, "job_count must be at least 1");
+    if (job_count > SKY_NOALLOC_MAX_JOBS)
+        return set_error(SKY_ERR_INVALID_CONFIG, "job_count " + std::to_string(job_count) +
+                                                     " exceeds SKY_NOALLOC_MAX_JOBS (" +
+                                                     std::to_string(SKY_NOALLOC_MAX_JOBS) + ")");
+    if (!outputs[0].status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[0].status is required");
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    const uint32_t B = s->dev.band_count;
+    NoAllocScratch image;
+    std::memset(&image, 0, sizeof(image));
+    uint32_t groups = 0;
+    for (uint32_t i = 0; i < job_count; ++i) {
+        const SkyRenderConfig* c = &configs[i];
+        int st = validate_config(s, c);
+        if (st) return st;
+        if (c->tracking != configs[0].tracking || c->phase_sampling != configs[0].phase_sampling)
+            return set_error(SKY_ERR_INVALID_CONFIG, "all jobs of a batch need the same tracking and phase sampling");
+        if (!outputs[i].cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[i].cell_sum is required");
+        const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
+        const uint64_t pixels = uint64_t(c->width) * c->height;
+        DevJob& job = image.jobs[i];
+        job.S = s->dev;
+        job.L = make_launch(s, c);
+        job.cell_sum = outputs[i].cell_sum;
+        job.cell_sumsq = outputs[i].cell_sumsq;
+        job.film = outputs[i].film;
+        job.xyz = s->has_xyz ? outputs[i].xyz : nullptr;
+        job.xyz_var = s->has_xyz ? outputs[i].xyz_var : nullptr;
+        job.accumulate = accumulate ? 1u : 0u;
+        job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
+        job.pixels_per_group = s->tuning.pixels_per_group
+                                   ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
+                                   : pixels_per_group(B, c->spp, s->tuning.pool_variant);
+        job.pixels_per_group = std::max(1u, job.pixels_per_group);
+        job.group_begin = groups;
+        job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
+        if (uint64_t(groups) + job.group_count > 0xffffffffull)
+            return set_error(SKY_ERR_INVALID_CONFIG, "batch has too many work groups");
+        groups += job.group_count;
+    }
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    void* scratch = nullptr;
+    int st = noalloc_scratch(s->device, &scratch);
+    if (st) return st;
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    // job table and a zeroed work counter, in one copy (the counter must start at zero)
+    cudaError_t e = cudaMemcpyAsync(scratch, &image, sizeof(image), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "job table upload", e);
+    PoolLaunch w{};
+    w.jobs = static_cast<const DevJob*>(scratch);
+    w.num_jobs = job_count;
+    w.total_groups = groups;
+    w.tracking = configs[0].tracking;
+    w.phase_sampling = configs[0].phase_sampling;
+    w.work_counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
+                                                 offsetof(NoAllocScratch, work_counter));
+    w.counters = outputs[0].counters;
+    w.status = outputs[0].status;
+    const bool with_maj = configs[0].tracking != SKY_TRACKING_MERGED_LAYERS;
+    w.variant = s->tuning.pool_variant;
+    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
+    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
+    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
+    e = launch_trace_pool(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "persistent tracing kernel launch", e);
+    return SKY_OK;
+}

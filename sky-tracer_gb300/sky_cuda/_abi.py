@@ -131,7 +131,10 @@ _SIGNATURES = {
                                             ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
     "sky_cuda_render_device": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                               ctypes.POINTER(SkyDeviceOutputs), _vp]),
+    "sky_cuda_render_batch_noalloc": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
+                                                     ctypes.POINTER(SkyDeviceOutputs), ctypes.c_uint32, _vp]),
 }
+NOALLOC_MAX_JOBS = 16
 
 _LIB = None
 
