@@ -54,6 +54,9 @@ WORKLOADS = {
                                       rr_start_depth=8, max_orders=0),
 }
 DEFAULT_WORKLOAD = "plain-512x256-81wl-256spp"
+# configs[2]: 32 sun elevations on [-6, 90] (denser near the horizon), each a
+# 256x128 sky-view LUT over 40 wavelengths, spp 64-1024 from a 16-spp pilot
+SWEEP_WORKLOAD = "sweep-32x256x128-40wl"
 
 
 def parse_args():
@@ -62,7 +65,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    p.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD], default=DEFAULT_WORKLOAD)
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
@@ -229,10 +232,105 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_sweep(args):
+    """Batched elevation sweep (one persistent launch, CUDA graph, per-elevation
+    budgets) against 32 separate plain-kernel launches, at equal error."""
+    import torch
+    from sky_cuda import GpuScene, RenderConfig, synthetic_scene, wavelengths
+    from sky_cuda import _abi
+    from sky_cuda.sweep import Sweep, elevation_schedule, p95_relative_error, plan_budgets
+    torch.cuda.set_device(0)
+    scene = synthetic_scene(wavelengths(380.0, 780.0, 40), DATA_DIR, sun_elevation_deg=10.0)
+    base = RenderConfig(width=256, height=128, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                        tracking=args.tracking, rr_start_depth=8, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
+    elevations = elevation_schedule(32, -6.0, 90.0)
+    stream = torch.cuda.current_stream().cuda_stream
+    gs = GpuScene(scene)
+    budgets, pilot_p95 = plan_budgets(gs, base, elevations, pilot_spp=16)
+    sweep = Sweep(gs, RenderConfig(**{**base.__dict__, "seed": 0x5EC7_2026_0430}), elevations, budgets)
+    sweep.capture()
+    for _ in range(max(args.warmup, 1)):
+        sweep.replay(stream)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sweep.replay(stream)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    clocks.stop()
+    t_batched = statistics.median(times)
+    errs_batched = sweep.errors()
+    chains_batched = sweep.chains
+
+    # 32 separate plain launches: per-elevation budgets, and one uniform spp
+    singles = [GpuScene(scene.with_sun(float(e))) for e in elevations]
+    cells = base.pixels * scene.band_count
+    bufs = [torch.zeros(cells, dtype=torch.float64, device="cuda") for _ in range(3)]
+    xyz = torch.zeros(base.pixels * 3, dtype=torch.float64, device="cuda")
+    var = torch.zeros(base.pixels * 3, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def plain_pass(spps, keep_errors=False):
+        errs = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for g, e, n in zip(singles, elevations, spps):
+            cfg = RenderConfig(**{**base.__dict__, "spp": int(n), "sun_elevation_deg": float(e),
+                                  "kernel": _abi.KERNEL_PLAIN, "seed": 0x5EC7_2026_0430})
+            g.render_device(cfg, {"cell_sum": bufs[0].data_ptr(), "cell_sumsq": bufs[1].data_ptr(),
+                                  "xyz": xyz.data_ptr(), "xyz_var": var.data_ptr(), "status": status.data_ptr()},
+                            stream)
+            if keep_errors:
+                torch.cuda.synchronize()
+                errs.append(p95_relative_error(xyz.cpu().numpy().reshape(-1, 3), var.cpu().numpy().reshape(-1, 3)))
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3, errs
+
+    plain_pass([16] * len(elevations))  # warm-up
+    t_plain_budget, _ = plain_pass(budgets)
+    uniform = int(budgets.max())
+    t_plain_uniform, errs_plain = plain_pass([uniform] * len(elevations), keep_errors=True)
+    chains_uniform = len(elevations) * cells * uniform
+    out = {
+        "metric": "spectral path samples/s (chains/s)", "value": chains_batched / t_batched, "unit": "chains/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batched * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": SWEEP_WORKLOAD, "elevations": [round(float(e), 3) for e in elevations],
+                   "width": base.width, "height": base.height, "wavelengths": scene.band_count,
+                   "spp_per_elevation": [int(b) for b in budgets], "pilot_spp": 16,
+                   "pilot_p95": [round(float(p), 5) for p in pilot_p95], "projection": "sky-view LUT",
+                   "tracking": ("segment-restart", "residual-carry", "merged-layers")[args.tracking]},
+        "sweep": {
+            "batched_graph_s": t_batched, "batched_chains": chains_batched,
+            "batched_p95_error_max": max(errs_batched), "batched_p95_error": [round(x, 5) for x in errs_batched],
+            "plain_per_elevation_budget_s": t_plain_budget,
+            "plain_uniform_spp": uniform, "plain_uniform_s": t_plain_uniform, "plain_uniform_chains": chains_uniform,
+            "plain_uniform_p95_error_max": max(errs_plain),
+            "speedup_vs_plain_uniform_at_equal_error": t_plain_uniform / t_batched,
+            "speedup_vs_plain_same_budgets": t_plain_budget / t_batched,
+            "plain_chains_per_s": chains_batched / t_plain_budget,
+        },
+        "clocks": clocks.summary(),
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(out))
+    for g in singles:
+        g.close()
+    gs.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == SWEEP_WORKLOAD:
+        return run_sweep(args)
     import torch
     import torch.distributed as dist
     from sky_cuda import GpuScene, render

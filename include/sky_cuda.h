@@ -300,6 +300,42 @@ int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config
 int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
                            const SkyDeviceOutputs* outputs, void* cuda_stream);
 
+/* ---- Batched sweeps ------------------------------------------------------ */
+
+/*
+ * One render of a batch: a config, the sun direction for this render (the
+ * scene's medium, bands and phase tables are shared by the whole batch; an
+ * elevation sweep only moves the sun) and its device outputs.  No
+ * counterpart in the reference, which renders one image per process
+ * (scripts/bake_skyview_elevations.ps1 loops the CLI over elevations).
+ */
+typedef struct SkyBatchJob {
+    SkyRenderConfig config;
+    float sun_direction[3];     /* unit vector; all zero = the scene's sun */
+    float _reserved;
+    SkyDeviceOutputs outputs;   /* as for sky_cuda_render_device; outputs.status is
+                                   used from the first job only */
+} SkyBatchJob;
+
+/*
+ * Render every job of the batch in ONE persistent launch on `cuda_stream`
+ * (asynchronous).  All jobs must share tracking and phase sampling.  The
+ * batch's watchdog bits go to jobs[0].outputs.status, its event counts to
+ * jobs[0].outputs.counters.
+ */
+int sky_cuda_render_batch(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count, void* cuda_stream);
+
+/*
+ * A batch captured once into a CUDA graph (job-table upload, work-counter
+ * reset and the persistent launch) and replayed with one graph launch per
+ * sweep.  The outputs named in `jobs` must stay valid while the graph lives.
+ */
+typedef struct SkyBatchGraph SkyBatchGraph;
+int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count,
+                                SkyBatchGraph** out_graph);
+int sky_cuda_batch_graph_launch(SkyBatchGraph* graph, void* cuda_stream);
+void sky_cuda_batch_graph_destroy(SkyBatchGraph* graph);
+
 /*
  * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
  * single launch of the persistent tracer.  No counterpart in the reference.

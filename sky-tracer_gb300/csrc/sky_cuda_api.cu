@@ -43,6 +43,11 @@ struct SkyScene {
     // persistent-kernel job table and work counter (one job per render call)
     DevJob* jobs = nullptr;
     uint32_t* work_counter = nullptr;
+    // batch job tables: device table + pinned host staging, grown on demand
+    DevJob* batch_jobs = nullptr;
+    DevJob* batch_host = nullptr;
+    uint32_t* batch_counter = nullptr;
+    uint32_t batch_capacity = 0;
     int smem_optin = 0;
     SkyTuning tuning{};
     // merged tracking grid in its own allocation (rebuilt by set_tuning)
@@ -505,6 +510,9 @@ void sky_cuda_scene_destroy(SkyScene* s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     free_workspace(s);
+    cudaFree(s->batch_jobs);
+    cudaFreeHost(s->batch_host);
+    cudaFree(s->batch_counter);
     cudaFree(s->trk_blob);
     cudaFree(s->jobs);
     cudaFree(s->work_counter);
@@ -553,6 +561,198 @@ int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
 }
 
 }  // extern "C"
+
+// ---- batched sweeps ----------------------------------------------------------------
+
+struct SkyBatchGraph {
+    SkyScene* scene = nullptr;
+    DevJob* jobs = nullptr;        // device job table owned by the graph
+    DevJob* host = nullptr;        // pinned copy the graph's memcpy node reads
+    uint32_t* counter = nullptr;
+    uint32_t job_count = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Fill DevJob rows for a batch; returns the total number of work groups.
+int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* out, uint32_t& groups) {
+    if (!s || !jobs || n == 0) return set_error(SKY_ERR_INVALID_CONFIG, "scene and at least one job are required");
+    if (!jobs[0].outputs.status) return set_error(SKY_ERR_INVALID_CONFIG, "jobs[0].outputs.status is required");
+    const uint32_t B = s->dev.band_count;
+    groups = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const SkyRenderConfig* c = &jobs[i].config;
+        int st = validate_config(s, c);
+        if (st) return st;
+        if (c->tracking != jobs[0].config.tracking || c->phase_sampling != jobs[0].config.phase_sampling)
+            return set_error(SKY_ERR_INVALID_CONFIG, "all jobs of a batch need the same tracking and phase sampling");
+        if (!jobs[i].outputs.cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "every job needs outputs.cell_sum");
+        DevJob& job = out[i];
+        job = DevJob{};
+        job.S = s->dev;
+        const float* d = jobs[i].sun_direction;
+        const float len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        if (len > 0.0f) {
+            if (!std::isfinite(len)) return set_error(SKY_ERR_INVALID_CONFIG, "sun direction must be finite");
+            for (int k = 0; k < 3; ++k) job.S.sun[k] = d[k] / len;
+            host_orthonormal_basis(job.S.sun, job.S.sun_t, job.S.sun_b);
+        }
+        job.L = make_launch(s, c);
+        if (len > 0.0f) {  // the sky-view LUT frame follows the job's sun
+            SkyScene tmp_view;
+            tmp_view.dev = job.S;
+            job.L = make_launch(&tmp_view, c);
+            tmp_view.dev = DevScene{};
+        }
+        const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
+        job.cell_sum = jobs[i].outputs.cell_sum;
+        job.cell_sumsq = jobs[i].outputs.cell_sumsq;
+        job.film = jobs[i].outputs.film;
+        job.xyz = s->has_xyz ? jobs[i].outputs.xyz : nullptr;
+        job.xyz_var = s->has_xyz ? jobs[i].outputs.xyz_var : nullptr;
+        job.accumulate = accumulate ? 1u : 0u;
+        job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
+        job.pixels_per_group = s->tuning.pixels_per_group ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
+                                                           : pixels_per_group(B, c->spp, s->tuning.pool_variant);
+        job.pixels_per_group = std::max(1u, job.pixels_per_group);
+        const uint64_t pixels = uint64_t(c->width) * c->height;
+        job.group_begin = groups;
+        job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
+        if (uint64_t(groups) + job.group_count > 0xffffffffull)
+            return set_error(SKY_ERR_INVALID_CONFIG, "batch has too many work groups");
+        groups += job.group_count;
+    }
+    return SKY_OK;
+}
+
+PoolLaunch batch_launch(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, const DevJob* dev_jobs, uint32_t groups,
+                        uint32_t* counter) {
+    PoolLaunch w{};
+    w.jobs = dev_jobs;
+    w.num_jobs = n;
+    w.total_groups = groups;
+    w.tracking = jobs[0].config.tracking;
+    w.phase_sampling = jobs[0].config.phase_sampling;
+    w.work_counter = counter;
+    w.counters = jobs[0].outputs.counters;
+    w.status = jobs[0].outputs.status;
+    const bool with_maj = w.tracking != SKY_TRACKING_MERGED_LAYERS;
+    w.variant = s->tuning.pool_variant;
+    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
+    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
+    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
+    return w;
+}
+
+int ensure_batch_capacity(SkyScene* s, uint32_t n) {
+    if (n <= s->batch_capacity) return SKY_OK;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->batch_jobs);
+    cudaFreeHost(s->batch_host);
+    cudaFree(s->batch_counter);
+    s->batch_jobs = nullptr;
+    s->batch_host = nullptr;
+    s->batch_counter = nullptr;
+    s->batch_capacity = 0;
+    cudaError_t e;
+    if ((e = cudaMalloc(&s->batch_jobs, size_t(n) * sizeof(DevJob))) != cudaSuccess ||
+        (e = cudaMallocHost(&s->batch_host, size_t(n) * sizeof(DevJob))) != cudaSuccess ||
+        (e = cudaMalloc(&s->batch_counter, sizeof(uint32_t))) != cudaSuccess)
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch job table allocation", e);
+    s->batch_capacity = n;
+    return SKY_OK;
+}
+
+}  // namespace
+
+extern "C" int sky_cuda_render_batch(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count,
+                                     void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    if (!s) return set_error(SKY_ERR_INVALID_CONFIG, "scene is null");
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    int st = ensure_batch_capacity(s, job_count);
+    if (st) return st;
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    // the previous batch may still read the pinned staging table
+    cudaStreamSynchronize(stream);
+    uint32_t groups = 0;
+    if ((st = build_batch_jobs(s, jobs, job_count, s->batch_host, groups))) return st;
+    cudaError_t e = cudaMemcpyAsync(s->batch_jobs, s->batch_host, size_t(job_count) * sizeof(DevJob),
+                                    cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->batch_counter, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "batch job table upload", e);
+    PoolLaunch w = batch_launch(s, jobs, job_count, s->batch_jobs, groups, s->batch_counter);
+    e = launch_trace_pool(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "batched persistent launch", e);
+    return SKY_OK;
+}
+
+extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count,
+                                           SkyBatchGraph** out_graph) {
+    if (!out_graph) return set_error(SKY_ERR_INVALID_CONFIG, "out_graph is null");
+    *out_graph = nullptr;
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    if (!s) return set_error(SKY_ERR_INVALID_CONFIG, "scene is null");
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    SkyBatchGraph* g = new SkyBatchGraph();
+    g->scene = s;
+    g->job_count = job_count;
+    uint32_t groups = 0;
+    cudaError_t e;
+    int st = SKY_OK;
+    cudaStream_t cap = nullptr;
+    if ((e = cudaMallocHost(&g->host, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
+        (e = cudaMalloc(&g->jobs, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
+        (e = cudaMalloc(&g->counter, sizeof(uint32_t))) != cudaSuccess) {
+        st = cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch graph allocation", e);
+    } else if ((st = build_batch_jobs(s, jobs, job_count, g->host, groups)) == SKY_OK) {
+        PoolLaunch w = batch_launch(s, jobs, job_count, g->jobs, groups, g->counter);
+        if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+            st = cuda_fail(SKY_ERR_DEVICE_INIT, "graph capture", e);
+        } else {
+            cudaError_t e1 = cudaMemcpyAsync(g->jobs, g->host, size_t(job_count) * sizeof(DevJob),
+                                             cudaMemcpyHostToDevice, cap);
+            cudaError_t e2 = cudaMemsetAsync(g->counter, 0, sizeof(uint32_t), cap);
+            cudaError_t e3 = launch_trace_pool(w, cap);
+            e = cudaStreamEndCapture(cap, &g->graph);
+            if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e != cudaSuccess)
+                st = cuda_fail(SKY_ERR_LAUNCH, "graph capture of the batch",
+                               e3 != cudaSuccess ? e3 : (e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e)));
+            else if ((e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+                st = cuda_fail(SKY_ERR_LAUNCH, "graph instantiation", e);
+        }
+    }
+    if (cap) cudaStreamDestroy(cap);
+    if (st) {
+        sky_cuda_batch_graph_destroy(g);
+        return st;
+    }
+    *out_graph = g;
+    return SKY_OK;
+}
+
+extern "C" int sky_cuda_batch_graph_launch(SkyBatchGraph* g, void* cuda_stream) {
+    if (!g || !g->exec) return set_error(SKY_ERR_INVALID_CONFIG, "graph is null");
+    if (cudaSetDevice(g->scene->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    cudaError_t e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(cuda_stream));
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "graph launch", e);
+    return SKY_OK;
+}
+
+extern "C" void sky_cuda_batch_graph_destroy(SkyBatchGraph* g) {
+    if (!g) return;
+    if (g->scene) cudaSetDevice(g->scene->device);
+    cudaDeviceSynchronize();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFree(g->jobs);
+    cudaFree(g->counter);
+    cudaFreeHost(g->host);
+    delete g;
+}
 
 // ---- allocation-free batch render -------------------------------------------------
 

@@ -110,6 +110,12 @@ class SkyTuning(ctypes.Structure):
     ]
 
 
+class SkyBatchJob(ctypes.Structure):
+    _fields_ = [
+        ("config", SkyRenderConfig), ("sun_direction", _f * 3), ("_reserved", _f), ("outputs", SkyDeviceOutputs),
+    ]
+
+
 assert ctypes.sizeof(SkySceneDesc) == 120
 assert ctypes.sizeof(SkyRenderConfig) == 80
 assert ctypes.sizeof(SkyRenderStats) == 96
@@ -131,6 +137,11 @@ _SIGNATURES = {
                                             ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
     "sky_cuda_render_device": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                               ctypes.POINTER(SkyDeviceOutputs), _vp]),
+    "sky_cuda_render_batch": (ctypes.c_int, [_vp, ctypes.POINTER(SkyBatchJob), ctypes.c_uint32, _vp]),
+    "sky_cuda_batch_graph_create": (ctypes.c_int, [_vp, ctypes.POINTER(SkyBatchJob), ctypes.c_uint32,
+                                                   ctypes.POINTER(_vp)]),
+    "sky_cuda_batch_graph_launch": (ctypes.c_int, [_vp, _vp]),
+    "sky_cuda_batch_graph_destroy": (None, [_vp]),
     "sky_cuda_render_batch_noalloc": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                                      ctypes.POINTER(SkyDeviceOutputs), ctypes.c_uint32, _vp]),
 }

@@ -18,7 +18,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import SkyDeviceOutputs, SkyRenderConfig, SkyRenderStats, SkyTuning, check, load_library
+from ._abi import (SkyBatchJob, SkyDeviceOutputs, SkyRenderConfig, SkyRenderStats, SkyTuning, check,
+                   load_library)
 from .scene import Scene
 
 DEFAULT_SEED = 0x5EC7_2026_0430  # config.rs:44
@@ -165,6 +166,14 @@ class GpuScene:
         f = Film(config.width, config.height, self.band_count, film) if film is not None else None
         return f, xyz, var, RenderStats.from_c(stats)
 
+    def render_batch(self, jobs, stream: int = 0) -> None:
+        """One persistent launch over [(RenderConfig, sun_direction or None, outputs), ...]."""
+        arr = batch_jobs(jobs)
+        check(self.lib.sky_cuda_render_batch(self.handle, arr, len(jobs), ctypes.c_void_p(stream)), self.lib)
+
+    def batch_graph(self, jobs) -> "BatchGraph":
+        return BatchGraph(self, jobs)
+
     def render_device(self, config: RenderConfig, outputs: dict, stream: int = 0) -> None:
         """Queue a render into device buffers given as integer device pointers
         (keys: cell_sum, cell_sumsq, film, xyz, xyz_var, counters, status)."""
@@ -173,6 +182,50 @@ class GpuScene:
             setattr(o, name, outputs.get(name) or None)
         check(self.lib.sky_cuda_render_device(self.handle, ctypes.byref(config.to_c()), ctypes.byref(o),
                                               ctypes.c_void_p(stream)), self.lib)
+
+
+def _device_outputs(outputs: dict) -> SkyDeviceOutputs:
+    o = SkyDeviceOutputs()
+    for name, _ in SkyDeviceOutputs._fields_:
+        setattr(o, name, outputs.get(name) or None)
+    return o
+
+
+def batch_jobs(jobs) -> ctypes.Array:
+    """SkyBatchJob array from [(RenderConfig, sun_direction or None, outputs dict), ...]."""
+    arr = (SkyBatchJob * len(jobs))()
+    for i, (cfg, sun, outs) in enumerate(jobs):
+        arr[i].config = cfg.to_c()
+        arr[i].sun_direction = (ctypes.c_float * 3)(*(sun if sun is not None else (0.0, 0.0, 0.0)))
+        arr[i].outputs = _device_outputs(outs)
+    return arr
+
+
+class BatchGraph:
+    """A batch captured once into a CUDA graph (sky_cuda_batch_graph_create)
+    and replayed with launch(); the outputs must outlive the graph."""
+
+    def __init__(self, gs: "GpuScene", jobs):
+        self.lib = gs.lib
+        self._jobs = batch_jobs(jobs)
+        handle = ctypes.c_void_p()
+        check(self.lib.sky_cuda_batch_graph_create(gs.handle, self._jobs, len(jobs), ctypes.byref(handle)),
+              self.lib)
+        self.handle = handle
+
+    def launch(self, stream: int = 0) -> None:
+        check(self.lib.sky_cuda_batch_graph_launch(self.handle, ctypes.c_void_p(stream)), self.lib)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and self.handle.value:
+            self.lib.sky_cuda_batch_graph_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def render(scene: Scene, config: RenderConfig) -> Film:

@@ -44,7 +44,7 @@ def test_struct_layouts_match_header(tmp_path):
     ctypes_structs = {
         "SkySceneDesc": _abi.SkySceneDesc, "SkyRenderConfig": _abi.SkyRenderConfig,
         "SkyRenderStats": _abi.SkyRenderStats, "SkyDeviceOutputs": _abi.SkyDeviceOutputs,
-        "SkyTuning": _abi.SkyTuning,
+        "SkyTuning": _abi.SkyTuning, "SkyBatchJob": _abi.SkyBatchJob,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for name, dt in structs.items():
