@@ -238,7 +238,7 @@ def run_sweep(args):
     import torch
     from sky_cuda import GpuScene, RenderConfig, synthetic_scene, wavelengths
     from sky_cuda import _abi
-    from sky_cuda.sweep import Sweep, elevation_schedule, p95_relative_error, plan_budgets
+    from sky_cuda.sweep import Sweep, elevation_schedule, p95_relative_error, plan_budgets, spp_for_target
     torch.cuda.set_device(0)
     scene = synthetic_scene(wavelengths(380.0, 780.0, 40), DATA_DIR, sun_elevation_deg=10.0)
     base = RenderConfig(width=256, height=128, spp=64, phase_sampling=_abi.PHASE_TABULATED,
@@ -297,6 +297,11 @@ def run_sweep(args):
     uniform = int(budgets.max())
     t_plain_uniform, errs_plain = plain_pass([uniform] * len(elevations), keep_errors=True)
     chains_uniform = len(elevations) * cells * uniform
+    # time to bring every elevation to 1 % p95 error, extrapolated (error^2 ~ 1/spp)
+    need_b = spp_for_target(errs_batched, budgets, 0.01)
+    t1_batched = t_batched * float(need_b.sum()) / float(np.sum(budgets))
+    need_u = spp_for_target(errs_plain, [uniform] * len(elevations), 0.01)
+    t1_plain_uniform = t_plain_uniform * float(need_u.max()) / uniform
     out = {
         "metric": "spectral path samples/s (chains/s)", "value": chains_batched / t_batched, "unit": "chains/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batched * 1e3,
@@ -313,6 +318,8 @@ def run_sweep(args):
             "plain_uniform_spp": uniform, "plain_uniform_s": t_plain_uniform, "plain_uniform_chains": chains_uniform,
             "plain_uniform_p95_error_max": max(errs_plain),
             "speedup_vs_plain_uniform_at_equal_error": t_plain_uniform / t_batched,
+            "time_to_1pct_batched_s": t1_batched, "time_to_1pct_plain_uniform_s": t1_plain_uniform,
+            "speedup_time_to_1pct": t1_plain_uniform / t1_batched,
             "speedup_vs_plain_same_budgets": t_plain_budget / t_batched,
             "plain_chains_per_s": chains_batched / t_plain_budget,
         },

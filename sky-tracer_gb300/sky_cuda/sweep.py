@@ -37,16 +37,23 @@ def p95_relative_error(xyz: np.ndarray, var: np.ndarray, dark_fraction: float = 
     return float(np.percentile(rel.max(axis=1), 95))
 
 
-def budgets_from_pilot(p95: np.ndarray, pilot_spp: int, target: float = 0.01, lo: int = 64, hi: int = 1024,
-                       multiple: int = 32, seed: int = 2026, jitter: float = 0.05) -> np.ndarray:
-    """Per-job spp proportional to the pilot's variance (error^2 scales as 1/spp),
-    jittered by +-jitter with a seeded generator, rounded up to `multiple` and
-    clamped to [lo, hi]."""
-    need = pilot_spp * (np.asarray(p95, dtype=np.float64) / target) ** 2
+def budgets_from_pilot(p95: np.ndarray, lo: int = 64, hi: int = 1024, multiple: int = 32, seed: int = 2026,
+                       jitter: float = 0.05) -> np.ndarray:
+    """Per-job spp in proportion to the variance a pilot estimated: the pilot's
+    p95 relative error squared, scaled so the noisiest job gets `hi`; jittered
+    by +-jitter with a seeded generator, rounded up to `multiple`, clamped to
+    [lo, hi].  Equal variance per sample budget equalises the jobs' errors."""
+    var = np.asarray(p95, dtype=np.float64) ** 2
+    spp = hi * var / max(float(var.max()), 1e-300)
     rng = np.random.default_rng(seed)
-    need = need * (1.0 + jitter * rng.uniform(-1.0, 1.0, size=need.shape))
-    spp = np.ceil(need / multiple) * multiple
+    spp = spp * (1.0 + jitter * rng.uniform(-1.0, 1.0, size=spp.shape))
+    spp = np.ceil(spp / multiple - 1e-6) * multiple
     return np.clip(spp, lo, hi).astype(np.int64)
+
+
+def spp_for_target(p95: np.ndarray, spp, target: float = 0.01) -> np.ndarray:
+    """Samples each job needs for a p95 error of `target` (error^2 ~ 1/spp)."""
+    return np.asarray(spp, dtype=np.float64) * (np.asarray(p95, dtype=np.float64) / target) ** 2
 
 
 @dataclass
@@ -115,7 +122,8 @@ class Sweep:
 
 
 def plan_budgets(gs: GpuScene, base: RenderConfig, elevations, pilot_spp: int = 16, **kw):
-    """Render a pilot sweep at pilot_spp and derive each elevation's budget."""
+    """Render a pilot sweep at pilot_spp and derive each elevation's budget
+    (budgets_from_pilot); returns (spp, pilot p95 errors)."""
     import torch
     pilot = Sweep(gs, base, elevations, pilot_spp)
     pilot.launch(torch.cuda.current_stream().cuda_stream)
@@ -123,4 +131,4 @@ def plan_budgets(gs: GpuScene, base: RenderConfig, elevations, pilot_spp: int = 
     if int(pilot.status.item()) != 0:
         raise RuntimeError("watchdog tripped in the pilot sweep")
     p95 = np.array(pilot.errors())
-    return budgets_from_pilot(p95, pilot_spp, **kw), p95
+    return budgets_from_pilot(p95, **kw), p95
