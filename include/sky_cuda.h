@@ -336,6 +336,108 @@ int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatchJob* jobs, 
 int sky_cuda_batch_graph_launch(SkyBatchGraph* graph, void* cuda_stream);
 void sky_cuda_batch_graph_destroy(SkyBatchGraph* graph);
 
+/* ---- Differentiable rendering ------------------------------------------ */
+
+/*
+ * No counterpart in the reference, which renders a fixed medium.  A
+ * differentiable render evaluates the scene's medium with parameters applied
+ * and returns dLoss/dparameters by path-replay backpropagation (each chain is
+ * traced, then replayed from the same counter-based random numbers; no path
+ * is stored).  The scene must hold one aerosol species (species 0, "Mie");
+ * species 1-3 must carry no mass or no optics.
+ *
+ * layer_params, float [3 * majorant_layers + 2], device memory:
+ *   [3 l + 0]  Rayleigh density scale of majorant layer l
+ *   [3 l + 1]  Mie density scale of layer l (scales species 0's extinction)
+ *   [3 l + 2]  ozone density scale of layer l
+ *   [3 L]      Mie single-scattering albedo (replaces species 0's)
+ *   [3 L + 1]  Mie Henyey-Greenstein asymmetry g, tabulated on the scene's
+ *              phase grid (held inside [-0.99, 0.99])
+ * band_params, float [band_count][4], device memory, or NULL for all ones:
+ *   multipliers of the band's Rayleigh cross section, Mie extinction, ozone
+ *   cross section and solar radiance (how a band-position change enters).
+ * Each call bakes the majorant grid of the parameterised medium on the device
+ * (medium.rs:63-102 probe rule) and, for SKY_TRACKING_MERGED_LAYERS, merges
+ * its layers as the scene's tracking grid does; SKY_TRACKING_RESIDUAL_CARRY
+ * tracks the uniform layers.  Segment-restart tracking is not offered.
+ *
+ * sample_layer_params / sample_band_params, when non-NULL, select a second
+ * parameter set whose medium drives every sampling decision while
+ * layer_params is evaluated (each path reweighted by the ratio of the two
+ * path densities): renders at nearby parameters then share their samples,
+ * which finite differences of the estimator need.  The evaluated medium's
+ * extinction must stay below the sampling medium's majorants.
+ */
+#define SKY_ADJOINT_BAND_PARAMS 4u
+
+/*
+ * How the backward pass estimates the derivative of each traversed segment's
+ * transmittance, -integral of d(sigma_t)/d(theta) along it:
+ *   SEGMENT_INTEGRALS  stratified points placed along the segment in
+ *                      majorant optical depth, from a random stream of their
+ *                      own (the default; far lower variance);
+ *   NULL_COLLISIONS    the null collisions the tracker drew: the exact
+ *                      derivative of the forward estimator with its samples
+ *                      held fixed, which central differences with
+ *                      sample_layer_params reproduce to rounding.
+ * Both are unbiased.
+ */
+typedef enum SkyAdjointEstimator {
+    SKY_ADJOINT_SEGMENT_INTEGRALS = 0,
+    SKY_ADJOINT_NULL_COLLISIONS = 1
+} SkyAdjointEstimator;
+
+typedef struct SkyAdjointParams {
+    const float* layer_params;
+    const float* band_params;
+    const float* sample_layer_params;
+    const float* sample_band_params;
+    float sun_direction[3];  /* unit vector; all zero = the scene's sun */
+    uint32_t estimator;      /* SkyAdjointEstimator (backward only) */
+} SkyAdjointParams;
+
+/*
+ * Gradient request.  dloss_dfilm [pixels][band_count] is dLoss/d(film value)
+ * of the mean film the forward call wrote; the gradients are ADDED to
+ * layer_grad [3 * majorant_layers + 2] and band_grad [band_count][4] (NULL to
+ * skip).  status (required) and counters (optional) as in SkyDeviceOutputs.
+ */
+typedef struct SkyAdjointGrads {
+    const float* dloss_dfilm;
+    double* layer_grad;
+    double* band_grad;
+    unsigned long long* counters;
+    uint32_t* status;
+} SkyAdjointGrads;
+
+/* Number of layer parameters of the scene (3 * majorant_layers + 2). */
+uint32_t sky_cuda_adjoint_param_count(const SkyScene* scene);
+
+/*
+ * Forward render over the parameterised medium into device outputs (as
+ * sky_cuda_render_device: cell_sum and status required), asynchronous on
+ * `cuda_stream`.  config->kernel is ignored; the whole call (table bake and
+ * render) is ordered on the stream.
+ */
+int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderConfig* config, const SkyAdjointParams* params,
+                             const SkyDeviceOutputs* outputs, void* cuda_stream);
+
+/*
+ * Backward: the gradient at `params` (sample_* must be NULL) of a loss whose
+ * derivative with respect to the film of the forward render with the same
+ * config is grads->dloss_dfilm.  Asynchronous on `cuda_stream`.
+ */
+int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderConfig* config, const SkyAdjointParams* params,
+                              const SkyAdjointGrads* grads, void* cuda_stream);
+
+/*
+ * Device majorant bake (compute_majorant_grid, medium.rs:63-102) of the
+ * parameterised medium: writes majorants [band_count][majorant_layers] to
+ * device memory.  With all scales 1 it reproduces the scene's own grid.
+ */
+int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* params, float* majorants_out,
+                            void* cuda_stream);
+
 /*
  * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
  * single launch of the persistent tracer.  No counterpart in the reference.

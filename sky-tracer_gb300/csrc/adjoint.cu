@@ -1,0 +1,857 @@
+// adjoint.cu — differentiable rendering of the sky: the device bake of the
+// majorants of a parameterised medium, its primal render, and the
+// path-replay adjoint that returns dLoss/dparams.  No counterpart in the
+// reference; the transport is the reference's (sky_trace.wgsl:703-776) over
+// the parameterised medium described in adjoint_kernels.h.
+//
+// Parameters of a set X (layer l, band b, altitude h inside layer l):
+//   sigma_R  = s_R[l] k_R[b] air(h) xs_R[b]            (sky_trace.wgsl:383)
+//   sigma_M  = s_M[l] k_M[b] m0(h) (sca0[b] + abs0[b])  (:370-380, species 0)
+//   sigma_O  = s_O[l] k_O[b] o3(h) xs_O[b]             (:384)
+//   sigma_Ms = omega sigma_M, sigma_t = sigma_R + sigma_M + sigma_O,
+//   sigma_s  = sigma_R + sigma_Ms, Mie phase = HG(g) tabulated on the scene's
+//   cube-root mu grid (phase.rs:37-46), solar radiance x k_S[b].
+//
+// Gradient estimator (path replay: a chain is traced once for its radiance
+// L, then replayed from the same counter-based random numbers; no path is
+// stored).  Each contribution C to L (an NEE term, the sun disc) is a
+// product of factors, and dC = C sum d log(factor):
+//   traversed segment       transmittance exp(-integral sigma_t): its
+//                           d log is -integral d(sigma_t) along the segment
+//   scattering vertex       sum_i sigma_i p_i(mu) for the direction mu that
+//                           the contribution uses (the sun direction of an
+//                           NEE term, the continuation direction for
+//                           everything after it); the albedo and the mixed
+//                           phase's normalisation cancel into it
+//   sun radiance            k_S (L is linear in it)
+// Russian roulette, camera, light and Lambert sampling carry no parameter.
+// The replay adds w * C_after * d log(factor) for each factor, where C_after
+// is the radiance the factor multiplies (L minus what was collected before
+// it, or the single NEE term for a shadow ray's factors) and w is dLoss/dL
+// of the chain (dLoss/dfilm of its cell / spp).
+// The segment integrals are estimated either by stratified points placed in
+// majorant optical depth from a random stream of their own
+// (SKY_ADJOINT_SEGMENT_INTEGRALS), or by the null collisions the tracker drew
+// (SKY_ADJOINT_NULL_COLLISIONS: factor mu_bar - sigma_t per null collision;
+// with the samples held fixed this is the exact derivative of the forward
+// estimator, and the shadow ray of an NEE term is traced a second time for
+// its null collisions).
+
+#include <algorithm>
+#include <cmath>
+
+#include "adjoint_kernels.h"
+#include "sky_device.cuh"
+
+namespace sky {
+namespace {
+
+// Unscaled coefficients at a point: air xs_R, m0 ext0 and o3 xs_O of the
+// band, and the uniform layer that holds the point.
+struct AdjBase {
+    float uR, uM, uO;
+    int layer;
+};
+
+// Coefficients of one parameter set at a point.
+struct AdjMed {
+    float R, M, O, Ms, t, s;
+};
+
+// A parameter set resolved for one band.
+struct AdjSet {
+    const float* layer;
+    float kR, kM, kO, kS;
+    float omega;
+    const float* phase;
+    const float* dphase;
+    const float* cdf;
+    const float* bin_pdf;
+};
+
+__device__ __forceinline__ AdjSet resolve(const AdjParamSet& X, uint32_t layers, uint32_t band) {
+    AdjSet r;
+    r.layer = X.layer;
+    if (X.band) {
+        const float* k = X.band + band * kAdjBandParams;
+        r.kR = __ldg(k);
+        r.kM = __ldg(k + 1);
+        r.kO = __ldg(k + 2);
+        r.kS = __ldg(k + 3);
+    } else {
+        r.kR = r.kM = r.kO = r.kS = 1.0f;
+    }
+    r.omega = __ldg(X.layer + 3 * layers);
+    r.phase = X.phase;
+    r.dphase = X.dphase;
+    r.cdf = X.cdf;
+    r.bin_pdf = X.bin_pdf;
+    return r;
+}
+
+__device__ __forceinline__ AdjBase adj_base(const DevScene& S, uint32_t band, float alt) {
+    AdjBase b;
+    b.uR = b.uM = b.uO = 0.0f;
+    b.layer = 0;
+    if (!(alt >= 0.0f && alt <= S.top_altitude)) return b;
+    const uint32_t k = knot_interval(S, S.knot_z, S.finder, alt);
+    const float dz = alt - S.knot_z[k];
+    const DevProfileKnot& P = S.profile[k];
+    const DevBand& B = S.bands[band];
+    b.uR = fmaxf(fmaf(dz, P.air_slope, P.air) * B.rayleigh_xs, 0.0f);
+    b.uO = fmaxf(fmaf(dz, P.ozone_slope, P.ozone) * B.ozone_xs, 0.0f);
+    const float mass = fmaxf(fmaf(dz, P.mass_slope[0], P.mass[0]), 0.0f);
+    const SkyAerosolOptics o = S.optics[band * kSpecies];
+    b.uM = fmaxf(mass * o.scattering_km_inv_per_g_m3, 0.0f) + fmaxf(mass * o.absorption_km_inv_per_g_m3, 0.0f);
+    b.layer = min(int(alt * S.inv_layer_dz), int(S.layer_count) - 1);
+    return b;
+}
+
+__device__ __forceinline__ AdjMed adj_med(const AdjSet& X, const AdjBase& b) {
+    const float* p = X.layer + 3 * b.layer;
+    AdjMed m;
+    m.R = __ldg(p) * X.kR * b.uR;
+    m.M = __ldg(p + 1) * X.kM * b.uM;
+    m.O = __ldg(p + 2) * X.kO * b.uO;
+    m.Ms = X.omega * m.M;
+    m.s = m.R + m.Ms;
+    m.t = m.R + m.M + m.O;
+    return m;
+}
+
+// Position of mu on the cube-root grid (mie_phase, sky_trace.wgsl:485-494).
+__device__ __forceinline__ void hg_slot(uint32_t bins, float mu, uint32_t& i0, uint32_t& i1, float& t) {
+    const float u = cbrt_pos((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
+    const float f = u * float(bins) - 0.5f;
+    i0 = min(uint32_t(fminf(fmaxf(floorf(f), 0.0f), float(bins - 1u))), bins - 1u);
+    i1 = min(i0 + 1u, bins - 1u);
+    t = fminf(fmaxf(f - float(i0), 0.0f), 1.0f);
+}
+
+__device__ __forceinline__ float hg_value(const AdjSet& X, uint32_t bins, float mu) {
+    uint32_t i0, i1;
+    float t;
+    hg_slot(bins, mu, i0, i1, t);
+    const float p0 = __ldg(X.phase + i0), p1 = __ldg(X.phase + i1);
+    return fmaxf(fmaf(t, p1 - p0, p0), 0.0f);
+}
+
+// sum_i sigma_i p_i(mu): the scattering-vertex factor.
+__device__ __forceinline__ float vertex_phase(const AdjSet& X, uint32_t bins, const AdjMed& m, float mu) {
+    return m.R * rayleigh_phase(mu) + (m.Ms > 0.0f ? m.Ms * hg_value(X, bins, mu) : 0.0f);
+}
+
+// Gradient accumulator of one lane: layer parameters in shared memory, the
+// multipliers of the lane's band in registers.
+struct AdjAcc {
+    float* sg;  // [3 L + 2]
+    uint32_t L;
+    float gR, gM, gO;
+};
+
+// d sigma_t terms of a null collision, times c (= -weight / sigma_n).
+__device__ __forceinline__ void null_terms(AdjAcc& a, const AdjSet& X, const AdjBase& b, float c) {
+    const float* p = X.layer + 3 * b.layer;
+    float* g = a.sg + 3 * b.layer;
+    if (b.uR > 0.0f) {
+        atomicAdd(g, c * X.kR * b.uR);
+        a.gR = fmaf(c * __ldg(p), b.uR, a.gR);
+    }
+    if (b.uM > 0.0f) {
+        atomicAdd(g + 1, c * X.kM * b.uM);
+        a.gM = fmaf(c * __ldg(p + 1), b.uM, a.gM);
+    }
+    if (b.uO > 0.0f) {
+        atomicAdd(g + 2, c * X.kO * b.uO);
+        a.gO = fmaf(c * __ldg(p + 2), b.uO, a.gO);
+    }
+}
+
+// weight * d log(sum_i sigma_i p_i(mu)) of a scattering vertex.
+__device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_t bins, const AdjBase& b,
+                                             const AdjMed& m, float mu, float weight) {
+    if (weight == 0.0f) return;
+    uint32_t i0, i1;
+    float t;
+    hg_slot(bins, mu, i0, i1, t);
+    const float p0 = __ldg(X.phase + i0), p1 = __ldg(X.phase + i1);
+    const float pm = fmaxf(fmaf(t, p1 - p0, p0), 0.0f);
+    const float d0 = __ldg(X.dphase + i0), d1 = __ldg(X.dphase + i1);
+    const float dpm = fmaf(t, d1 - d0, d0);
+    const float pr = rayleigh_phase(mu);
+    const float sum = m.R * pr + m.Ms * pm;
+    if (!(sum > 0.0f)) return;
+    const float w = weight / sum;
+    const float* p = X.layer + 3 * b.layer;
+    float* g = a.sg + 3 * b.layer;
+    if (b.uR > 0.0f) {
+        atomicAdd(g, w * X.kR * b.uR * pr);
+        a.gR = fmaf(w * __ldg(p), b.uR * pr, a.gR);
+    }
+    if (b.uM > 0.0f) {
+        atomicAdd(g + 1, w * X.omega * X.kM * b.uM * pm);
+        atomicAdd(a.sg + 3 * a.L, w * m.M * pm);
+        atomicAdd(a.sg + 3 * a.L + 1, w * m.Ms * dpm);
+        a.gM = fmaf(w * X.omega * __ldg(p + 1), b.uM * pm, a.gM);
+    }
+}
+
+// Residual-carry delta tracking over Q's tracking grid (track_ray_merged of
+// the plain tracer with the parameterised medium).  w_eval collects the
+// null-collision ratios of P over Q; with kGrad every null collision adds
+// gw * d log(mu_bar - sigma_t).
+template <bool kGrad>
+__device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band, const RayGeo& g,
+                          float t_max, Rng& rng, float& t_hit, AdjBase& hit, float& w_eval, float gw, AdjAcc& acc,
+                          Counters& n, bool& watchdog) {
+    const DevScene& S = A.S;
+    const uint32_t L = S.layer_count;
+    MergedGrid G;
+    G.radius = A.G.radius + band * (L + 1u);
+    G.maj = A.G.maj + band * (L + 1u);
+    G.map = A.G.map + band * L;
+    G.count = int(__ldg(A.G.count + band));
+    float t = 0.0f;
+    int m = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_max), S.ground_radius));
+    int dir;
+    float t_seg = merged_crossing(G, g, m, t, t_max, dir);
+    float maj = __ldg(G.maj + m);
+    ++n.e[SKY_EVENT_SEGMENT];
+    float tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+    uint32_t guard = 0;
+    for (;;) {
+        const float dt = tau / maj;
+        if (t + dt < t_seg) {
+            t = t + dt;
+            ++n.e[SKY_EVENT_TRACK_STEP];
+            const AdjBase b = adj_base(S, band, altitude_at(g, t, S.ground_radius));
+            const AdjMed mq = adj_med(Q, b);
+            if (rng.next() * maj < mq.t) {
+                t_hit = t;
+                hit = b;
+                return true;
+            }
+            const float sn = maj - mq.t;
+            if (A.distinct && sn > 0.0f) w_eval *= (maj - adj_med(P, b).t) / sn;
+            if (kGrad && A.estimator == SKY_ADJOINT_NULL_COLLISIONS && gw != 0.0f && sn > 0.0f)
+                null_terms(acc, Q, b, -gw / sn);
+            tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
+        } else {
+            if (dir == 0) return false;
+            if (++guard > 100000u) {
+                watchdog = true;
+                return false;
+            }
+            tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
+            t = t_seg;
+            m += dir;
+            t_seg = merged_crossing(G, g, m, t, t_max, dir);
+            maj = __ldg(G.maj + m);
+            ++n.e[SKY_EVENT_SEGMENT];
+        }
+    }
+}
+
+// Estimate of -integral d(sigma_t) over [0, t_end] of a ray, times weight:
+// N points stratified in the majorant optical depth of Q's tracking grid
+// (density mu_bar / tau_bar along the ray), each adding
+// -weight (tau_bar / N) d(sigma_t) / mu_bar.  N grows with tau_bar.  The
+// points' random numbers come from a stream of their own (another pcg4d
+// key, 16 draws per position of the path's stream), so the path's own
+// draws are untouched.
+constexpr int kMaxSegmentPoints = 8;
+
+__device__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, const RayGeo& g, float t_end,
+                              float weight, const Rng& rng, AdjAcc& acc) {
+    if (weight == 0.0f || !(t_end > 0.0f)) return;
+    const DevScene& S = A.S;
+    const uint32_t L = S.layer_count;
+    MergedGrid G;
+    G.radius = A.G.radius + band * (L + 1u);
+    G.maj = A.G.maj + band * (L + 1u);
+    G.map = A.G.map + band * L;
+    G.count = int(__ldg(A.G.count + band));
+    const int m0 = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_end), S.ground_radius));
+    const int guard_max = 2 * G.count + 4;
+    float tau = 0.0f, t = 0.0f;
+    int m = m0, dir = 0;
+    for (int guard = 0; guard < guard_max; ++guard) {
+        const float t_seg = merged_crossing(G, g, m, t, t_end, dir);
+        tau += (t_seg - t) * __ldg(G.maj + m);
+        if (dir == 0) break;
+        t = t_seg;
+        m += dir;
+    }
+    if (!(tau > 0.0f)) return;
+    const int n = min(kMaxSegmentPoints, 1 + int(2.0f * tau));
+    const float step = tau / float(n);
+    Rng r2 = rng;  // 16 draws of its own per position of the path's stream
+    r2.k2 ^= 0x68E31DA4u;
+    r2.dim = rng.dim * 16u;
+    int j = 0;
+    float uj = r2.next() * step;
+    float u0 = 0.0f;
+    t = 0.0f;
+    m = m0;
+    for (int guard = 0; guard < guard_max && j < n; ++guard) {
+        const float t_seg = merged_crossing(G, g, m, t, t_end, dir);
+        const float maj = __ldg(G.maj + m);
+        const float u1 = u0 + (t_seg - t) * maj;
+        while (j < n && (uj < u1 || dir == 0)) {
+            const float tj = fminf(t + (uj - u0) / maj, t_seg);
+            const AdjBase b = adj_base(S, band, altitude_at(g, tj, S.ground_radius));
+            null_terms(acc, Q, b, -weight * step / maj);
+            ++j;
+            uj = (float(j) + r2.next()) * step;
+        }
+        if (dir == 0) break;
+        u0 = u1;
+        t = t_seg;
+        m += dir;
+    }
+}
+
+// Inverse CDF of an HG table (MiePhaseTable::sample_mu_pdf, phase.rs:53-69).
+__device__ __forceinline__ float hg_sample_mu(const AdjSet& X, uint32_t bins, float xi) {
+    xi = fminf(fmaxf(xi, 0.0f), 1.0f - kF32Epsilon);
+    uint32_t lo = 0, hi = bins;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(X.cdf + mid) <= xi) lo = mid + 1u;
+        else hi = mid;
+    }
+    const uint32_t bin = min(lo, bins - 1u);
+    const float prev = bin == 0u ? 0.0f : __ldg(X.cdf + bin - 1u);
+    const float next = __ldg(X.cdf + bin);
+    const float t = next > prev ? (xi - prev) / (next - prev) : 0.5f;
+    return mu_edge(bin, bins) * (1.0f - t) + mu_edge(bin + 1u, bins) * t;
+}
+
+// MiePhaseTable::sampling_pdf (phase.rs:71-75)
+__device__ __forceinline__ float hg_sampling_pdf(const AdjSet& X, uint32_t bins, float mu) {
+    const float u = cbrt_pos((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
+    const uint32_t bin = min(uint32_t(floorf(u * float(bins))), bins - 1u);
+    return fmaxf(__ldg(X.bin_pdf + bin), 1.0e-12f);
+}
+
+// Shadow ray of an NEE sample: the P/Q weight of a ray that reaches the sun,
+// 0 when it hits the ground, leaves through no sun or collides.  dim0 is the
+// random-number index at which its tracking started.
+__device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band, V3 pos,
+                                            V3 ldir, Rng& rng, AdjAcc& acc, Counters& n, bool& watchdog,
+                                            uint32_t& dim0) {
+    const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
+    float st;
+    uint32_t sk;
+    ++n.e[SKY_EVENT_BOUNDARY];
+    if (!(next_boundary(A.S, sg, st, sk) && sk == 1u)) return 0.0f;
+    dim0 = rng.dim;
+    float th, w = 1.0f;
+    AdjBase bh;
+    if (adj_track<false>(A, P, Q, band, sg, st, rng, th, bh, w, 0.0f, acc, n, watchdog)) return 0.0f;
+    return w;
+}
+
+// Gradient terms of an unblocked shadow ray: its segment integral, or (null
+// collisions) the same ray traced again from dim0 for its null collisions.
+__device__ __forceinline__ void adj_shadow_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, V3 pos, V3 ldir,
+                                                 Rng& rng, uint32_t dim0, float weight, AdjAcc& acc, Counters& n,
+                                                 bool& watchdog) {
+    if (weight == 0.0f) return;
+    const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
+    float st;
+    uint32_t sk;
+    next_boundary(A.S, sg, st, sk);
+    if (A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
+        segment_terms(A, Q, band, sg, st, weight, rng, acc);
+        return;
+    }
+    const uint32_t dim1 = rng.dim;
+    rng.dim = dim0;
+    float th, w = 1.0f;
+    AdjBase bh;
+    adj_track<true>(A, Q, Q, band, sg, st, rng, th, bh, w, weight, acc, n, watchdog);
+    rng.dim = dim1;
+}
+
+// One chain of the parameterised medium (trace_path, sky_trace.wgsl:703-776)
+// at unit solar multiplier.  kGrad replays a chain whose radiance `total`
+// pass 1 returned and accumulates w * dL/dparams.
+template <int kPhase, bool kGrad>
+__device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, const DevLaunch& L, uint32_t x,
+                           uint32_t y, uint32_t band, uint32_t sample, float w, float total, AdjAcc& acc,
+                           Counters& n, bool& watchdog) {
+    const DevScene& S = A.S;
+    const uint32_t bins = S.phase_bins;
+    Rng rng;
+    rng.init(y * L.width + x, sample, band, L.seed_lo, L.seed_hi);
+    V3 dir = camera_dir(L, x, y, rng);
+    V3 org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
+    ++n.e[SKY_EVENT_CHAIN];
+    const float l_sun = __ldg(&S.bands[band].solar_radiance);
+    const float inv_lights = 1.0f / float(L.direct_light_samples);
+    // thr_q: throughput under Q (drives Russian roulette); thr: under P.
+    float thr = 1.0f, thr_q = 1.0f, rad = 0.0f;
+    for (uint32_t depth = 0;; ++depth) {
+        if (depth >= L.watchdog_limit) {
+            watchdog = true;
+            return rad;
+        }
+        if (L.max_orders != 0u && depth >= L.max_orders) break;
+        const RayGeo g = ray_geo(org, dir);
+        float t_b;
+        uint32_t kind;
+        ++n.e[SKY_EVENT_BOUNDARY];
+        if (!next_boundary(S, g, t_b, kind)) break;
+        float t_hit, w_eval = 1.0f;
+        AdjBase hb;
+        const float gw = kGrad ? w * (total - rad) : 0.0f;
+        const uint32_t dim_seg = rng.dim;
+        const bool hit = adj_track<kGrad>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, gw, acc, n, watchdog);
+        if (kGrad && A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
+            Rng at = rng;
+            at.dim = dim_seg;
+            segment_terms(A, Q, band, g, hit ? t_hit : t_b, gw, at, acc);
+        }
+        thr *= w_eval;
+        if (hit) {
+            ++n.e[SKY_EVENT_SCATTER];
+            const V3 pos = madd(org, dir, t_hit);
+            const AdjMed mq = adj_med(Q, hb);
+            if (mq.t <= 0.0f || mq.s <= 0.0f) break;
+            const AdjMed mp = A.distinct ? adj_med(P, hb) : mq;
+            thr_q *= fminf(fmaxf(mq.s / mq.t, 0.0f), 1.0f);
+            thr = A.distinct ? thr * (mp.s / mq.t) : thr_q;
+            if (thr_q <= 0.0f) break;
+            // direct_sun_at_scatter (sky_trace.wgsl:566-585)
+            float nee = 0.0f;
+            for (uint32_t ls = 0; ls < L.direct_light_samples; ++ls) {
+                const V3 ldir = sample_sun_cone(S, rng);
+                ++n.e[SKY_EVENT_NEE];
+                uint32_t dim0 = 0;
+                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0);
+                if (!(trans != 0.0f)) continue;
+                const float mu = dot3(dir, ldir);
+                const float ph = mp.s > 0.0f ? vertex_phase(P, bins, mp, mu) / mp.s : 0.0f;
+                const float term = l_sun * trans * ph / S.light_pdf;
+                nee += term;
+                if (kGrad) {
+                    const float c = w * thr * term * inv_lights;
+                    vertex_terms(acc, Q, bins, hb, mq, mu, c);
+                    adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, c, acc, n, watchdog);
+                }
+            }
+            rad += thr * (nee * inv_lights);
+            V3 nd;
+            float mu_c, fq, fp;
+            if (kPhase == SKY_PHASE_TABULATED) {
+                // phase.rs:53-75, sampling.rs:182-185 over Q's mixture
+                const float target = rng.next() * mq.s;
+                const bool rayleigh = target < mq.R || !(mq.Ms > 0.0f);
+                const float xi_mu = rng.next();
+                mu_c = rayleigh ? invert_rayleigh_cdf(xi_mu) : hg_sample_mu(Q, bins, xi_mu);
+                const float xi_phi = rng.next();
+                nd = direction_from_axis_mu(dir, mu_c, xi_phi);
+                const float pdf = mq.R * rayleigh_phase(mu_c) +
+                                  (mq.Ms > 0.0f ? mq.Ms * hg_sampling_pdf(Q, bins, mu_c) : 0.0f);
+                fq = vertex_phase(Q, bins, mq, mu_c) / pdf;
+                fp = A.distinct ? (mp.s > 0.0f ? vertex_phase(P, bins, mp, mu_c) / mp.s : 0.0f) * mq.s / pdf : fq;
+            } else {
+                nd = sample_isotropic(rng);
+                mu_c = dot3(dir, nd);
+                fq = vertex_phase(Q, bins, mq, mu_c) / mq.s / kIsotropicPdf;
+                fp = A.distinct ? (mp.s > 0.0f ? vertex_phase(P, bins, mp, mu_c) / mp.s : 0.0f) / kIsotropicPdf : fq;
+            }
+            thr_q *= fq;
+            thr = A.distinct ? thr * fp : thr_q;
+            if (kGrad) vertex_terms(acc, Q, bins, hb, mq, mu_c, w * (total - rad));
+            if (depth >= L.rr_start_depth) {  // russian_roulette (sky_trace.wgsl:691-701)
+                const float q = fminf(fmaxf(thr_q, 0.05f), 0.95f);
+                if (rng.next() > q) break;
+                thr_q = thr_q / q;
+                thr = A.distinct ? thr / q : thr_q;
+            }
+            org = madd(pos, nd, kRayEpsilonKm);
+            dir = nd;
+        } else if (kind == 1u) {
+            if (depth == 0u && dot3(dir, load3(S.sun)) >= S.cos_max) rad += thr * l_sun;
+            break;
+        } else {
+            // ground_radiance (sky_trace.wgsl:587-608) and the Lambert bounce (:750-766)
+            ++n.e[SKY_EVENT_GROUND];
+            const V3 pos = madd(org, dir, t_b);
+            const V3 normal = normalize_or_y(pos);
+            float ground = 0.0f;
+            for (uint32_t ls = 0; ls < L.direct_light_samples; ++ls) {
+                const V3 ldir = sample_sun_cone(S, rng);
+                ++n.e[SKY_EVENT_NEE];
+                const float cos_sun = fmaxf(dot3(normal, ldir), 0.0f);
+                if (!(cos_sun > 0.0f)) continue;
+                uint32_t dim0 = 0;
+                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0);
+                if (!(trans != 0.0f)) continue;
+                const float term = S.ground_albedo * kInvPi * l_sun * trans * cos_sun / S.light_pdf;
+                ground += term;
+                if (kGrad) adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, w * thr * term * inv_lights, acc, n,
+                                             watchdog);
+            }
+            rad += thr * (ground * inv_lights);
+            float pdf;
+            const V3 bounce = sample_cosine_hemisphere(normal, rng, pdf);
+            const float cos_out = fmaxf(dot3(normal, bounce), 0.0f);
+            if (pdf <= 0.0f || cos_out <= 0.0f) break;
+            const float f = S.ground_albedo * kInvPi * cos_out / pdf;
+            thr_q *= f;
+            thr = A.distinct ? thr * f : thr_q;
+            if (depth >= L.rr_start_depth) {
+                const float q = fminf(fmaxf(thr_q, 0.05f), 0.95f);
+                if (rng.next() > q) break;
+                thr_q = thr_q / q;
+                thr = A.distinct ? thr / q : thr_q;
+            }
+            org = madd(pos, bounce, kRayEpsilonKm);
+            dir = bounce;
+        }
+        if (rad < 0.0f || rad != rad || thr_q < 0.0f || thr_q != thr_q || thr != thr) return 0.0f;
+    }
+    return fmaxf(rad, 0.0f);
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void flush_counters(const Counters& n, unsigned long long* counters, uint32_t lane) {
+    if (!counters) return;
+#pragma unroll
+    for (int e = 0; e < SKY_EVENT_COUNT; ++e) {
+        const uint32_t v = warp_sum_u(n.e[e]);
+        if (lane == 0 && v) atomicAdd(counters + e, (unsigned long long)v);
+    }
+}
+
+// Primal: one warp per (pixel, band) cell, 32 samples per round, FP64 cell
+// sums in a fixed order (as the plain tracer).
+template <int kPhase>
+__global__ void __launch_bounds__(256) adjoint_primal_kernel(AdjCtx A, DevLaunch L, double* __restrict__ cell_sum,
+                                                             double* __restrict__ cell_sumsq, uint32_t accumulate,
+                                                             unsigned long long* __restrict__ counters,
+                                                             uint32_t* __restrict__ status, uint64_t cells) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
+    const uint32_t band = uint32_t(cell % L.band_count);
+    const uint64_t pixel = cell / L.band_count;
+    const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
+    const AdjSet P = resolve(A.P, A.S.layer_count, band);
+    const AdjSet Q = A.distinct ? resolve(A.Q, A.S.layer_count, band) : P;
+    AdjAcc acc{nullptr, 0u, 0.0f, 0.0f, 0.0f};
+    Counters n;
+    n.clear();
+    bool watchdog = false;
+    double sum = 0.0, sumsq = 0.0;
+    if (accumulate) {
+        sum = cell_sum[cell];
+        if (cell_sumsq) sumsq = cell_sumsq[cell];
+    }
+    for (uint32_t base = 0; base < L.spp; base += 32u) {
+        const uint32_t s = base + lane;
+        float r = 0.0f;
+        if (s < L.spp)
+            r = P.kS * adj_chain<kPhase, false>(A, P, Q, L, x, y, band, L.sample_offset + s, 0.0f, 0.0f, acc, n,
+                                                 watchdog);
+        const double rd = double(r);
+        sum += warp_sum_d(rd);
+        sumsq += warp_sum_d(rd * rd);
+    }
+    if (lane == 0) {
+        cell_sum[cell] = sum;
+        if (cell_sumsq) cell_sumsq[cell] = sumsq;
+    }
+    flush_counters(n, counters, lane);
+    if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
+}
+
+// Adjoint: warps stride over the cells; each chain is traced (pass 1) and
+// replayed (pass 2).  Layer gradients gather in shared memory (FP32), band
+// gradients per warp, and each block adds its totals to the FP64 outputs
+// once at the end.
+template <int kPhase>
+__global__ void __launch_bounds__(256) adjoint_grad_kernel(AdjCtx A, DevLaunch L, const float* __restrict__ dloss,
+                                                           double* __restrict__ layer_grad,
+                                                           double* __restrict__ band_grad,
+                                                           unsigned long long* __restrict__ counters,
+                                                           uint32_t* __restrict__ status, uint64_t cells) {
+    extern __shared__ float smem[];
+    const uint32_t Lc = A.S.layer_count, B = A.S.band_count;
+    const uint32_t nlayer = 3u * Lc + 2u;
+    float* sg = smem;
+    float* sb = smem + nlayer;
+    for (uint32_t i = threadIdx.x; i < nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+    Counters n;
+    n.clear();
+    bool watchdog = false;
+    const float inv_spp = 1.0f / float(L.spp);
+    for (uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; cell < cells; cell += warps) {
+        const float wcell = __ldg(dloss + cell) * inv_spp;
+        if (wcell == 0.0f) continue;  // uniform across the warp
+        const uint32_t band = uint32_t(cell % L.band_count);
+        const uint64_t pixel = cell / L.band_count;
+        const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
+        const AdjSet P = resolve(A.P, Lc, band);
+        const float w = wcell * P.kS;
+        AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f};
+        float gS = 0.0f;
+        for (uint32_t base = 0; base < L.spp; base += 32u) {
+            const uint32_t s = base + lane;
+            if (s >= L.spp) continue;
+            const float total = adj_chain<kPhase, false>(A, P, P, L, x, y, band, L.sample_offset + s, 0.0f, 0.0f,
+                                                         acc, n, watchdog);
+            gS = fmaf(wcell, total, gS);
+            if (total > 0.0f)
+                adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, w, total, acc, n, watchdog);
+        }
+        const float r = warp_sum_f(acc.gR), m = warp_sum_f(acc.gM), o = warp_sum_f(acc.gO), s = warp_sum_f(gS);
+        if (lane == 0) {
+            float* b = sb + band * kAdjBandParams;
+            atomicAdd(b, r);
+            atomicAdd(b + 1, m);
+            atomicAdd(b + 2, o);
+            atomicAdd(b + 3, s);
+        }
+    }
+    flush_counters(n, counters, lane);
+    if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nlayer; i += blockDim.x)
+        if (sg[i] != 0.0f) atomicAdd(layer_grad + i, double(sg[i]));
+    if (band_grad)
+        for (uint32_t i = threadIdx.x; i < kAdjBandParams * B; i += blockDim.x)
+            if (sb[i] != 0.0f) atomicAdd(band_grad + i, double(sb[i]));
+}
+
+// Majorant of Q's medium over one uniform layer: compute_majorant_grid's
+// probe rule (medium.rs:63-102: layer edges, mid-point and every profile
+// knot inside the layer; 1.05 x max, at least 1e-8) with the layer's own
+// scales applied at its edges.
+__device__ float bake_one(const AdjCtx& A, const AdjSet& Q, uint32_t band, uint32_t layer) {
+    const DevScene& S = A.S;
+    const float lo = float(layer) * S.layer_dz, hi = float(layer + 1u) * S.layer_dz;
+    const float* p = Q.layer + 3 * layer;
+    const float sR = p[0] * Q.kR, sM = p[1] * Q.kM, sO = p[2] * Q.kO;
+    auto ext = [&](float h) {
+        const AdjBase b = adj_base(S, band, h);
+        return sR * b.uR + sM * b.uM + sO * b.uO;
+    };
+    float mx = fmaxf(fmaxf(ext(lo), ext(hi)), ext(0.5f * (lo + hi)));
+    for (uint32_t k = 0; k < S.knot_count; ++k) {
+        const float z = S.knot_z[k];
+        if (z > lo && z < hi) mx = fmaxf(mx, ext(z));
+    }
+    return fmaxf(fmaxf(mx, 0.0f) * 1.05f, 1.0e-8f);
+}
+
+// Henyey-Greenstein table of g at the cube-root bin centres, its derivative
+// in g, and the sampling CDF / per-bin pdf of one row
+// (build_phase_sampling_tables, phase.rs:105-135).  |g| is held below 0.99.
+__device__ void build_hg_tables(float g_in, uint32_t bins, float* values, float* dvalues, float* cdf,
+                                float* bin_pdf) {
+    const double g = double(fminf(fmaxf(g_in, -0.99f), 0.99f));
+    const double four_pi = 4.0 * 3.14159265358979323846;
+    for (uint32_t i = threadIdx.x; i < bins; i += blockDim.x) {
+        const double u = (double(i) + 0.5) / double(bins);
+        const double mu = 1.0 - 2.0 * u * u * u;
+        const double d = 1.0 + g * g - 2.0 * g * mu;
+        const double sd = sqrt(d);
+        values[i] = float((1.0 - g * g) / (four_pi * d * sd));
+        dvalues[i] = float((-2.0 * g * d - 3.0 * (1.0 - g * g) * (g - mu)) / (four_pi * d * d * sd));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float two_pi = 2.0f * kPi;
+        float norm = 0.0f;
+        for (uint32_t b = 0; b < bins; ++b)
+            norm += two_pi * fmaxf(values[b], 0.0f) * fabsf(mu_edge(b, bins) - mu_edge(b + 1u, bins));
+        norm = fmaxf(norm, 1.0e-20f);
+        float cum = 0.0f;
+        for (uint32_t b = 0; b < bins; ++b) {
+            const float v = fmaxf(values[b], 0.0f);
+            cum += two_pi * v * fabsf(mu_edge(b, bins) - mu_edge(b + 1u, bins)) / norm;
+            cdf[b] = fminf(cum, 1.0f);
+            bin_pdf[b] = v / norm;
+        }
+        cdf[bins - 1u] = 1.0f;
+    }
+}
+
+// Blocks [0, B) bake one band each: majorants of every uniform layer, then
+// the tracking grid (the layers merged by the dynamic programme of the
+// scene's merged grid, or one tracking layer per uniform layer).  Block B
+// builds P's HG tables, block B + 1 Q's.
+__global__ void __launch_bounds__(128) adjoint_prepare_kernel(AdjCtx A, AdjWorkspace W) {
+    extern __shared__ float smem[];
+    const DevScene& S = A.S;
+    const uint32_t B = S.band_count, L = S.layer_count, bins = S.phase_bins;
+    if (blockIdx.x >= B) {
+        const bool q = blockIdx.x > B;
+        const AdjParamSet& X = q ? A.Q : A.P;
+        float* base = q ? W.q_tables : W.p_tables;
+        build_hg_tables(X.layer[3 * L + 1], bins, base, base + bins, base + 2 * bins, base + 3 * bins);
+        return;
+    }
+    const uint32_t band = blockIdx.x;
+    const AdjSet Q = resolve(A.Q, L, band);
+    float* maj = smem;                                           // [L]
+    float* best = smem + L;                                      // [L + 1]
+    uint32_t* from = reinterpret_cast<uint32_t*>(best + L + 1);  // [L + 1]
+    for (uint32_t l = threadIdx.x; l < L; l += blockDim.x) {
+        const float v = bake_one(A, Q, band, l);
+        maj[l] = v;
+        W.layer_maj[band * L + l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const float dz = S.layer_dz;
+    if (A.merge) {
+        best[0] = 0.0f;
+        for (uint32_t j = 1; j <= L; ++j) {
+            float bj = INFINITY, mx = 0.0f, sum = 0.0f;
+            uint32_t fj = 0;
+            for (uint32_t i = j; i-- > 0;) {  // group [i, j)
+                const float m = fmaxf(maj[i], 1e-8f);
+                mx = fmaxf(mx, m);
+                sum += m;
+                const float c = best[i] + A.crossing_cost + (mx * float(j - i) - sum) * dz;
+                if (c < bj) {
+                    bj = c;
+                    fj = i;
+                }
+            }
+            best[j] = bj;
+            from[j] = fj;
+        }
+    } else {
+        for (uint32_t j = 1; j <= L; ++j) from[j] = j - 1u;
+    }
+    uint32_t groups = 0;
+    for (uint32_t j = L; j > 0; j = from[j]) ++groups;
+    float* radius = W.radius + band * (L + 1u);
+    float* gmaj = W.maj + band * (L + 1u);
+    uint16_t* map = W.map + band * L;
+    uint32_t idx = groups;
+    for (uint32_t j = L; j > 0; j = from[j]) {
+        --idx;
+        const uint32_t k0 = from[j];
+        float mx = 0.0f;
+        for (uint32_t k = k0; k < j; ++k) {
+            mx = fmaxf(mx, fmaxf(maj[k], 0.00000001f));
+            map[k] = uint16_t(idx);
+        }
+        gmaj[idx] = mx;
+        radius[idx] = S.ground_radius + float(k0) * dz;
+    }
+    gmaj[groups] = 0.0f;
+    radius[groups] = S.ground_radius + S.top_altitude;
+    W.count[band] = groups;
+}
+
+uint32_t grid_blocks(const void* kernel, uint32_t threads, size_t smem, uint64_t want) {
+    int device = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, int(threads), smem);
+    const uint64_t resident = uint64_t(std::max(sms, 1)) * uint64_t(std::max(per_sm, 1));
+    return uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(want, resident)));
+}
+
+size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+}  // namespace
+
+size_t adjoint_workspace_bytes(uint32_t B, uint32_t L, uint32_t bins) {
+    return 2 * align256(4 * size_t(bins) * sizeof(float)) + align256(size_t(B) * L * sizeof(float)) +
+           2 * align256(size_t(B) * (L + 1) * sizeof(float)) + align256(size_t(B) * L * sizeof(uint16_t)) +
+           align256(size_t(B) * sizeof(uint32_t));
+}
+
+AdjWorkspace adjoint_workspace(void* base, uint32_t B, uint32_t L, uint32_t bins) {
+    unsigned char* p = static_cast<unsigned char*>(base);
+    AdjWorkspace W;
+    W.p_tables = reinterpret_cast<float*>(p);
+    p += align256(4 * size_t(bins) * sizeof(float));
+    W.q_tables = reinterpret_cast<float*>(p);
+    p += align256(4 * size_t(bins) * sizeof(float));
+    W.layer_maj = reinterpret_cast<float*>(p);
+    p += align256(size_t(B) * L * sizeof(float));
+    W.radius = reinterpret_cast<float*>(p);
+    p += align256(size_t(B) * (L + 1) * sizeof(float));
+    W.maj = reinterpret_cast<float*>(p);
+    p += align256(size_t(B) * (L + 1) * sizeof(float));
+    W.map = reinterpret_cast<uint16_t*>(p);
+    p += align256(size_t(B) * L * sizeof(uint16_t));
+    W.count = reinterpret_cast<uint32_t*>(p);
+    return W;
+}
+
+cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaStream_t stream) {
+    const uint32_t L = A.S.layer_count;
+    const size_t smem = (size_t(L) + 2u * (size_t(L) + 1u)) * sizeof(float);
+    const uint32_t blocks = A.S.band_count + (A.distinct ? 2u : 1u);
+    adjoint_prepare_kernel<<<blocks, 128, smem, stream>>>(A, W);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
+                                  bool accumulate, unsigned long long* counters, uint32_t* status,
+                                  cudaStream_t stream) {
+    const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    const uint64_t blocks = (cells * 32u + 255u) / 256u;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    const dim3 grid(static_cast<uint32_t>(blocks));
+    const uint32_t acc = accumulate ? 1u : 0u;
+    if (L.phase_sampling == SKY_PHASE_TABULATED)
+        adjoint_primal_kernel<SKY_PHASE_TABULATED>
+            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+    else
+        adjoint_primal_kernel<SKY_PHASE_ISOTROPIC>
+            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
+                                double* band_grad, unsigned long long* counters, uint32_t* status,
+                                cudaStream_t stream) {
+    const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    const size_t smem =
+        (size_t(3u * A.S.layer_count + 2u) + size_t(kAdjBandParams) * A.S.band_count) * sizeof(float);
+    const uint64_t want = (cells * 32u + 255u) / 256u;
+    if (L.phase_sampling == SKY_PHASE_TABULATED) {
+        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED>);
+        const uint32_t blocks = grid_blocks(k, 256, smem, want);
+        adjoint_grad_kernel<SKY_PHASE_TABULATED>
+            <<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad, band_grad, counters, status, cells);
+    } else {
+        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>);
+        const uint32_t blocks = grid_blocks(k, 256, smem, want);
+        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>
+            <<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad, band_grad, counters, status, cells);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace sky

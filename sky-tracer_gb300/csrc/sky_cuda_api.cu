@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/sky_cuda.h"
+#include "adjoint_kernels.h"
 #include "scene_build.h"
 #include "trace_kernels.h"
 
@@ -55,6 +56,9 @@ struct SkyScene {
     std::vector<float> host_majorants;
     float host_ground_radius = 0.0f, host_top = 0.0f;
     uint32_t host_layers = 0;
+    // differentiable rendering: tables rebuilt per call, allocated on first use
+    void* adj_ws = nullptr;
+    std::string adjoint_unsupported;  // empty when the scene's medium can be parameterised
 };
 
 namespace {
@@ -490,6 +494,18 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
         return st;
     }
     s->has_xyz = h.has_xyz;
+    // Differentiable renders parameterise aerosol species 0 only.
+    for (uint32_t sp = 1; sp < kSpecies && s->adjoint_unsupported.empty(); ++sp) {
+        bool mass = false, optics = false;
+        for (uint32_t i = 0; i < desc->aerosol_len; ++i) mass = mass || desc->aerosol[i].mass_g_m3[sp] != 0.0f;
+        for (uint32_t b = 0; b < desc->band_count; ++b) {
+            const SkyAerosolOptics& o = desc->aerosol_optics[size_t(b) * kSpecies + sp];
+            optics = optics || o.scattering_km_inv_per_g_m3 != 0.0f || o.absorption_km_inv_per_g_m3 != 0.0f;
+        }
+        if (mass && optics)
+            s->adjoint_unsupported = "differentiable renders need a scene whose only aerosol is species 0; species " +
+                                     std::to_string(sp) + " has mass and optics";
+    }
     cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
     if ((e = cudaMalloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
         (e = cudaMalloc(&s->work_counter, sizeof(uint32_t))) != cudaSuccess) {
@@ -514,6 +530,7 @@ void sky_cuda_scene_destroy(SkyScene* s) {
     cudaFreeHost(s->batch_host);
     cudaFree(s->batch_counter);
     cudaFree(s->trk_blob);
+    cudaFree(s->adj_ws);
     cudaFree(s->jobs);
     cudaFree(s->work_counter);
     cudaFree(s->blob);
@@ -752,6 +769,163 @@ extern "C" void sky_cuda_batch_graph_destroy(SkyBatchGraph* g) {
     cudaFree(g->counter);
     cudaFreeHost(g->host);
     delete g;
+}
+
+// ---- differentiable rendering -----------------------------------------------------
+
+namespace {
+
+// Kernel context of a differentiable render: the scene (with the caller's
+// sun), both parameter sets and the device workspace their tables go to.
+int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspace& W) {
+    if (!s) return set_error(SKY_ERR_INVALID_CONFIG, "scene is null");
+    if (!p || !p->layer_params) return set_error(SKY_ERR_INVALID_CONFIG, "params.layer_params is required");
+    if (!s->adjoint_unsupported.empty()) return set_error(SKY_ERR_INVALID_CONFIG, s->adjoint_unsupported);
+    if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    const uint32_t B = s->dev.band_count, L = s->dev.layer_count, bins = s->dev.phase_bins;
+    if (!s->adj_ws) {
+        cudaError_t e = cudaMalloc(&s->adj_ws, adjoint_workspace_bytes(B, L, bins));
+        if (e != cudaSuccess) {
+            s->adj_ws = nullptr;
+            return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "differentiable-render workspace allocation", e);
+        }
+    }
+    W = adjoint_workspace(s->adj_ws, B, L, bins);
+    A = AdjCtx{};
+    A.S = s->dev;
+    const float* d = p->sun_direction;
+    const float len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (len > 0.0f) {
+        if (!std::isfinite(len)) return set_error(SKY_ERR_INVALID_CONFIG, "sun direction must be finite");
+        for (int k = 0; k < 3; ++k) A.S.sun[k] = d[k] / len;
+        host_orthonormal_basis(A.S.sun, A.S.sun_t, A.S.sun_b);
+    }
+    auto tables = [bins](AdjParamSet& X, const float* t) {
+        X.phase = t;
+        X.dphase = t + bins;
+        X.cdf = t + 2 * bins;
+        X.bin_pdf = t + 3 * bins;
+    };
+    A.P.layer = p->layer_params;
+    A.P.band = p->band_params;
+    tables(A.P, W.p_tables);
+    A.distinct = (p->sample_layer_params && p->sample_layer_params != p->layer_params) ||
+                 (p->sample_band_params && p->sample_band_params != p->band_params);
+    if (A.distinct) {
+        A.Q.layer = p->sample_layer_params ? p->sample_layer_params : p->layer_params;
+        A.Q.band = p->sample_band_params ? p->sample_band_params : p->band_params;
+        tables(A.Q, W.q_tables);
+    } else {
+        A.Q = A.P;
+    }
+    A.G.layer_maj = W.layer_maj;
+    A.G.radius = W.radius;
+    A.G.maj = W.maj;
+    A.G.map = W.map;
+    A.G.count = W.count;
+    A.crossing_cost = s->tuning.crossing_cost;
+    if (p->estimator > SKY_ADJOINT_NULL_COLLISIONS)
+        return set_error(SKY_ERR_INVALID_CONFIG, "unknown adjoint estimator");
+    A.estimator = p->estimator;
+    return SKY_OK;
+}
+
+int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& L) {
+    int st = validate_config(s, c);
+    if (st) return st;
+    if (c->tracking != SKY_TRACKING_RESIDUAL_CARRY && c->tracking != SKY_TRACKING_MERGED_LAYERS)
+        return set_error(SKY_ERR_INVALID_CONFIG,
+                         "differentiable renders track with SKY_TRACKING_RESIDUAL_CARRY or SKY_TRACKING_MERGED_LAYERS");
+    A.merge = c->tracking == SKY_TRACKING_MERGED_LAYERS ? 1u : 0u;
+    SkyScene view;  // launch constants (sky-view LUT frame) for the render's sun
+    view.dev = A.S;
+    L = make_launch(&view, c);
+    view.dev = DevScene{};
+    return SKY_OK;
+}
+
+}  // namespace
+
+extern "C" uint32_t sky_cuda_adjoint_param_count(const SkyScene* scene) {
+    return scene ? 3u * scene->dev.layer_count + 2u : 0u;
+}
+
+extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderConfig* config,
+                                        const SkyAdjointParams* params, const SkyDeviceOutputs* outputs,
+                                        void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    AdjCtx A;
+    AdjWorkspace W;
+    DevLaunch L;
+    int st = adjoint_setup(s, params, A, W);
+    if (st) return st;
+    if ((st = adjoint_config(s, config, A, L))) return st;
+    if (!outputs || !outputs->cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
+    if (!outputs->status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.status is required");
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    const bool accumulate = (config->flags & SKY_FLAG_ACCUMULATE) != 0;
+    const uint32_t total_spp = accumulate ? config->sample_offset + config->spp : config->spp;
+    const uint64_t pixels = uint64_t(config->width) * config->height;
+    cudaError_t e = launch_adjoint_prepare(A, W, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+    e = launch_adjoint_primal(A, L, outputs->cell_sum, outputs->cell_sumsq, accumulate, outputs->counters,
+                              outputs->status, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
+    e = launch_finalize(A.S, pixels, total_spp, outputs->cell_sum, outputs->cell_sumsq, outputs->film,
+                        s->has_xyz ? outputs->xyz : nullptr, s->has_xyz ? outputs->xyz_var : nullptr, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
+    return SKY_OK;
+}
+
+extern "C" int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderConfig* config,
+                                         const SkyAdjointParams* params, const SkyAdjointGrads* grads,
+                                         void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    if (params && (params->sample_layer_params || params->sample_band_params))
+        return set_error(SKY_ERR_INVALID_CONFIG,
+                         "the gradient is taken at the sampling parameters: sample_layer_params and "
+                         "sample_band_params must be NULL");
+    AdjCtx A;
+    AdjWorkspace W;
+    DevLaunch L;
+    int st = adjoint_setup(s, params, A, W);
+    if (st) return st;
+    if ((st = adjoint_config(s, config, A, L))) return st;
+    if (!grads || !grads->dloss_dfilm || !grads->layer_grad)
+        return set_error(SKY_ERR_INVALID_CONFIG, "grads.dloss_dfilm and grads.layer_grad are required");
+    if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    cudaError_t e = launch_adjoint_prepare(A, W, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+    e = launch_adjoint_grad(A, L, grads->dloss_dfilm, grads->layer_grad, grads->band_grad, grads->counters,
+                            grads->status, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);
+    return SKY_OK;
+}
+
+extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* params, float* majorants_out,
+                                       void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    if (!majorants_out) return set_error(SKY_ERR_INVALID_CONFIG, "majorants_out is null");
+    SkyAdjointParams p{};
+    if (params) {
+        p = *params;
+        if (p.sample_layer_params) p.layer_params = p.sample_layer_params;
+        if (p.sample_band_params) p.band_params = p.sample_band_params;
+        p.sample_layer_params = nullptr;
+        p.sample_band_params = nullptr;
+    }
+    AdjCtx A;
+    AdjWorkspace W;
+    int st = adjoint_setup(s, params ? &p : nullptr, A, W);
+    if (st) return st;
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    cudaError_t e = launch_adjoint_prepare(A, W, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+    e = cudaMemcpyAsync(majorants_out, W.layer_maj, size_t(s->dev.band_count) * s->dev.layer_count * sizeof(float),
+                        cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "majorant copy", e);
+    return SKY_OK;
 }
 
 // ---- allocation-free batch render -------------------------------------------------

@@ -116,6 +116,23 @@ class SkyBatchJob(ctypes.Structure):
     ]
 
 
+class SkyAdjointParams(ctypes.Structure):
+    _fields_ = [
+        ("layer_params", _vp), ("band_params", _vp), ("sample_layer_params", _vp), ("sample_band_params", _vp),
+        ("sun_direction", _f * 3), ("estimator", _u32),
+    ]
+
+
+class SkyAdjointGrads(ctypes.Structure):
+    _fields_ = [
+        ("dloss_dfilm", _vp), ("layer_grad", _vp), ("band_grad", _vp), ("counters", _vp), ("status", _vp),
+    ]
+
+
+ADJOINT_BAND_PARAMS = 4
+ADJOINT_SEGMENT_INTEGRALS = 0
+ADJOINT_NULL_COLLISIONS = 1
+
 assert ctypes.sizeof(SkySceneDesc) == 120
 assert ctypes.sizeof(SkyRenderConfig) == 80
 assert ctypes.sizeof(SkyRenderStats) == 96
@@ -142,6 +159,14 @@ _SIGNATURES = {
                                                    ctypes.POINTER(_vp)]),
     "sky_cuda_batch_graph_launch": (ctypes.c_int, [_vp, _vp]),
     "sky_cuda_batch_graph_destroy": (None, [_vp]),
+    "sky_cuda_adjoint_param_count": (ctypes.c_uint32, [_vp]),
+    "sky_cuda_adjoint_forward": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
+                                                ctypes.POINTER(SkyAdjointParams), ctypes.POINTER(SkyDeviceOutputs),
+                                                _vp]),
+    "sky_cuda_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
+                                                 ctypes.POINTER(SkyAdjointParams), ctypes.POINTER(SkyAdjointGrads),
+                                                 _vp]),
+    "sky_cuda_bake_majorants": (ctypes.c_int, [_vp, ctypes.POINTER(SkyAdjointParams), _vp, _vp]),
     "sky_cuda_render_batch_noalloc": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                                      ctypes.POINTER(SkyDeviceOutputs), ctypes.c_uint32, _vp]),
 }

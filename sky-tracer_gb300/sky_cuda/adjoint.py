@@ -1,0 +1,211 @@
+"""Differentiable sky rendering: the forward/backward pair of the C ABI
+(sky_cuda_adjoint_forward / sky_cuda_adjoint_backward) and a
+torch.autograd.Function over it.
+
+No counterpart in the reference, which renders a fixed medium.  The medium
+of a differentiable render is the scene's with parameters applied (see
+include/sky_cuda.h): per majorant layer, density scales of Rayleigh, Mie
+(aerosol species 0) and ozone; the Mie single-scattering albedo and
+Henyey-Greenstein g; optionally per band, multipliers of the Rayleigh, Mie
+and ozone cross sections and of the solar radiance.  Gradients come from
+path-replay backpropagation on the GPU: no path is stored.
+
+    r = AdjointRenderer(gpu_scene, RenderConfig(width=128, height=64, spp=64))
+    theta = torch.tensor(initial_layer_params(scene, g=0.76), device="cuda", requires_grad=True)
+    film = render_film(r, theta)                 # [H, W, B], differentiable
+    loss = ((film_to_xyz(film, scene) - target) ** 2).sum()
+    loss.backward()                              # theta.grad via the adjoint kernel
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _abi
+from ._abi import SkyAdjointGrads, SkyAdjointParams, SkyDeviceOutputs, check
+from .render import GpuScene, RenderConfig
+from .scene import Scene
+
+BAND_PARAMS = _abi.ADJOINT_BAND_PARAMS
+PARAMS_PER_LAYER = 3  # Rayleigh, Mie, ozone density scales
+SEGMENT_INTEGRALS = _abi.ADJOINT_SEGMENT_INTEGRALS  # default backward estimator (lower variance)
+NULL_COLLISIONS = _abi.ADJOINT_NULL_COLLISIONS      # exact derivative of the forward estimator
+
+
+def mie_albedo(scene: Scene) -> float:
+    """Single-scattering albedo of aerosol species 0, averaged over bands."""
+    o = scene.aerosol_optics.reshape(scene.band_count, _abi.SPECIES_COUNT)[:, 0]
+    sca = o["scattering_km_inv_per_g_m3"].astype(np.float64)
+    ext = sca + o["absorption_km_inv_per_g_m3"].astype(np.float64)
+    keep = ext > 0
+    return float(np.mean(sca[keep] / ext[keep])) if keep.any() else 0.0
+
+
+def initial_layer_params(scene: Scene, g: float) -> np.ndarray:
+    """Parameters that reproduce `scene` (scales 1, the scene's Mie albedo, HG g)."""
+    layers = scene.layer_count
+    p = np.ones(PARAMS_PER_LAYER * layers + 2, dtype=np.float32)
+    p[PARAMS_PER_LAYER * layers] = mie_albedo(scene)
+    p[PARAMS_PER_LAYER * layers + 1] = g
+    return p
+
+
+def param_names(layers: int) -> list[str]:
+    names = [f"{kind}[{l}]" for l in range(layers) for kind in ("rayleigh", "mie", "ozone")]
+    return names + ["mie_albedo", "mie_g"]
+
+
+def _ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+class AdjointRenderer:
+    """Forward and backward renders of one RenderConfig on a GpuScene.
+
+    Tensors are CUDA torch tensors; calls are queued on torch's current
+    stream.  Tracking defaults to merged layers (the fastest mode)."""
+
+    def __init__(self, gs: GpuScene, config: RenderConfig, estimator: int = SEGMENT_INTEGRALS):
+        import torch
+        if config.tracking == _abi.TRACKING_SEGMENT_RESTART:
+            config = RenderConfig(**{**config.__dict__, "tracking": _abi.TRACKING_MERGED_LAYERS})
+        self.gs = gs
+        self.lib = gs.lib
+        self.config = config
+        self.estimator = estimator
+        self._c_config = config.to_c()
+        self.bands = gs.band_count
+        self.pixels = config.pixels
+        self.param_count = int(self.lib.sky_cuda_adjoint_param_count(gs.handle))
+        self.layers = (self.param_count - 2) // PARAMS_PER_LAYER
+        self._status = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def _params(self, layer, band, sample_layer=None, sample_band=None, sun=None) -> SkyAdjointParams:
+        for name, t, n in (("layer_params", layer, self.param_count), ("sample_layer_params", sample_layer,
+                                                                       self.param_count),
+                           ("band_params", band, self.bands * BAND_PARAMS),
+                           ("sample_band_params", sample_band, self.bands * BAND_PARAMS)):
+            if t is None:
+                continue
+            if not (t.is_cuda and t.is_contiguous()) or t.numel() != n or str(t.dtype) != "torch.float32":
+                raise ValueError(f"{name} must be a contiguous float32 CUDA tensor of {n} values")
+        p = SkyAdjointParams()
+        p.layer_params = _ptr(layer)
+        p.band_params = _ptr(band)
+        p.sample_layer_params = _ptr(sample_layer)
+        p.sample_band_params = _ptr(sample_band)
+        p.sun_direction = (ctypes.c_float * 3)(*(sun if sun is not None else (0.0, 0.0, 0.0)))
+        p.estimator = self.estimator
+        return p
+
+    def _check_status(self) -> None:
+        import torch
+        torch.cuda.current_stream().synchronize()
+        if int(self._status.item()):
+            self._status.zero_()
+            raise _abi.RenderWatchdog(_abi.SKY_ERR_WATCHDOG, "GPU path watchdog was reached")
+
+    def forward(self, layer, band=None, *, sample_layer=None, sample_band=None, sun=None, xyz: bool = False,
+                check_status: bool = True) -> dict:
+        """Film [pixels * B] (float32) and cell sums; XYZ and its variance too with xyz=True."""
+        import torch
+        cells = self.pixels * self.bands
+        out = {
+            "cell_sum": torch.empty(cells, dtype=torch.float64, device="cuda"),
+            "cell_sumsq": torch.empty(cells, dtype=torch.float64, device="cuda"),
+            "film": torch.empty(cells, dtype=torch.float32, device="cuda"),
+        }
+        if xyz:
+            out["xyz"] = torch.empty(self.pixels * 3, dtype=torch.float64, device="cuda")
+            out["xyz_var"] = torch.empty(self.pixels * 3, dtype=torch.float64, device="cuda")
+        o = SkyDeviceOutputs()
+        for name, _ in SkyDeviceOutputs._fields_:
+            setattr(o, name, _ptr(out.get(name)))
+        o.status = self._status.data_ptr()
+        p = self._params(layer, band, sample_layer, sample_band, sun)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(self.lib.sky_cuda_adjoint_forward(self.gs.handle, ctypes.byref(self._c_config), ctypes.byref(p),
+                                                ctypes.byref(o), ctypes.c_void_p(stream)), self.lib)
+        if check_status:
+            self._check_status()
+        return out
+
+    def backward(self, layer, band, dloss_dfilm, *, sun=None, check_status: bool = True):
+        """(dLoss/dlayer_params, dLoss/dband_params or None) as float64 tensors."""
+        import torch
+        d = dloss_dfilm.reshape(-1).to(torch.float32).contiguous()
+        if d.numel() != self.pixels * self.bands:
+            raise ValueError("dloss_dfilm must hold pixels * bands values")
+        lg = torch.zeros(self.param_count, dtype=torch.float64, device="cuda")
+        bg = torch.zeros(self.bands * BAND_PARAMS, dtype=torch.float64, device="cuda") if band is not None else None
+        g = SkyAdjointGrads()
+        g.dloss_dfilm = d.data_ptr()
+        g.layer_grad = lg.data_ptr()
+        g.band_grad = _ptr(bg)
+        g.status = self._status.data_ptr()
+        p = self._params(layer, band, None, None, sun)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(self.lib.sky_cuda_adjoint_backward(self.gs.handle, ctypes.byref(self._c_config), ctypes.byref(p),
+                                                 ctypes.byref(g), ctypes.c_void_p(stream)), self.lib)
+        if check_status:
+            self._check_status()
+        return lg, bg
+
+    def bake_majorants(self, layer, band=None):
+        """Majorant grid [B, L] of the parameterised medium (device bake)."""
+        import torch
+        out = torch.empty((self.bands, self.layers), dtype=torch.float32, device="cuda")
+        p = self._params(layer, band)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(self.lib.sky_cuda_bake_majorants(self.gs.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()),
+                                               ctypes.c_void_p(stream)), self.lib)
+        return out
+
+
+def _autograd_function():
+    import torch
+
+    class SkyRenderFunction(torch.autograd.Function):
+        """film = render(layer_params, band_params); backward runs the adjoint kernel."""
+
+        @staticmethod
+        def forward(ctx, layer, band, renderer, sun):
+            layer_c = layer.detach().contiguous()
+            band_c = band.detach().contiguous() if band is not None else None
+            out = renderer.forward(layer_c, band_c, sun=sun)
+            ctx.renderer = renderer
+            ctx.sun = sun
+            ctx.has_band = band is not None
+            ctx.save_for_backward(layer_c, band_c if band_c is not None else layer_c)
+            cfg = renderer.config
+            return out["film"].reshape(cfg.height, cfg.width, renderer.bands)
+
+        @staticmethod
+        def backward(ctx, grad_film):
+            layer_c, band_c = ctx.saved_tensors
+            band_c = band_c if ctx.has_band else None
+            lg, bg = ctx.renderer.backward(layer_c, band_c, grad_film.contiguous(), sun=ctx.sun)
+            return lg.to(layer_c.dtype), (bg.to(band_c.dtype) if bg is not None else None), None, None
+
+    return SkyRenderFunction
+
+
+_FUNCTION = None
+
+
+def render_film(renderer: AdjointRenderer, layer, band=None, sun=None):
+    """Differentiable film [H, W, B] (float32) of the renderer's config."""
+    global _FUNCTION
+    if _FUNCTION is None:
+        _FUNCTION = _autograd_function()
+    return _FUNCTION.apply(layer, band, renderer, sun)
+
+
+def film_to_xyz(film, scene: Scene):
+    """CIE XYZ [H, W, 3] (float64) of a film, with the scene's band weights
+    (spectrum_to_xyz_with_weights, spectrum.rs:232-241)."""
+    import torch
+    w = torch.as_tensor(np.asarray(scene.band_xyz, dtype=np.float64), device=film.device)
+    return film.to(torch.float64) @ w

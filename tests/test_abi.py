@@ -45,6 +45,7 @@ def test_struct_layouts_match_header(tmp_path):
         "SkySceneDesc": _abi.SkySceneDesc, "SkyRenderConfig": _abi.SkyRenderConfig,
         "SkyRenderStats": _abi.SkyRenderStats, "SkyDeviceOutputs": _abi.SkyDeviceOutputs,
         "SkyTuning": _abi.SkyTuning, "SkyBatchJob": _abi.SkyBatchJob,
+        "SkyAdjointParams": _abi.SkyAdjointParams, "SkyAdjointGrads": _abi.SkyAdjointGrads,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for name, dt in structs.items():

@@ -1,0 +1,332 @@
+"""Differentiable rendering through the C ABI (sky_cuda_adjoint_*).
+
+  * the primal over the parameterised medium at the scene's own parameters
+    traces the plain tracer's chains (same random numbers) and matches its
+    statistics;
+  * the device majorant bake reproduces the scene's grid and a numpy bake of
+    a perturbed medium;
+  * the path-replay gradient equals central finite differences (h = 1e-3) of
+    the same estimator with its samples held fixed (the sampling parameters
+    stay at the evaluation point while the evaluated ones move);
+  * summed along whole-atmosphere directions it agrees, within statistical
+    error, with central differences of the plain tracer at 4096 spp;
+  * the torch.autograd.Function returns the same gradient.
+"""
+
+import dataclasses
+
+import numpy as np
+import pytest
+
+from sky_cuda import GpuScene, RenderConfig, SkyCudaError, synthetic_scene, wavelengths
+from sky_cuda import _abi
+from sky_cuda.adjoint import (BAND_PARAMS, NULL_COLLISIONS, SEGMENT_INTEGRALS, AdjointRenderer, film_to_xyz,
+                              initial_layer_params, param_names, render_film)
+from sky_cuda.scene import SPECIES_COUNT, hg_phase_values
+from skystats import parity_report, xyz_from_sums
+
+pytestmark = pytest.mark.gpu
+
+G0 = 0.76  # HG asymmetry of the synthetic scene's aerosol
+
+
+def _t(x, dtype=None):
+    import torch
+    return torch.as_tensor(np.asarray(x), device="cuda", dtype=dtype or torch.float32).contiguous()
+
+
+def plain_sums(gs, cfg):
+    import torch
+    cells = cfg.pixels * gs.band_count
+    s = torch.zeros(cells, dtype=torch.float64, device="cuda")
+    q = torch.zeros(cells, dtype=torch.float64, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    gs.render_device(cfg, {"cell_sum": s.data_ptr(), "cell_sumsq": q.data_ptr(), "status": st.data_ptr()},
+                     torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    return s.cpu().numpy(), q.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def small_scene(data_dir):
+    """8 bands (400-700 nm) of the benchmark atmosphere, sun at 10 degrees."""
+    return synthetic_scene(wavelengths(400.0, 700.0, 8), data_dir, sun_elevation_deg=10.0)
+
+
+@pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
+def test_primal_traces_the_plain_chains(gpu, cfg0_scene, phase):
+    """One sample per cell: the adjoint primal (residual carry over the
+    device-baked uniform layers) and the plain tracer (residual carry over the
+    scene's grid) consume the same random numbers; their chains agree except
+    where float rounding flips a decision."""
+    cfg = RenderConfig(width=32, height=16, spp=1, sample_offset=3, phase_sampling=phase,
+                       tracking=_abi.TRACKING_RESIDUAL_CARRY)
+    with GpuScene(cfg0_scene) as gs:
+        want, _ = plain_sums(gs, dataclasses.replace(cfg, kernel=_abi.KERNEL_PLAIN))
+        r = AdjointRenderer(gs, cfg)
+        got = r.forward(_t(initial_layer_params(cfg0_scene, G0)))["cell_sum"].cpu().numpy()
+    close = np.abs(got - want) <= 1e-3 * np.maximum(np.abs(got), np.abs(want)) + 1e-30
+    print("chain agreement", close.mean())
+    assert close.mean() >= 0.98
+
+
+def test_primal_statistics_match_plain_tracer(gpu, cfg0_scene):
+    cfg = RenderConfig(width=32, height=16, spp=256, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    with GpuScene(cfg0_scene) as gs:
+        s_p, q_p = plain_sums(gs, cfg)
+        out = AdjointRenderer(gs, dataclasses.replace(cfg, seed=cfg.seed + 1)).forward(
+            _t(initial_layer_params(cfg0_scene, G0)))
+    s_a, q_a = out["cell_sum"].cpu().numpy(), out["cell_sumsq"].cpu().numpy()
+    shape = (cfg.pixels, cfg0_scene.band_count)
+    xa, va = xyz_from_sums(s_a.reshape(shape), q_a.reshape(shape), cfg.spp, cfg0_scene.band_xyz)
+    xp, vp = xyz_from_sums(s_p.reshape(shape), q_p.reshape(shape), cfg.spp, cfg0_scene.band_xyz)
+    rep = parity_report(xa, va, xp, vp)
+    print("adjoint primal vs plain", rep)
+    assert rep["frac_beyond_3se"] <= 0.02
+    for b, se in zip(rep["bias_xyz"], rep["bias_se_xyz"]):
+        assert abs(b) <= 4 * se + 1e-3
+
+
+def _numpy_bake(scene, params, layers):
+    """compute_majorant_grid's probe rule over the parameterised medium."""
+    top = np.float32(scene.atmosphere_radius_km) - np.float32(scene.ground_radius_km)
+    dz = top / np.float32(layers)
+    atm, aer = scene.atmosphere, scene.aerosol
+    opt = scene.aerosol_optics.reshape(scene.band_count, SPECIES_COUNT)[:, 0]
+    ext0 = opt["scattering_km_inv_per_g_m3"].astype(np.float64) + opt["absorption_km_inv_per_g_m3"]
+    xs_r = scene.bands["rayleigh_cross_section_m2"].astype(np.float64) * 1e9
+    xs_o = scene.bands["ozone_cross_section_cm2"].astype(np.float64) * 1e5
+    knots = np.concatenate([atm["altitude_km"], aer["altitude_km"]]).astype(np.float64)
+    out = np.zeros((scene.band_count, layers))
+    for l in range(layers):
+        lo, hi = float(np.float32(l) * dz), float(np.float32(l + 1) * dz)
+        h = np.array([lo, hi, 0.5 * (lo + hi)] + [z for z in knots if lo < z < hi])
+        air = np.interp(h, atm["altitude_km"], atm["air_cm3"])
+        o3 = np.interp(h, atm["altitude_km"], atm["ozone_cm3"])
+        m0 = np.interp(h, aer["altitude_km"], aer["mass_g_m3"][:, 0])
+        sr, sm, so = params[3 * l:3 * l + 3]
+        ext = sr * xs_r[:, None] * air + sm * ext0[:, None] * m0 + so * xs_o[:, None] * o3
+        out[:, l] = np.maximum(ext.max(axis=1) * 1.05, 1e-8)
+    return out
+
+
+def test_device_majorant_bake(gpu, cfg0_scene):
+    layers = cfg0_scene.layer_count
+    theta0 = initial_layer_params(cfg0_scene, G0)
+    rng = np.random.default_rng(3)
+    theta = theta0.copy()
+    theta[:3 * layers] = (1.0 + rng.normal(0.0, 0.05, 3 * layers)).astype(np.float32)
+    with GpuScene(cfg0_scene) as gs:
+        r = AdjointRenderer(gs, RenderConfig(width=4, height=4, spp=1, tracking=_abi.TRACKING_MERGED_LAYERS))
+        base = r.bake_majorants(_t(theta0)).cpu().numpy()
+        moved = r.bake_majorants(_t(theta)).cpu().numpy()
+    np.testing.assert_allclose(base, cfg0_scene.majorants, rtol=2e-5)
+    np.testing.assert_allclose(moved, _numpy_bake(cfg0_scene, theta, layers), rtol=1e-4)
+
+
+def _loss_setup(gs, scene, cfg, target_spp=256):
+    """The adjoint benchmark's loss: L2 on XYZ against a target rendered at
+    perturbed parameters.  The loss reads the FP64 cell sums (the float32
+    film's rounding would swamp finite differences of small gradients)."""
+    import torch
+    layers = scene.layer_count
+    theta0 = initial_layer_params(scene, G0)
+    rng = np.random.default_rng(3)
+    theta_t = theta0.copy()
+    theta_t[:3 * layers] = (1.0 + rng.normal(0.0, 0.05, 3 * layers)).astype(np.float32)
+    theta_t[3 * layers] *= np.float32(1.0 + rng.normal(0.0, 0.02))
+    theta_t[3 * layers + 1] += np.float32(rng.normal(0.0, 0.02))
+    tcfg = dataclasses.replace(cfg, spp=target_spp, seed=cfg.seed ^ 0xABCDEF)
+    w = torch.as_tensor(np.asarray(scene.band_xyz, np.float64), device="cuda")
+
+    def xyz_of(out, spp):
+        return (out["cell_sum"] / spp).reshape(cfg.pixels, scene.band_count) @ w
+
+    txyz = xyz_of(AdjointRenderer(gs, tcfg).forward(_t(theta_t)), target_spp)
+
+    def loss_of(out):
+        return float(((xyz_of(out, cfg.spp) - txyz) ** 2).sum().item())
+
+    def dloss(out):
+        return (2.0 * (xyz_of(out, cfg.spp) - txyz) @ w.T).float()
+
+    return theta0, loss_of, dloss
+
+
+def test_gradient_matches_central_differences(gpu, cfg0_scene):
+    """The adjoint benchmark's finite-difference check (h = 1e-3, 16 parameters drawn with
+    seed 4) on a 32x16 image, 32 bands, 64 spp."""
+    cfg = RenderConfig(width=32, height=16, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    h = 1e-3
+    with GpuScene(cfg0_scene) as gs:
+        theta0, loss_of, dloss = _loss_setup(gs, cfg0_scene, cfg)
+        r = AdjointRenderer(gs, cfg, estimator=NULL_COLLISIONS)
+        th0 = _t(theta0)
+        grad, _ = r.backward(th0, None, dloss(r.forward(th0)))
+        grad = grad.cpu().numpy()
+        idx = np.random.default_rng(4).choice(theta0.size, 16, replace=False)
+        names = param_names(cfg0_scene.layer_count)
+        rows = []
+        for i in idx:
+            tp, tm = theta0.copy(), theta0.copy()
+            tp[i] += np.float32(h)
+            tm[i] -= np.float32(h)
+            jp = loss_of(r.forward(_t(tp), sample_layer=th0))
+            jm = loss_of(r.forward(_t(tm), sample_layer=th0))
+            rows.append((names[i], (jp - jm) / float(tp[i] - tm[i]), grad[i]))
+    scale = np.abs(grad).max()
+    for name, fd, g in rows:
+        print(f"{name:14s} fd {fd: .6e} adjoint {g: .6e} rel {abs(fd - g) / max(abs(fd), 1e-300):.2e}")
+    for name, fd, g in rows:
+        assert abs(fd - g) <= 1e-2 * abs(fd) + 2e-5 * scale, name
+
+
+def test_band_gradients_match_central_differences(gpu, small_scene):
+    cfg = RenderConfig(width=16, height=8, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    h = 1e-3
+    B = small_scene.band_count
+    with GpuScene(small_scene) as gs:
+        theta0, loss_of, dloss = _loss_setup(gs, small_scene, cfg)
+        r = AdjointRenderer(gs, cfg, estimator=NULL_COLLISIONS)
+        th0 = _t(theta0)
+        band0 = np.ones(B * BAND_PARAMS, dtype=np.float32)
+        b0 = _t(band0)
+        lg, bg = r.backward(th0, b0, dloss(r.forward(th0, b0)))
+        bg = bg.cpu().numpy()
+        rows = []
+        for b in (1, 5):
+            for k in range(BAND_PARAMS):
+                i = b * BAND_PARAMS + k
+                bp, bm = band0.copy(), band0.copy()
+                bp[i] += np.float32(h)
+                bm[i] -= np.float32(h)
+                jp = loss_of(r.forward(th0, _t(bp), sample_band=b0))
+                jm = loss_of(r.forward(th0, _t(bm), sample_band=b0))
+                rows.append((f"band{b}.{('R', 'M', 'O', 'S')[k]}", (jp - jm) / float(bp[i] - bm[i]), bg[i]))
+    scale = np.abs(bg).max()
+    for name, fd, g in rows:
+        print(f"{name:10s} fd {fd: .6e} adjoint {g: .6e}")
+    for name, fd, g in rows:
+        assert abs(fd - g) <= 1e-2 * abs(fd) + 2e-5 * scale, name
+
+
+def _scene_along(scene, direction, delta):
+    """The synthetic scene moved along one whole-atmosphere direction."""
+    s = dataclasses.replace(scene)
+    bands = scene.bands.copy()
+    optics = scene.aerosol_optics.copy()
+    phase = scene.phase_values.copy()
+    sca = optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT].astype(np.float64)
+    ab = optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT].astype(np.float64)
+    if direction == "rayleigh":
+        bands["rayleigh_cross_section_m2"] *= np.float32(1 + delta)
+    elif direction == "mie":
+        optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT] = sca * (1 + delta)
+        optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT] = ab * (1 + delta)
+    elif direction == "ozone":
+        bands["ozone_cross_section_cm2"] *= np.float32(1 + delta)
+    elif direction == "albedo":
+        ext = sca + ab
+        omega = sca / ext + delta
+        optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT] = ext * omega
+        optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT] = ext * (1 - omega)
+    elif direction == "g":
+        phase[0] = hg_phase_values(G0 + delta, scene.phase_bins)[None, :]
+    s.bands, s.aerosol_optics, s.phase_values = bands, optics, phase
+    return s.bake_majorants(scene.layer_count)
+
+
+@pytest.mark.parametrize("estimator", [SEGMENT_INTEGRALS, NULL_COLLISIONS])
+@pytest.mark.parametrize("direction,delta", [("rayleigh", 0.05), ("mie", 0.05), ("ozone", 0.2), ("albedo", 0.02),
+                                             ("g", 0.02)])
+def test_gradient_matches_plain_tracer_differences(gpu, small_scene, direction, delta, estimator):
+    """The adjoint gradient projected on a whole-atmosphere direction against
+    central differences of the plain tracer (scene tables moved along the
+    direction, 4096 spp in 16 batches, common seeds), for the linear loss
+    J = sum_cells w_cell film_cell."""
+    import torch
+    batches, spp = 16, 256
+    L = small_scene.layer_count
+    cfg = RenderConfig(width=16, height=8, spp=spp, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    cells = cfg.pixels * small_scene.band_count
+    w = np.random.default_rng(7).uniform(0.5, 1.5, cells) / cells
+    proj = {"rayleigh": lambda g: g[0:3 * L:3].sum(), "mie": lambda g: g[1:3 * L:3].sum(),
+            "ozone": lambda g: g[2:3 * L:3].sum(), "albedo": lambda g: g[3 * L], "g": lambda g: g[3 * L + 1]}[direction]
+    fd, adj = [], []
+    with GpuScene(_scene_along(small_scene, direction, +delta)) as gp, \
+            GpuScene(_scene_along(small_scene, direction, -delta)) as gm, GpuScene(small_scene) as g0:
+        th0 = _t(initial_layer_params(small_scene, G0))
+        wt = _t(w)
+        for k in range(batches):
+            c = dataclasses.replace(cfg, sample_offset=k * spp)
+            jp = float(np.dot(plain_sums(gp, c)[0], w)) / spp
+            jm = float(np.dot(plain_sums(gm, c)[0], w)) / spp
+            fd.append((jp - jm) / (2 * delta))
+            rk = AdjointRenderer(g0, c, estimator=estimator)
+            lg, _ = rk.backward(th0, None, wt)
+            adj.append(proj(lg.cpu().numpy()))
+    fd, adj = np.array(fd), np.array(adj)
+    se = np.sqrt(fd.var(ddof=1) / batches + adj.var(ddof=1) / batches)
+    print(f"{direction} (estimator {estimator}): plain FD {fd.mean():.6e} +- {fd.std(ddof=1) / 4:.2e}, "
+          f"adjoint {adj.mean():.6e} +- {adj.std(ddof=1) / 4:.2e}")
+    assert abs(fd.mean() - adj.mean()) <= 4 * se + 0.02 * abs(fd.mean())
+
+
+def test_autograd_function_matches_direct_backward(gpu, small_scene):
+    import torch
+    cfg = RenderConfig(width=16, height=8, spp=32, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    with GpuScene(small_scene) as gs:
+        r = AdjointRenderer(gs, cfg)
+        layer = _t(initial_layer_params(small_scene, G0)).requires_grad_(True)
+        band = _t(np.ones(small_scene.band_count * BAND_PARAMS, np.float32)).requires_grad_(True)
+        target = torch.zeros((cfg.height, cfg.width, 3), dtype=torch.float64, device="cuda")
+        film = render_film(r, layer, band)
+        assert film.shape == (cfg.height, cfg.width, small_scene.band_count)
+        xyz = film_to_xyz(film, small_scene)
+        loss = ((xyz - target) ** 2).sum()
+        loss.backward()
+        w = torch.as_tensor(np.asarray(small_scene.band_xyz, np.float64), device="cuda")
+        d = (2.0 * xyz.detach().reshape(-1, 3) @ w.T).float()
+        lg, bg = r.backward(layer.detach(), band.detach(), d)
+    np.testing.assert_allclose(layer.grad.cpu().numpy(), lg.float().cpu().numpy(), rtol=1e-4,
+                               atol=1e-6 * float(lg.abs().max()))
+    np.testing.assert_allclose(band.grad.cpu().numpy(), bg.float().cpu().numpy(), rtol=1e-4,
+                               atol=1e-6 * float(bg.abs().max()))
+
+
+def test_adjoint_errors(gpu, ref_scene, cfg0_scene):
+    import ctypes
+    import torch
+    with GpuScene(ref_scene) as gs:  # the reference's four aerosol species
+        r = AdjointRenderer(gs, RenderConfig(width=4, height=4, spp=1))
+        with pytest.raises(SkyCudaError, match="species"):
+            r.forward(torch.ones(r.param_count, device="cuda"))
+    with GpuScene(cfg0_scene) as gs:
+        lib = gs.lib
+        cfg = RenderConfig(width=4, height=4, spp=1, tracking=_abi.TRACKING_SEGMENT_RESTART).to_c()
+        th = _t(initial_layer_params(cfg0_scene, G0))
+        p = _abi.SkyAdjointParams()
+        p.layer_params = th.data_ptr()
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        s = torch.zeros(16 * cfg0_scene.band_count, dtype=torch.float64, device="cuda")
+        o = _abi.SkyDeviceOutputs()
+        o.cell_sum, o.status = s.data_ptr(), st.data_ptr()
+        assert lib.sky_cuda_adjoint_forward(gs.handle, ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(o),
+                                            None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert "RESIDUAL_CARRY" in _abi.last_error(lib)
+        r = AdjointRenderer(gs, RenderConfig(width=4, height=4, spp=1))
+        other = th.clone()  # a second parameter set is refused by the backward call
+        p.sample_layer_params = other.data_ptr()
+        g = _abi.SkyAdjointGrads()
+        d = torch.zeros(16 * cfg0_scene.band_count, device="cuda")
+        lg = torch.zeros(r.param_count, dtype=torch.float64, device="cuda")
+        g.dloss_dfilm, g.layer_grad, g.status = d.data_ptr(), lg.data_ptr(), st.data_ptr()
+        assert lib.sky_cuda_adjoint_backward(gs.handle, ctypes.byref(r._c_config), ctypes.byref(p),
+                                             ctypes.byref(g), None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert lib.sky_cuda_adjoint_param_count(gs.handle) == 3 * cfg0_scene.layer_count + 2
