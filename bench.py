@@ -54,9 +54,12 @@ WORKLOADS = {
                                       rr_start_depth=8, max_orders=0),
 }
 DEFAULT_WORKLOAD = "plain-512x256-81wl-256spp"
-# configs[2]: 32 sun elevations on [-6, 90] (denser near the horizon), each a
+# the elevation sweep: 32 sun elevations on [-6, 90] (denser near the horizon), each a
 # 256x128 sky-view LUT over 40 wavelengths, spp 64-1024 from a 16-spp pilot
 SWEEP_WORKLOAD = "sweep-32x256x128-40wl"
+ADJOINT_WORKLOAD = "adjoint-128x64-32wl-64spp"
+# 4 primary wavelengths + a 4x3 XYZ matrix fitted against 81-wavelength renders at 16 elevations
+FIT_WORKLOAD = "fit-16x256x128-4primaries"
 
 
 def parse_args():
@@ -65,7 +68,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    p.add_argument("--workload", choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD], default=DEFAULT_WORKLOAD)
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD, ADJOINT_WORKLOAD, FIT_WORKLOAD],
+                   default=DEFAULT_WORKLOAD)
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
@@ -73,6 +77,10 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    p.add_argument("--no-adjoint", action="store_true", help="leave the differentiable-render block out")
+    p.add_argument("--fit-iterations", type=int, default=200, help="Adam steps of each primary fit")
+    p.add_argument("--no-adjoint-checks", action="store_true",
+                   help="time the differentiable render only (no gradient checks)")
     return p.parse_args()
 
 
@@ -332,12 +340,263 @@ def run_sweep(args):
     gs.close()
 
 
+def _sun_pixel_mask(scene, cfg):
+    """Panorama pixels whose footprint holds part of the sun disc."""
+    x, y, z = scene.sun_direction
+    u = math.atan2(x, z) / (2 * math.pi) + 0.5
+    v = 0.5 - math.asin(y) / math.pi
+    r = scene.sun_angular_radius_rad
+    du, dv = r / (2 * math.pi * max(math.cos(math.asin(y)), 1e-3)), r / math.pi
+    px = np.arange(cfg.pixels) % cfg.width
+    py = np.arange(cfg.pixels) // cfg.width
+    return (((px + 1) / cfg.width >= u - du) & (px / cfg.width <= u + du) &
+            ((py + 1) / cfg.height >= v - dv) & (py / cfg.height <= v + dv))
+
+
+def adjoint_report(args, steps, warmup, checks=True):
+    """Differentiable render of a 128x64 panorama, 32 wavelengths, 64 spp: L2
+    loss on XYZ against a target rendered at perturbed parameters (64 layers x
+    3 density scales ~ 1 + N(0, 0.05), seed 3, plus Mie albedo and g), the
+    pixels holding the sun disc left out of the loss.  Times
+    forward + backward (path replay) and checks the gradient against central
+    differences (h = 1e-3, 16 parameters, seed 4) of the same estimator with
+    shared samples, against the 4096-spp adjoint gradient, and, along five
+    whole-atmosphere directions, against central differences of the plain
+    tracer at 4096 spp."""
+    import dataclasses
+    import torch
+    from sky_cuda import GpuScene, RenderConfig, synthetic_scene, wavelengths
+    from sky_cuda import _abi
+    from sky_cuda.adjoint import NULL_COLLISIONS, AdjointRenderer, initial_layer_params, param_names
+    from sky_cuda.scene import SPECIES_COUNT, hg_phase_values
+    g0 = 0.76
+    scene = synthetic_scene(wavelengths(380.0, 780.0, 32), DATA_DIR, sun_elevation_deg=10.0)
+    cfg = RenderConfig(width=128, height=64, spp=64, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS, rr_start_depth=8, seed=0x5EC7_2026_0430)
+    B, L = scene.band_count, scene.layer_count
+    cells = cfg.pixels * B
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.as_tensor(np.asarray(a), device=dev, dtype=torch.float32).contiguous()  # noqa: E731
+    theta0 = initial_layer_params(scene, g0)
+    rng = np.random.default_rng(3)
+    theta_t = theta0.copy()
+    theta_t[:3 * L] = (1.0 + rng.normal(0.0, 0.05, 3 * L)).astype(np.float32)
+    theta_t[3 * L] *= np.float32(1.0 + rng.normal(0.0, 0.02))
+    theta_t[3 * L + 1] += np.float32(rng.normal(0.0, 0.02))
+    w = torch.as_tensor(np.asarray(scene.band_xyz, np.float64), device=dev)
+    gs = GpuScene(scene)
+    r = AdjointRenderer(gs, cfg)
+    th0 = t(theta0)
+
+    # the pixels holding the sun disc stay out of the loss: rare sun hits dominate their value
+    keep = torch.as_tensor(~_sun_pixel_mask(scene, cfg), device=dev, dtype=torch.float64)[:, None]
+
+    def xyz_of(out, spp):
+        return (out["cell_sum"] / spp).reshape(cfg.pixels, B) @ w
+
+    tgt = AdjointRenderer(gs, dataclasses.replace(cfg, spp=1024, seed=cfg.seed ^ 0xABCDEF)).forward(t(theta_t))
+    txyz = xyz_of(tgt, 1024)
+
+    def dloss(out):
+        return (2.0 * keep * (xyz_of(out, cfg.spp) - txyz) @ w.T).float()
+
+    def step():
+        out = r.forward(th0, check_status=False)
+        return out, r.backward(th0, None, dloss(out), check_status=False)
+
+    for _ in range(max(warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    fwd_ms, bwd_ms = [], []
+    stream = torch.cuda.current_stream()
+    for _ in range(steps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        out = r.forward(th0, check_status=False)
+        e1.record(stream)
+        d = dloss(out)
+        e_b = torch.cuda.Event(enable_timing=True)
+        e_b.record(stream)
+        grad, _ = r.backward(th0, None, d, check_status=False)
+        e2.record(stream)
+        e2.synchronize()
+        fwd_ms.append(e0.elapsed_time(e1))
+        bwd_ms.append(e_b.elapsed_time(e2))
+    r._check_status()
+    chains = cells * cfg.spp
+    f_ms, b_ms = statistics.median(fwd_ms), statistics.median(bwd_ms)
+    rep = {"workload": "adjoint-128x64-32wl-64spp", "params": int(theta0.size), "chains_per_render": chains,
+           "forward_ms": f_ms, "backward_ms": b_ms, "step_ms": f_ms + b_ms,
+           "forward_chains_per_s": chains / (f_ms * 1e-3), "backward_chains_per_s": chains / (b_ms * 1e-3),
+           "step_chains_per_s": chains / ((f_ms + b_ms) * 1e-3), "estimator": "segment integrals",
+           "gpu_launches_per_step": 5}
+    if not checks:
+        gs.close()
+        return rep
+    # central differences of the same estimator, samples shared (h = 1e-3, 16 parameters, seed 4)
+    rn = AdjointRenderer(gs, cfg, estimator=NULL_COLLISIONS)
+    d0 = dloss(rn.forward(th0))
+    gnull = rn.backward(th0, None, d0)[0].cpu().numpy()
+
+    def loss_of(out):
+        return float((keep * (xyz_of(out, cfg.spp) - txyz) ** 2).sum().item())
+
+    names = param_names(L)
+    rows = []
+    for i in np.random.default_rng(4).choice(theta0.size, 16, replace=False):
+        tp, tm = theta0.copy(), theta0.copy()
+        tp[i] += np.float32(1e-3)
+        tm[i] -= np.float32(1e-3)
+        fd = (loss_of(rn.forward(t(tp), sample_layer=th0)) - loss_of(rn.forward(t(tm), sample_layer=th0))) / \
+            float(tp[i] - tm[i])
+        rows.append((names[int(i)], fd, float(gnull[i])))
+    scale = float(np.abs(gnull).max())
+    resolved = [(n, fd, g) for n, fd, g in rows if abs(fd) > 1e-5 * scale]
+    rep["fd_check"] = {
+        "h": 1e-3, "params": [[n, fd, g] for n, fd, g in rows], "estimator": "null collisions",
+        "resolved_params": len(resolved),
+        "max_rel_err_resolved": max((abs(fd - g) / abs(fd) for n, fd, g in resolved), default=None),
+        "max_abs_err_over_max_grad": max(abs(fd - g) for n, fd, g in rows) / scale}
+    # the 64-spp gradient against the 4096-spp gradient with the same dLoss/dfilm
+    batches, bspp = 16, 256
+    dfix = d0.clone()
+    g64 = r.backward(th0, None, dfix)[0].cpu().numpy()
+    gref = np.zeros_like(g64)
+    for k in range(batches):
+        rk = AdjointRenderer(gs, dataclasses.replace(cfg, spp=bspp, sample_offset=k * bspp))
+        gref += rk.backward(th0, None, dfix)[0].cpu().numpy() / batches
+    rep["vs_4096spp"] = {"rel_l2_err_64spp": float(np.linalg.norm(g64 - gref) / np.linalg.norm(gref)),
+                         "cosine_64spp": float(g64 @ gref / (np.linalg.norm(g64) * np.linalg.norm(gref)))}
+    # the plain tracer at 4096 spp along whole-atmosphere directions (linearised loss, sun disc excluded)
+    wcell = dfix.double().reshape(cfg.pixels, B).cpu().numpy()
+    wcell[_sun_pixel_mask(scene, cfg)] = 0.0
+    wt = torch.as_tensor(wcell.reshape(-1), device=dev, dtype=torch.float32)
+    dirs = {"rayleigh": (0.05, lambda g: g[0:3 * L:3].sum()), "mie": (0.05, lambda g: g[1:3 * L:3].sum()),
+            "ozone": (0.2, lambda g: g[2:3 * L:3].sum()), "albedo": (0.02, lambda g: g[3 * L]),
+            "g": (0.02, lambda g: g[3 * L + 1])}
+
+    def moved(direction, delta):
+        s = dataclasses.replace(scene)
+        bands, optics, phase = scene.bands.copy(), scene.aerosol_optics.copy(), scene.phase_values.copy()
+        sca = optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT].astype(np.float64)
+        ab = optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT].astype(np.float64)
+        if direction == "rayleigh":
+            bands["rayleigh_cross_section_m2"] *= np.float32(1 + delta)
+        elif direction == "mie":
+            optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT] = sca * (1 + delta)
+            optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT] = ab * (1 + delta)
+        elif direction == "ozone":
+            bands["ozone_cross_section_cm2"] *= np.float32(1 + delta)
+        elif direction == "albedo":
+            ext = sca + ab
+            optics["scattering_km_inv_per_g_m3"][0::SPECIES_COUNT] = ext * (sca / ext + delta)
+            optics["absorption_km_inv_per_g_m3"][0::SPECIES_COUNT] = ext * (1 - sca / ext - delta)
+        else:
+            phase[0] = hg_phase_values(g0 + delta, scene.phase_bins)[None, :]
+        s.bands, s.aerosol_optics, s.phase_values = bands, optics, phase
+        return s.bake_majorants(L)
+
+    wnp = wcell.reshape(-1)
+    plain = {}
+    for name, (delta, proj) in dirs.items():
+        gp, gm = GpuScene(moved(name, delta)), GpuScene(moved(name, -delta))
+        fd, adj = [], []
+        for k in range(batches):
+            c = dataclasses.replace(cfg, spp=bspp, sample_offset=k * bspp)
+            js = []
+            for g in (gp, gm):
+                sm = torch.zeros(cells, dtype=torch.float64, device=dev)
+                st = torch.zeros(1, dtype=torch.int32, device=dev)
+                g.render_device(c, {"cell_sum": sm.data_ptr(), "status": st.data_ptr()}, stream.cuda_stream)
+                torch.cuda.synchronize()
+                js.append(float(sm.cpu().numpy() @ wnp) / bspp)
+            fd.append((js[0] - js[1]) / (2 * delta))
+            rk = AdjointRenderer(gs, c)
+            adj.append(float(proj(rk.backward(th0, None, wt)[0].cpu().numpy())))
+        gp.close()
+        gm.close()
+        fd, adj = np.array(fd), np.array(adj)
+        se_fd, se_adj = fd.std(ddof=1) / math.sqrt(batches), adj.std(ddof=1) / math.sqrt(batches)
+        plain[name] = {"delta": delta, "plain_fd": float(fd.mean()), "plain_fd_se": float(se_fd),
+                       "adjoint": float(adj.mean()), "adjoint_se": float(se_adj),
+                       "z": float((adj.mean() - fd.mean()) / math.hypot(se_fd, se_adj))}
+    rep["vs_plain_tracer_4096spp"] = plain
+    gs.close()
+    return rep
+
+
+def run_adjoint(args):
+    import torch
+    torch.cuda.set_device(0)
+    clocks = ClockSampler(0)
+    clocks.start()
+    rep = adjoint_report(args, args.steps, args.warmup, checks=not args.no_adjoint_checks)
+    clocks.stop()
+    out = {"metric": "spectral path samples/s (chains/s), forward + path-replay backward",
+           "value": rep["step_chains_per_s"], "unit": "chains/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": rep["step_ms"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": ADJOINT_WORKLOAD, "width": 128, "height": 64, "wavelengths": 32, "spp": 64,
+                      "l2": "tables < 1 MB; compute-bound"},
+           "adjoint": rep, "clocks": clocks.summary(), "gpu_launches": 5 * args.steps}
+    print(json.dumps(out))
+
+
+def run_fit(args):
+    """Wavelength-primary fit driven by the adjoint against the same fit
+    driven by central differences of the plain tracer: final XYZ error of
+    each (plain-tracer evaluation at the target's sample count) and wall time."""
+    import torch
+    from sky_cuda.primaries import PrimaryFitConfig, evaluate, fit_adjoint, fit_finite_differences, target_xyz
+    torch.cuda.set_device(0)
+    cfg = PrimaryFitConfig(data_dir=str(DATA_DIR), iterations=args.fit_iterations)
+    t0 = time.perf_counter()
+    target, target_var = target_xyz(cfg)
+    t_target = time.perf_counter() - t0
+    clocks = ClockSampler(0)
+    clocks.start()
+    start = fit_adjoint(cfg, target, iterations=0)
+    adj = fit_adjoint(cfg, target)
+    fd = fit_finite_differences(cfg, target)
+    clocks.stop()
+    res = {}
+    for name, fit in (("initial", start), ("adjoint", adj), ("finite_differences", fd)):
+        ev = evaluate(cfg, fit["lambda_nm"], fit["matrix"], target, target_var)
+        res[name] = {"lambda_nm": [round(float(v), 3) for v in fit["lambda_nm"]],
+                     "matrix": fit["matrix"].cpu().numpy().round(6).tolist(),
+                     "relative_xyz_error": ev["relative_xyz_error"], "oklab": ev["oklab"],
+                     "relative_rms_error": ev["relative_rms_error"],
+                     "relative_rms_error_debiased": ev["relative_rms_error_debiased"],
+                     "relative_rms_noise": ev["relative_rms_noise"],
+                     "wall_s": fit["seconds"], "iterations": fit["iterations"],
+                     "loss_first": fit["loss"][0] if fit["loss"] else None,
+                     "loss_last": fit["loss"][-1] if fit["loss"] else None}
+    out = {"metric": "wavelength-primary fit: final relative RMS XYZ error, Monte Carlo noise removed "
+                     "(adjoint-driven)",
+           "value": res["adjoint"]["relative_rms_error_debiased"], "unit": "relative XYZ error", "n_gpus": 1,
+           "steps": cfg.iterations, "warmup": 0, "ms_per_step": adj["seconds"] / max(cfg.iterations, 1) * 1e3,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": FIT_WORKLOAD, "elevations": [round(float(e), 3) for e in cfg.elevations],
+                      "width": cfg.width, "height": cfg.height, "fit_spp": cfg.fit_spp,
+                      "target_wavelengths": cfg.target_wavelengths[2], "target_spp": cfg.target_spp,
+                      "primaries_init_nm": list(cfg.primaries_nm), "lr_nm": cfg.lr_nm, "fd_step_nm": cfg.fd_step_nm,
+                      "projection": "sky-view LUT"},
+           "target_render_s": t_target, "fit": res,
+           "speedup_wall_adjoint_vs_fd": fd["seconds"] / adj["seconds"] if adj["seconds"] else None,
+           "clocks": clocks.summary(), "gpu_launches": None}
+    print(json.dumps(out))
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == SWEEP_WORKLOAD:
         return run_sweep(args)
+    if args.workload == ADJOINT_WORKLOAD:
+        return run_adjoint(args)
+    if args.workload == FIT_WORKLOAD:
+        return run_fit(args)
     import torch
     import torch.distributed as dist
     from sky_cuda import GpuScene, render
@@ -436,6 +695,7 @@ def main():
         e2e_s = float(t.item())
 
     peak = measure_fp32_peak(torch, dev) if rank == 0 and not args.no_peak else None
+    adjoint = adjoint_report(args, 3, 2) if rank == 0 and world == 1 and not args.no_adjoint else None
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample = cpu_baseline_run(w, args, args.cpu_seconds)
@@ -464,6 +724,7 @@ def main():
                                         "has no FP32 figure)",
                          "flops_per_step": flops_per_step, "events_per_step": ev},
             "cpu_baseline": cpu,
+            "adjoint": adjoint,
             "clocks": clocks.summary(),
             "gpu_launches": (2 if cfg.kernel == 1 else 1) * args.steps,
         }

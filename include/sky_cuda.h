@@ -399,8 +399,9 @@ typedef struct SkyAdjointParams {
 /*
  * Gradient request.  dloss_dfilm [pixels][band_count] is dLoss/d(film value)
  * of the mean film the forward call wrote; the gradients are ADDED to
- * layer_grad [3 * majorant_layers + 2] and band_grad [band_count][4] (NULL to
- * skip).  status (required) and counters (optional) as in SkyDeviceOutputs.
+ * layer_grad [3 * majorant_layers + 2] and band_grad [band_count][4] (either
+ * may be NULL to skip it, not both).  status (required) and counters
+ * (optional) as in SkyDeviceOutputs.
  */
 typedef struct SkyAdjointGrads {
     const float* dloss_dfilm;
@@ -448,7 +449,7 @@ int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* param
  * scene once at start-up, owns every output buffer, and renders through this
  * call, which calls no cudaMalloc, cudaFree or allocating library routine.
  *
- * configs[i] / outputs[i] describe job i exactly as in
+ * job_configs[i] / outputs[i] describe job i exactly as in
  * sky_cuda_render_device(); every job must use the same tracking mode and
  * phase sampling.  outputs[0].status is required and receives the watchdog
  * bits of the whole batch (OR-ed in; the caller clears it); outputs[0].counters
@@ -465,7 +466,7 @@ int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* param
  */
 #define SKY_NOALLOC_MAX_JOBS 16u
 #define SKY_NOALLOC_SCRATCH_BYTES 16384u
-int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* configs,
+int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* job_configs,
                                   const SkyDeviceOutputs* outputs, uint32_t job_count, void* cuda_stream);
 
 #ifdef __cplusplus

@@ -141,28 +141,30 @@ __device__ __forceinline__ float vertex_phase(const AdjSet& X, uint32_t bins, co
     return m.R * rayleigh_phase(mu) + (m.Ms > 0.0f ? m.Ms * hg_value(X, bins, mu) : 0.0f);
 }
 
-// Gradient accumulator of one lane: layer parameters in shared memory, the
-// multipliers of the lane's band in registers.
+// Gradient accumulator of one lane: per-layer scales in the warp's copy of
+// the layer gradient in shared memory; the Mie albedo and g, and the
+// multipliers of the lane's band, in registers.
 struct AdjAcc {
     float* sg;  // [3 L + 2]
     uint32_t L;
-    float gR, gM, gO;
+    float gR, gM, gO;  // band multipliers
+    float gW, gG;      // Mie albedo, Mie g
 };
 
 // d sigma_t terms of a null collision, times c (= -weight / sigma_n).
 __device__ __forceinline__ void null_terms(AdjAcc& a, const AdjSet& X, const AdjBase& b, float c) {
     const float* p = X.layer + 3 * b.layer;
-    float* g = a.sg + 3 * b.layer;
+    float* g = a.sg ? a.sg + 3 * b.layer : nullptr;  // null: band gradients only
     if (b.uR > 0.0f) {
-        atomicAdd(g, c * X.kR * b.uR);
+        if (g) atomicAdd(g, c * X.kR * b.uR);
         a.gR = fmaf(c * __ldg(p), b.uR, a.gR);
     }
     if (b.uM > 0.0f) {
-        atomicAdd(g + 1, c * X.kM * b.uM);
+        if (g) atomicAdd(g + 1, c * X.kM * b.uM);
         a.gM = fmaf(c * __ldg(p + 1), b.uM, a.gM);
     }
     if (b.uO > 0.0f) {
-        atomicAdd(g + 2, c * X.kO * b.uO);
+        if (g) atomicAdd(g + 2, c * X.kO * b.uO);
         a.gO = fmaf(c * __ldg(p + 2), b.uO, a.gO);
     }
 }
@@ -183,27 +185,27 @@ __device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_
     if (!(sum > 0.0f)) return;
     const float w = weight / sum;
     const float* p = X.layer + 3 * b.layer;
-    float* g = a.sg + 3 * b.layer;
+    float* g = a.sg ? a.sg + 3 * b.layer : nullptr;
     if (b.uR > 0.0f) {
-        atomicAdd(g, w * X.kR * b.uR * pr);
+        if (g) atomicAdd(g, w * X.kR * b.uR * pr);
         a.gR = fmaf(w * __ldg(p), b.uR * pr, a.gR);
     }
     if (b.uM > 0.0f) {
-        atomicAdd(g + 1, w * X.omega * X.kM * b.uM * pm);
-        atomicAdd(a.sg + 3 * a.L, w * m.M * pm);
-        atomicAdd(a.sg + 3 * a.L + 1, w * m.Ms * dpm);
+        if (g) atomicAdd(g + 1, w * X.omega * X.kM * b.uM * pm);
+        a.gW = fmaf(w * m.M, pm, a.gW);
+        a.gG = fmaf(w * m.Ms, dpm, a.gG);
         a.gM = fmaf(w * X.omega * __ldg(p + 1), b.uM * pm, a.gM);
     }
 }
 
 // Residual-carry delta tracking over Q's tracking grid (track_ray_merged of
 // the plain tracer with the parameterised medium).  w_eval collects the
-// null-collision ratios of P over Q; with kGrad every null collision adds
-// gw * d log(mu_bar - sigma_t).
-template <bool kGrad>
-__device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band, const RayGeo& g,
-                          float t_max, Rng& rng, float& t_hit, AdjBase& hit, float& w_eval, float gw, AdjAcc& acc,
-                          Counters& n, bool& watchdog) {
+// null-collision ratios of P over Q; with gw != 0 and the null-collision
+// estimator every null collision adds gw * d log(mu_bar - sigma_t).
+__device__ __forceinline__ bool adj_track_body(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
+                                               const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
+                                               float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
+                                               bool& watchdog) {
     const DevScene& S = A.S;
     const uint32_t L = S.layer_count;
     MergedGrid G;
@@ -211,7 +213,8 @@ __device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uin
     G.maj = A.G.maj + band * (L + 1u);
     G.map = A.G.map + band * L;
     G.count = int(__ldg(A.G.count + band));
-    float t = 0.0f;
+    float t = 0.0f, t_piece = 0.0f;
+    tau_bar = 0.0f;  // majorant optical depth of the traversed part
     int m = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_max), S.ground_radius));
     int dir;
     float t_seg = merged_crossing(G, g, m, t, t_max, dir);
@@ -229,14 +232,16 @@ __device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uin
             if (rng.next() * maj < mq.t) {
                 t_hit = t;
                 hit = b;
+                tau_bar += (t - t_piece) * maj;
                 return true;
             }
             const float sn = maj - mq.t;
             if (A.distinct && sn > 0.0f) w_eval *= (maj - adj_med(P, b).t) / sn;
-            if (kGrad && A.estimator == SKY_ADJOINT_NULL_COLLISIONS && gw != 0.0f && sn > 0.0f)
+            if (A.estimator == SKY_ADJOINT_NULL_COLLISIONS && gw != 0.0f && sn > 0.0f)
                 null_terms(acc, Q, b, -gw / sn);
             tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
         } else {
+            tau_bar += (t_seg - t_piece) * maj;
             if (dir == 0) return false;
             if (++guard > 100000u) {
                 watchdog = true;
@@ -244,6 +249,7 @@ __device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uin
             }
             tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
             t = t_seg;
+            t_piece = t_seg;
             m += dir;
             t_seg = merged_crossing(G, g, m, t, t_max, dir);
             maj = __ldg(G.maj + m);
@@ -252,18 +258,39 @@ __device__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uin
     }
 }
 
+// The adjoint kernel calls the tracker through one out-of-line copy (four
+// call sites, two passes: a smaller instruction footprint); the primal
+// kernel inlines it.
+__device__ __noinline__ bool adj_track_shared(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
+                                              const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
+                                              float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
+                                              bool& watchdog) {
+    return adj_track_body(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
+}
+
+template <bool kShared>
+__device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
+                                          const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
+                                          float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
+                                          bool& watchdog) {
+    if (kShared)
+        return adj_track_shared(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
+    return adj_track_body(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
+}
+
 // Estimate of -integral d(sigma_t) over [0, t_end] of a ray, times weight:
 // N points stratified in the majorant optical depth of Q's tracking grid
-// (density mu_bar / tau_bar along the ray), each adding
-// -weight (tau_bar / N) d(sigma_t) / mu_bar.  N grows with tau_bar.  The
+// (density mu_bar / tau_bar along the ray; tau_bar as the tracker summed
+// it), each adding -weight (tau_bar / N) d(sigma_t) / mu_bar.  N grows with
+// tau_bar.  The
 // points' random numbers come from a stream of their own (another pcg4d
 // key, 16 draws per position of the path's stream), so the path's own
 // draws are untouched.
-constexpr int kMaxSegmentPoints = 8;
+constexpr int kMaxSegmentPoints = 4;
 
-__device__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, const RayGeo& g, float t_end,
-                              float weight, const Rng& rng, AdjAcc& acc) {
-    if (weight == 0.0f || !(t_end > 0.0f)) return;
+__device__ __noinline__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, const RayGeo& g,
+                                           float t_end, float tau, float weight, const Rng& rng, AdjAcc& acc) {
+    if (weight == 0.0f || !(t_end > 0.0f) || !(tau > 0.0f)) return;
     const DevScene& S = A.S;
     const uint32_t L = S.layer_count;
     MergedGrid G;
@@ -273,17 +300,9 @@ __device__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, c
     G.count = int(__ldg(A.G.count + band));
     const int m0 = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_end), S.ground_radius));
     const int guard_max = 2 * G.count + 4;
-    float tau = 0.0f, t = 0.0f;
+    float t = 0.0f;
     int m = m0, dir = 0;
-    for (int guard = 0; guard < guard_max; ++guard) {
-        const float t_seg = merged_crossing(G, g, m, t, t_end, dir);
-        tau += (t_seg - t) * __ldg(G.maj + m);
-        if (dir == 0) break;
-        t = t_seg;
-        m += dir;
-    }
-    if (!(tau > 0.0f)) return;
-    const int n = min(kMaxSegmentPoints, 1 + int(2.0f * tau));
+    const int n = min(kMaxSegmentPoints, 1 + int(tau));
     const float step = tau / float(n);
     Rng r2 = rng;  // 16 draws of its own per position of the path's stream
     r2.k2 ^= 0x68E31DA4u;
@@ -336,10 +355,12 @@ __device__ __forceinline__ float hg_sampling_pdf(const AdjSet& X, uint32_t bins,
 
 // Shadow ray of an NEE sample: the P/Q weight of a ray that reaches the sun,
 // 0 when it hits the ground, leaves through no sun or collides.  dim0 is the
-// random-number index at which its tracking started.
+// random-number index at which its tracking started, tau_bar its majorant
+// optical depth.
+template <bool kShared>
 __device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band, V3 pos,
                                             V3 ldir, Rng& rng, AdjAcc& acc, Counters& n, bool& watchdog,
-                                            uint32_t& dim0) {
+                                            uint32_t& dim0, float& tau_bar) {
     const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
     float st;
     uint32_t sk;
@@ -348,39 +369,40 @@ __device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, co
     dim0 = rng.dim;
     float th, w = 1.0f;
     AdjBase bh;
-    if (adj_track<false>(A, P, Q, band, sg, st, rng, th, bh, w, 0.0f, acc, n, watchdog)) return 0.0f;
+    if (adj_track<kShared>(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
     return w;
 }
 
 // Gradient terms of an unblocked shadow ray: its segment integral, or (null
 // collisions) the same ray traced again from dim0 for its null collisions.
 __device__ __forceinline__ void adj_shadow_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, V3 pos, V3 ldir,
-                                                 Rng& rng, uint32_t dim0, float weight, AdjAcc& acc, Counters& n,
-                                                 bool& watchdog) {
+                                                 Rng& rng, uint32_t dim0, float tau_bar, float weight, AdjAcc& acc,
+                                                 Counters& n, bool& watchdog) {
     if (weight == 0.0f) return;
     const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
     float st;
     uint32_t sk;
     next_boundary(A.S, sg, st, sk);
     if (A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
-        segment_terms(A, Q, band, sg, st, weight, rng, acc);
+        segment_terms(A, Q, band, sg, st, tau_bar, weight, rng, acc);
         return;
     }
     const uint32_t dim1 = rng.dim;
     rng.dim = dim0;
-    float th, w = 1.0f;
+    float th, w = 1.0f, tb;
     AdjBase bh;
-    adj_track<true>(A, Q, Q, band, sg, st, rng, th, bh, w, weight, acc, n, watchdog);
+    adj_track<true>(A, Q, Q, band, sg, st, rng, th, bh, w, tb, weight, acc, n, watchdog);
     rng.dim = dim1;
 }
 
 // One chain of the parameterised medium (trace_path, sky_trace.wgsl:703-776)
-// at unit solar multiplier.  kGrad replays a chain whose radiance `total`
-// pass 1 returned and accumulates w * dL/dparams.
-template <int kPhase, bool kGrad>
-__device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, const DevLaunch& L, uint32_t x,
-                           uint32_t y, uint32_t band, uint32_t sample, float w, float total, AdjAcc& acc,
-                           Counters& n, bool& watchdog) {
+// at unit solar multiplier.  With `grad` it replays a chain whose radiance
+// `total` the first pass returned and accumulates w * dL/dparams (a run-time
+// flag, so that both passes share one copy of the code).
+template <int kPhase, bool kShared>
+__device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, const DevLaunch& L,
+                                           uint32_t x, uint32_t y, uint32_t band, uint32_t sample, bool grad,
+                                           float w, float total, AdjAcc& acc, Counters& n, bool& watchdog) {
     const DevScene& S = A.S;
     const uint32_t bins = S.phase_bins;
     Rng rng;
@@ -405,13 +427,15 @@ __device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, co
         if (!next_boundary(S, g, t_b, kind)) break;
         float t_hit, w_eval = 1.0f;
         AdjBase hb;
-        const float gw = kGrad ? w * (total - rad) : 0.0f;
+        const float gw = grad ? w * (total - rad) : 0.0f;
         const uint32_t dim_seg = rng.dim;
-        const bool hit = adj_track<kGrad>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, gw, acc, n, watchdog);
-        if (kGrad && A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
+        float tau_bar;
+        const bool hit =
+            adj_track<kShared>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, gw, acc, n, watchdog);
+        if (grad && A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
             Rng at = rng;
             at.dim = dim_seg;
-            segment_terms(A, Q, band, g, hit ? t_hit : t_b, gw, at, acc);
+            segment_terms(A, Q, band, g, hit ? t_hit : t_b, tau_bar, gw, at, acc);
         }
         thr *= w_eval;
         if (hit) {
@@ -429,16 +453,18 @@ __device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, co
                 const V3 ldir = sample_sun_cone(S, rng);
                 ++n.e[SKY_EVENT_NEE];
                 uint32_t dim0 = 0;
-                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0);
+                float tau_s = 0.0f;
+                const float trans =
+                    adj_shadow<kShared>(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0, tau_s);
                 if (!(trans != 0.0f)) continue;
                 const float mu = dot3(dir, ldir);
                 const float ph = mp.s > 0.0f ? vertex_phase(P, bins, mp, mu) / mp.s : 0.0f;
                 const float term = l_sun * trans * ph / S.light_pdf;
                 nee += term;
-                if (kGrad) {
+                if (grad) {
                     const float c = w * thr * term * inv_lights;
                     vertex_terms(acc, Q, bins, hb, mq, mu, c);
-                    adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, c, acc, n, watchdog);
+                    adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, tau_s, c, acc, n, watchdog);
                 }
             }
             rad += thr * (nee * inv_lights);
@@ -464,7 +490,7 @@ __device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, co
             }
             thr_q *= fq;
             thr = A.distinct ? thr * fp : thr_q;
-            if (kGrad) vertex_terms(acc, Q, bins, hb, mq, mu_c, w * (total - rad));
+            if (grad) vertex_terms(acc, Q, bins, hb, mq, mu_c, w * (total - rad));
             if (depth >= L.rr_start_depth) {  // russian_roulette (sky_trace.wgsl:691-701)
                 const float q = fminf(fmaxf(thr_q, 0.05f), 0.95f);
                 if (rng.next() > q) break;
@@ -488,11 +514,13 @@ __device__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, co
                 const float cos_sun = fmaxf(dot3(normal, ldir), 0.0f);
                 if (!(cos_sun > 0.0f)) continue;
                 uint32_t dim0 = 0;
-                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0);
+                float tau_s = 0.0f;
+                const float trans =
+                    adj_shadow<kShared>(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0, tau_s);
                 if (!(trans != 0.0f)) continue;
                 const float term = S.ground_albedo * kInvPi * l_sun * trans * cos_sun / S.light_pdf;
                 ground += term;
-                if (kGrad) adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, w * thr * term * inv_lights, acc, n,
+                if (grad) adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, tau_s, w * thr * term * inv_lights, acc, n,
                                              watchdog);
             }
             rad += thr * (ground * inv_lights);
@@ -545,7 +573,8 @@ __device__ __forceinline__ void flush_counters(const Counters& n, unsigned long 
 // Primal: one warp per (pixel, band) cell, 32 samples per round, FP64 cell
 // sums in a fixed order (as the plain tracer).
 template <int kPhase>
-__global__ void __launch_bounds__(256) adjoint_primal_kernel(AdjCtx A, DevLaunch L, double* __restrict__ cell_sum,
+__global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_constant__ AdjCtx A,
+                                                             const __grid_constant__ DevLaunch L, double* __restrict__ cell_sum,
                                                              double* __restrict__ cell_sumsq, uint32_t accumulate,
                                                              unsigned long long* __restrict__ counters,
                                                              uint32_t* __restrict__ status, uint64_t cells) {
@@ -557,7 +586,7 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(AdjCtx A, DevLaunch
     const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
     const AdjSet P = resolve(A.P, A.S.layer_count, band);
     const AdjSet Q = A.distinct ? resolve(A.Q, A.S.layer_count, band) : P;
-    AdjAcc acc{nullptr, 0u, 0.0f, 0.0f, 0.0f};
+    AdjAcc acc{nullptr, 0u, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     Counters n;
     n.clear();
     bool watchdog = false;
@@ -570,8 +599,8 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(AdjCtx A, DevLaunch
         const uint32_t s = base + lane;
         float r = 0.0f;
         if (s < L.spp)
-            r = P.kS * adj_chain<kPhase, false>(A, P, Q, L, x, y, band, L.sample_offset + s, 0.0f, 0.0f, acc, n,
-                                                 watchdog);
+            r = P.kS * adj_chain<kPhase, false>(A, P, Q, L, x, y, band, L.sample_offset + s, false, 0.0f, 0.0f, acc, n,
+                                         watchdog);
         const double rd = double(r);
         sum += warp_sum_d(rd);
         sumsq += warp_sum_d(rd * rd);
@@ -584,30 +613,38 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(AdjCtx A, DevLaunch
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
 }
 
-// Adjoint: warps stride over the cells; each chain is traced (pass 1) and
-// replayed (pass 2).  Layer gradients gather in shared memory (FP32), band
-// gradients per warp, and each block adds its totals to the FP64 outputs
-// once at the end.
+// Adjoint: warps take cells one at a time; each chain is traced (pass 1) and
+// replayed (pass 2).  Layer gradients gather in shared memory (FP32, one copy
+// per warp when they fit, so that only a warp's own lanes contend), the
+// albedo, g and band gradients in registers reduced per cell; each block adds
+// its totals to the FP64 outputs once at the end.
 template <int kPhase>
-__global__ void __launch_bounds__(256) adjoint_grad_kernel(AdjCtx A, DevLaunch L, const float* __restrict__ dloss,
+__global__ void __launch_bounds__(256) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
+                                                           const __grid_constant__ DevLaunch L,
+                                                           const float* __restrict__ dloss,
                                                            double* __restrict__ layer_grad,
                                                            double* __restrict__ band_grad,
                                                            unsigned long long* __restrict__ counters,
-                                                           uint32_t* __restrict__ status, uint64_t cells) {
+                                                           uint32_t* __restrict__ status, uint64_t cells,
+                                                           uint32_t copies, uint32_t* __restrict__ next_cell) {
     extern __shared__ float smem[];
     const uint32_t Lc = A.S.layer_count, B = A.S.band_count;
     const uint32_t nlayer = 3u * Lc + 2u;
-    float* sg = smem;
-    float* sb = smem + nlayer;
-    for (uint32_t i = threadIdx.x; i < nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
+    const uint32_t warp = threadIdx.x >> 5;
+    float* sg = layer_grad ? smem + (warp % copies) * nlayer : nullptr;
+    float* sb = smem + copies * nlayer;
+    for (uint32_t i = threadIdx.x; i < copies * nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t warps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
     Counters n;
     n.clear();
     bool watchdog = false;
     const float inv_spp = 1.0f / float(L.spp);
-    for (uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; cell < cells; cell += warps) {
+    for (;;) {  // warps take cells from a shared counter: no tail of unequal fixed shares
+        uint32_t next = 0;
+        if (lane == 0) next = atomicAdd(next_cell, 1u);
+        const uint64_t cell = __shfl_sync(0xffffffffu, next, 0);
+        if (cell >= cells) break;
         const float wcell = __ldg(dloss + cell) * inv_spp;
         if (wcell == 0.0f) continue;  // uniform across the warp
         const uint32_t band = uint32_t(cell % L.band_count);
@@ -615,31 +652,46 @@ __global__ void __launch_bounds__(256) adjoint_grad_kernel(AdjCtx A, DevLaunch L
         const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
         const AdjSet P = resolve(A.P, Lc, band);
         const float w = wcell * P.kS;
-        AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f};
+        AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         float gS = 0.0f;
         for (uint32_t base = 0; base < L.spp; base += 32u) {
             const uint32_t s = base + lane;
             if (s >= L.spp) continue;
-            const float total = adj_chain<kPhase, false>(A, P, P, L, x, y, band, L.sample_offset + s, 0.0f, 0.0f,
-                                                         acc, n, watchdog);
-            gS = fmaf(wcell, total, gS);
-            if (total > 0.0f)
-                adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, w, total, acc, n, watchdog);
+            // pass 0 traces the chain, pass 1 replays it: one call site, so
+            // lanes in different passes run the same instructions
+            float total = 0.0f;
+            for (int pass = 0; pass < 2; ++pass) {
+                const float r = adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, pass == 1, w, total,
+                                                  acc, n, watchdog);
+                if (pass == 0) {
+                    total = r;
+                    gS = fmaf(wcell, total, gS);
+                    if (!(total > 0.0f)) break;
+                }
+            }
         }
         const float r = warp_sum_f(acc.gR), m = warp_sum_f(acc.gM), o = warp_sum_f(acc.gO), s = warp_sum_f(gS);
+        const float gw = warp_sum_f(acc.gW), gg = warp_sum_f(acc.gG);
         if (lane == 0) {
             float* b = sb + band * kAdjBandParams;
             atomicAdd(b, r);
             atomicAdd(b + 1, m);
             atomicAdd(b + 2, o);
             atomicAdd(b + 3, s);
+            if (sg) {
+                atomicAdd(sg + 3u * Lc, gw);
+                atomicAdd(sg + 3u * Lc + 1u, gg);
+            }
         }
     }
     flush_counters(n, counters, lane);
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nlayer; i += blockDim.x)
-        if (sg[i] != 0.0f) atomicAdd(layer_grad + i, double(sg[i]));
+    for (uint32_t i = threadIdx.x; layer_grad && i < nlayer; i += blockDim.x) {
+        float v = 0.0f;
+        for (uint32_t c = 0; c < copies; ++c) v += smem[c * nlayer + i];
+        if (v != 0.0f) atomicAdd(layer_grad + i, double(v));
+    }
     if (band_grad)
         for (uint32_t i = threadIdx.x; i < kAdjBandParams * B; i += blockDim.x)
             if (sb[i] != 0.0f) atomicAdd(band_grad + i, double(sb[i]));
@@ -786,7 +838,7 @@ size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 size_t adjoint_workspace_bytes(uint32_t B, uint32_t L, uint32_t bins) {
     return 2 * align256(4 * size_t(bins) * sizeof(float)) + align256(size_t(B) * L * sizeof(float)) +
            2 * align256(size_t(B) * (L + 1) * sizeof(float)) + align256(size_t(B) * L * sizeof(uint16_t)) +
-           align256(size_t(B) * sizeof(uint32_t));
+           align256(size_t(B) * sizeof(uint32_t)) + align256(sizeof(uint32_t));
 }
 
 AdjWorkspace adjoint_workspace(void* base, uint32_t B, uint32_t L, uint32_t bins) {
@@ -805,6 +857,8 @@ AdjWorkspace adjoint_workspace(void* base, uint32_t B, uint32_t L, uint32_t bins
     W.map = reinterpret_cast<uint16_t*>(p);
     p += align256(size_t(B) * L * sizeof(uint16_t));
     W.count = reinterpret_cast<uint32_t*>(p);
+    p += align256(size_t(B) * sizeof(uint32_t));
+    W.next_cell = reinterpret_cast<uint32_t*>(p);
     return W;
 }
 
@@ -835,21 +889,27 @@ cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* c
 
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
-                                cudaStream_t stream) {
+                                uint32_t* next_cell, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
-    const size_t smem =
-        (size_t(3u * A.S.layer_count + 2u) + size_t(kAdjBandParams) * A.S.band_count) * sizeof(float);
+    const size_t nlayer = size_t(3u * A.S.layer_count + 2u), nband = size_t(kAdjBandParams) * A.S.band_count;
+    // one layer-gradient copy per warp while it stays within the default 48 KB
+    const uint32_t copies = (8 * nlayer + nband) * sizeof(float) <= 48u * 1024u ? 8u : 1u;
+    const size_t smem = (copies * nlayer + nband) * sizeof(float);
     const uint64_t want = (cells * 32u + 255u) / 256u;
     if (L.phase_sampling == SKY_PHASE_TABULATED) {
         const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_TABULATED>
-            <<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad, band_grad, counters, status, cells);
+        adjoint_grad_kernel<SKY_PHASE_TABULATED><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
+                                                                                band_grad, counters, status, cells,
+                                                                                copies, next_cell);
     } else {
         const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>
-            <<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad, band_grad, counters, status, cells);
+        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
+                                                                                band_grad, counters, status, cells,
+                                                                                copies, next_cell);
     }
     return cudaGetLastError();
 }

@@ -61,6 +61,7 @@ struct AdjWorkspace {
     float* maj;
     uint16_t* map;
     uint32_t* count;
+    uint32_t* next_cell;  // work counter of the adjoint kernel
 };
 
 // Scene workspace layout for a scene of B bands, L layers and `bins` phase bins.
@@ -80,6 +81,6 @@ cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* c
 // and band_grad [B][4] (may be null) given dLoss/dfilm [pixels][B].
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
-                                cudaStream_t stream);
+                                uint32_t* next_cell, cudaStream_t stream);
 
 }  // namespace sky

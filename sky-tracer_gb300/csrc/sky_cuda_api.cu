@@ -891,14 +891,15 @@ extern "C" int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderC
     int st = adjoint_setup(s, params, A, W);
     if (st) return st;
     if ((st = adjoint_config(s, config, A, L))) return st;
-    if (!grads || !grads->dloss_dfilm || !grads->layer_grad)
-        return set_error(SKY_ERR_INVALID_CONFIG, "grads.dloss_dfilm and grads.layer_grad are required");
+    if (!grads || !grads->dloss_dfilm || (!grads->layer_grad && !grads->band_grad))
+        return set_error(SKY_ERR_INVALID_CONFIG,
+                         "grads.dloss_dfilm and at least one of grads.layer_grad, grads.band_grad are required");
     if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = launch_adjoint_grad(A, L, grads->dloss_dfilm, grads->layer_grad, grads->band_grad, grads->counters,
-                            grads->status, stream);
+                            grads->status, W.next_cell, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);
     return SKY_OK;
 }
@@ -964,10 +965,10 @@ int noalloc_scratch(int device, void** out) {
 
 }  // namespace
 
-extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* configs,
+extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRenderConfig* job_configs,
                                              const SkyDeviceOutputs* outputs, uint32_t job_count,
                                              void* cuda_stream) {
-    if (!scene || !configs || !outputs) return set_error(SKY_ERR_INVALID_CONFIG, "scene, configs and outputs are required");
+    if (!scene || !job_configs || !outputs) return set_error(SKY_ERR_INVALID_CONFIG, "scene, job_configs and outputs are required");
     if (job_count == 0) return set_error(SKY_ERR_INVALID_CONFIG, "job_count must be at least 1");
     if (job_count > SKY_NOALLOC_MAX_JOBS)
         return set_error(SKY_ERR_INVALID_CONFIG, "job_count " + std::to_string(job_count) +
@@ -980,10 +981,10 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
     std::memset(&image, 0, sizeof(image));
     uint32_t groups = 0;
     for (uint32_t i = 0; i < job_count; ++i) {
-        const SkyRenderConfig* c = &configs[i];
+        const SkyRenderConfig* c = &job_configs[i];
         int st = validate_config(s, c);
         if (st) return st;
-        if (c->tracking != configs[0].tracking || c->phase_sampling != configs[0].phase_sampling)
+        if (c->tracking != job_configs[0].tracking || c->phase_sampling != job_configs[0].phase_sampling)
             return set_error(SKY_ERR_INVALID_CONFIG, "all jobs of a batch need the same tracking and phase sampling");
         if (!outputs[i].cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[i].cell_sum is required");
         const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
@@ -1020,13 +1021,13 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
     w.jobs = static_cast<const DevJob*>(scratch);
     w.num_jobs = job_count;
     w.total_groups = groups;
-    w.tracking = configs[0].tracking;
-    w.phase_sampling = configs[0].phase_sampling;
+    w.tracking = job_configs[0].tracking;
+    w.phase_sampling = job_configs[0].phase_sampling;
     w.work_counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
                                                  offsetof(NoAllocScratch, work_counter));
     w.counters = outputs[0].counters;
     w.status = outputs[0].status;
-    const bool with_maj = configs[0].tracking != SKY_TRACKING_MERGED_LAYERS;
+    const bool with_maj = job_configs[0].tracking != SKY_TRACKING_MERGED_LAYERS;
     w.variant = s->tuning.pool_variant;
     w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
     if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);

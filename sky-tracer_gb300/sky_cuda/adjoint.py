@@ -32,6 +32,7 @@ BAND_PARAMS = _abi.ADJOINT_BAND_PARAMS
 PARAMS_PER_LAYER = 3  # Rayleigh, Mie, ozone density scales
 SEGMENT_INTEGRALS = _abi.ADJOINT_SEGMENT_INTEGRALS  # default backward estimator (lower variance)
 NULL_COLLISIONS = _abi.ADJOINT_NULL_COLLISIONS      # exact derivative of the forward estimator
+DECORRELATE_SEED = 0x9E3779B97F4A7C15  # xor-ed into the seed of a decorrelated backward pass
 
 
 def mie_albedo(scene: Scene) -> float:
@@ -132,22 +133,31 @@ class AdjointRenderer:
             self._check_status()
         return out
 
-    def backward(self, layer, band, dloss_dfilm, *, sun=None, check_status: bool = True):
-        """(dLoss/dlayer_params, dLoss/dband_params or None) as float64 tensors."""
+    def backward(self, layer, band, dloss_dfilm, *, sun=None, check_status: bool = True, decorrelate: bool = False,
+                 layer_grad: bool = True):
+        """(dLoss/dlayer_params or None, dLoss/dband_params or None) as float64
+        tensors.  decorrelate=True replays chains of another seed than the
+        forward's; layer_grad=False skips the layer gradient (band only)."""
         import torch
         d = dloss_dfilm.reshape(-1).to(torch.float32).contiguous()
         if d.numel() != self.pixels * self.bands:
             raise ValueError("dloss_dfilm must hold pixels * bands values")
-        lg = torch.zeros(self.param_count, dtype=torch.float64, device="cuda")
+        if not layer_grad and band is None:
+            raise ValueError("nothing to differentiate: layer_grad=False and no band parameters")
+        lg = torch.zeros(self.param_count, dtype=torch.float64, device="cuda") if layer_grad else None
         bg = torch.zeros(self.bands * BAND_PARAMS, dtype=torch.float64, device="cuda") if band is not None else None
         g = SkyAdjointGrads()
         g.dloss_dfilm = d.data_ptr()
-        g.layer_grad = lg.data_ptr()
+        g.layer_grad = _ptr(lg)
         g.band_grad = _ptr(bg)
         g.status = self._status.data_ptr()
         p = self._params(layer, band, None, None, sun)
         stream = torch.cuda.current_stream().cuda_stream
-        check(self.lib.sky_cuda_adjoint_backward(self.gs.handle, ctypes.byref(self._c_config), ctypes.byref(p),
+        c = self._c_config
+        if decorrelate:
+            c = self.config.to_c()
+            c.seed = self.config.seed ^ DECORRELATE_SEED
+        check(self.lib.sky_cuda_adjoint_backward(self.gs.handle, ctypes.byref(c), ctypes.byref(p),
                                                  ctypes.byref(g), ctypes.c_void_p(stream)), self.lib)
         if check_status:
             self._check_status()
@@ -171,12 +181,13 @@ def _autograd_function():
         """film = render(layer_params, band_params); backward runs the adjoint kernel."""
 
         @staticmethod
-        def forward(ctx, layer, band, renderer, sun):
+        def forward(ctx, layer, band, renderer, sun, decorrelate):
             layer_c = layer.detach().contiguous()
             band_c = band.detach().contiguous() if band is not None else None
             out = renderer.forward(layer_c, band_c, sun=sun)
             ctx.renderer = renderer
             ctx.sun = sun
+            ctx.decorrelate = decorrelate
             ctx.has_band = band is not None
             ctx.save_for_backward(layer_c, band_c if band_c is not None else layer_c)
             cfg = renderer.config
@@ -186,8 +197,12 @@ def _autograd_function():
         def backward(ctx, grad_film):
             layer_c, band_c = ctx.saved_tensors
             band_c = band_c if ctx.has_band else None
-            lg, bg = ctx.renderer.backward(layer_c, band_c, grad_film.contiguous(), sun=ctx.sun)
-            return lg.to(layer_c.dtype), (bg.to(band_c.dtype) if bg is not None else None), None, None
+            want_layer = ctx.needs_input_grad[0] or band_c is None
+            lg, bg = ctx.renderer.backward(layer_c, band_c, grad_film.contiguous(), sun=ctx.sun,
+                                           decorrelate=ctx.decorrelate, layer_grad=want_layer)
+            gl = lg.to(layer_c.dtype).reshape(layer_c.shape) if lg is not None else None
+            gb = bg.to(band_c.dtype).reshape(band_c.shape) if bg is not None else None
+            return gl, gb, None, None, None
 
     return SkyRenderFunction
 
@@ -195,12 +210,17 @@ def _autograd_function():
 _FUNCTION = None
 
 
-def render_film(renderer: AdjointRenderer, layer, band=None, sun=None):
-    """Differentiable film [H, W, B] (float32) of the renderer's config."""
+def render_film(renderer: AdjointRenderer, layer, band=None, sun=None, decorrelate: bool = False):
+    """Differentiable film [H, W, B] (float32) of the renderer's config.
+
+    With decorrelate=True the backward pass traces its own samples (another
+    seed) instead of replaying the forward's: the gradient of a loss that is
+    nonlinear in the film (e.g. L2) is then free of the correlation between
+    the film's noise and its derivative's noise."""
     global _FUNCTION
     if _FUNCTION is None:
         _FUNCTION = _autograd_function()
-    return _FUNCTION.apply(layer, band, renderer, sun)
+    return _FUNCTION.apply(layer, band, renderer, sun, decorrelate)
 
 
 def film_to_xyz(film, scene: Scene):

@@ -1,0 +1,348 @@
+"""Wavelength-primary fitting through the differentiable renderer.
+
+K primary wavelengths and a K x 3 matrix M rebuild the CIE XYZ of
+full-spectrum sky renders from K-band renders: XYZ ~ sum_k L(lambda_k) M[k].
+The reference picks its primaries by a discrete search over baked band
+images, scoring each combination by the Oklab distance of its XYZ
+reconstruction (sky-wavelength-optimizer/src/main.rs:414-488, 1121-1137).
+Here the wavelengths are continuous and fitted by Adam together with M.
+
+A band at wavelength lambda is the scene's band at lambda0 with its Rayleigh
+cross section, ozone cross section and solar radiance multiplied by their
+ratios at lambda and lambda0: lambda^-4 for Rayleigh (medium.rs:104-106) and
+piecewise-linear lerps of bands.csv for ozone and the sun (as the scene
+builder tabulates them).  A change of lambda therefore needs no new scene;
+the adjoint returns dLoss/d(band multipliers) and torch carries it through
+those formulas to dLoss/dlambda (analytic lambda^-4, piecewise-linear table
+slopes).  The Mie extinction and phase of the benchmark atmosphere do not
+depend on wavelength.
+
+fit_adjoint() drives the fit with adjoint gradients; fit_finite_differences()
+is the same fit driven by central differences of the plain tracer, which
+needs new scenes at lambda +- h for every step.
+"""
+
+from __future__ import annotations
+
+import dataclasses
+import math
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+from .adjoint import AdjointRenderer, initial_layer_params, render_film
+from .render import GpuScene, RenderConfig
+from .scene import SyntheticAtmosphere, load_bands, sun_from_degrees, synthetic_scene, wavelengths
+from .sweep import elevation_schedule
+
+RAYLEIGH_REF_NM = 550.0  # medium.rs:104-106: 5.8e-31 (550 / lambda)^4 m^2
+
+
+def _interp(x_tab, y_tab, x):
+    """np.interp in torch (clamped ends), differentiable in x."""
+    import torch
+    i = torch.searchsorted(x_tab, x.detach()).clamp(1, x_tab.numel() - 1)
+    x0, x1 = x_tab[i - 1], x_tab[i]
+    y0, y1 = y_tab[i - 1], y_tab[i]
+    t = ((x - x0) / (x1 - x0)).clamp(0.0, 1.0)
+    return y0 + t * (y1 - y0)
+
+
+class BandModel:
+    """Wavelength-dependent band quantities of the synthetic atmosphere, as
+    differentiable torch functions of the band centres."""
+
+    def __init__(self, data_dir, lambda0_nm, device="cuda"):
+        import torch
+        raw = load_bands(Path(data_dir) / "bands.csv")
+        f64 = dict(dtype=torch.float64, device=device)
+        self.centers = torch.as_tensor(raw["center_nm"].astype(np.float64), **f64)
+        self.irradiance = torch.as_tensor(raw["solar_irradiance_w_m2"].astype(np.float64), **f64)
+        self.ozone = torch.as_tensor(raw["ozone_cross_section_cm2"].astype(np.float64), **f64)
+        self.lambda0 = torch.as_tensor(np.asarray(lambda0_nm, dtype=np.float64), **f64)
+        with torch.no_grad():
+            self.ref = self.tables(self.lambda0)
+
+    def tables(self, lam):
+        """(Rayleigh cross section / 5.8e-31, ozone cross section, solar irradiance) at lam."""
+        return (RAYLEIGH_REF_NM / lam) ** 4, _interp(self.centers, self.ozone, lam), \
+            _interp(self.centers, self.irradiance, lam)
+
+    def multipliers(self, lam):
+        """Band multipliers [K, 4] (Rayleigh, Mie, ozone, solar) of wavelengths lam
+        relative to lambda0, float32 for the renderer."""
+        import torch
+        r, o, s = self.tables(lam)
+        r0, o0, s0 = self.ref
+        ones = torch.ones_like(r)
+        ozone = torch.where(o0 > 0, o / torch.where(o0 > 0, o0, ones), ones)
+        return torch.stack([r / r0, ones, ozone, s / s0], dim=1).to(torch.float32)
+
+
+# ---- scoring: sky-wavelength-optimizer/src/main.rs:1121-1156 -------------------------------
+
+
+def xyz_to_oklab(xyz):
+    """Oklab of XYZ (Ottosson's published matrices), signed cube root."""
+    import torch
+    m1 = torch.tensor([[0.8189330101, 0.3618667424, -0.1288597137],
+                       [0.0329845436, 0.9293118715, 0.0361456387],
+                       [0.0482003018, 0.2643662691, 0.6338517070]], dtype=xyz.dtype, device=xyz.device)
+    m2 = torch.tensor([[0.2104542553, 0.7936177850, -0.0040720468],
+                       [1.9779984951, -2.4285922050, 0.4505937099],
+                       [0.0259040371, 0.7827717662, -0.8086757660]], dtype=xyz.dtype, device=xyz.device)
+    lms = xyz @ m1.T
+    lms = torch.sign(lms) * lms.abs().pow(1.0 / 3.0)
+    return lms @ m2.T
+
+
+def _percentile_sorted(values, q: float) -> float:
+    """percentile_sorted (main.rs:1150-1156): the element at round((n-1) q)."""
+    n = values.numel()
+    return float(values[int(round((n - 1) * min(max(q, 0.0), 1.0)))])
+
+
+def oklab_score(xyz, xyz_ref) -> dict:
+    """The reference optimizer's score of a reconstruction: XYZ / p99(Y_ref)
+    to Oklab, per-sample distance, rmse, p50..p99 and rmse + 0.25 p95
+    (evaluate_combo, main.rs:414-488)."""
+    import torch
+    xyz, xyz_ref = xyz.reshape(-1, 3).double(), xyz_ref.reshape(-1, 3).double()
+    y_sorted = torch.sort(xyz_ref[:, 1][torch.isfinite(xyz_ref[:, 1])]).values
+    scale = max(_percentile_sorted(y_sorted, 0.99), 1e-12)
+    d = (xyz_to_oklab(xyz / scale) - xyz_to_oklab(xyz_ref / scale)).norm(dim=1)
+    d = torch.sort(d[torch.isfinite(d)]).values
+    rmse = float(torch.sqrt((d * d).mean()))
+    p95 = _percentile_sorted(d, 0.95)
+    return {"mean": float(d.mean()), "rmse": rmse, "p50": _percentile_sorted(d, 0.50),
+            "p90": _percentile_sorted(d, 0.90), "p95": p95, "p99": _percentile_sorted(d, 0.99),
+            "max": float(d[-1]), "score": rmse + 0.25 * p95}
+
+
+def relative_xyz_error(xyz, xyz_ref) -> float:
+    """sum |XYZ - XYZ_ref| / sum |XYZ_ref| over all pixels and components."""
+    return float((xyz - xyz_ref).abs().sum() / xyz_ref.abs().sum())
+
+
+# ---- the fit ----------------------------------------------------------------------------
+
+
+@dataclass
+class PrimaryFitConfig:
+    """Sixteen sun elevations (denser near the horizon), each a 256x128
+    sky-view LUT; targets from 81 wavelengths (380-780 nm, 5 nm); the fit
+    renders 4 primaries at 32 spp per elevation and step."""
+
+    primaries_nm: tuple = (450.0, 520.0, 570.0, 630.0)
+    elevation_count: int = 16
+    elevation_range: tuple = (0.0, 90.0)
+    width: int = 256
+    height: int = 128
+    fit_spp: int = 32
+    target_spp: int = 1024
+    target_wavelengths: tuple = (380.0, 780.0, 81)
+    iterations: int = 200
+    lr_nm: float = 1.0
+    lr_matrix: float = 0.01      # relative to the initial matrix's mean magnitude
+    fd_step_nm: float = 1.0
+    seed: int = 0x5EC7_2026_0430
+    data_dir: str = ""
+    atmosphere: SyntheticAtmosphere = field(default_factory=SyntheticAtmosphere)
+    # sky-view LUT columns nearest the sun's azimuth, which hold the sun disc:
+    # its rare hits would dominate every squared error, so they are left out
+    sun_columns: int = 2
+
+    @property
+    def elevations(self) -> np.ndarray:
+        lo, hi = self.elevation_range
+        return elevation_schedule(self.elevation_count, lo, hi)
+
+    def keep(self):
+        """[P, 1] float64 mask of the pixels the loss and the errors use."""
+        import torch
+        x = torch.arange(self.width * self.height, device="cuda") % self.width
+        return (x >= self.sun_columns).to(torch.float64)[:, None]
+
+    def render_config(self, spp: int, seed: int) -> RenderConfig:
+        return RenderConfig(width=self.width, height=self.height, spp=spp, seed=seed,
+                            output_projection=_abi.PROJECTION_SKY_VIEW_LUT, phase_sampling=_abi.PHASE_TABULATED,
+                            tracking=_abi.TRACKING_MERGED_LAYERS, rr_start_depth=8)
+
+
+def _suns(cfg: PrimaryFitConfig, scene):
+    return [sun_from_degrees(float(e), 0.0, scene.sun_angular_radius_rad)[0] for e in cfg.elevations]
+
+
+def render_band_films(scene, cfg: PrimaryFitConfig, spp: int, seed: int):
+    """Films [E, P, B] (float64 means) of `scene` at every elevation and the
+    variances of those means, rendered by the persistent tracer as one batch
+    (one job per elevation)."""
+    import torch
+    gs = GpuScene(scene)
+    try:
+        base = cfg.render_config(spp, seed)
+        cells = base.pixels * scene.band_count
+        sums = [torch.zeros(cells, dtype=torch.float64, device="cuda") for _ in cfg.elevations]
+        sqs = [torch.zeros(cells, dtype=torch.float64, device="cuda") for _ in cfg.elevations]
+        status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        jobs = []
+        for i, (e, sun) in enumerate(zip(cfg.elevations, _suns(cfg, scene))):
+            c = dataclasses.replace(base, sun_elevation_deg=float(e))
+            outs = {"cell_sum": sums[i].data_ptr(), "cell_sumsq": sqs[i].data_ptr()}
+            if i == 0:
+                outs["status"] = status.data_ptr()
+            jobs.append((c, sun, outs))
+        gs.render_batch(jobs, torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        if int(status.item()):
+            raise _abi.RenderWatchdog(_abi.SKY_ERR_WATCHDOG, "GPU path watchdog was reached")
+        shape = (len(sums), base.pixels, scene.band_count)
+        mean = torch.stack(sums).reshape(shape) / spp
+        var = ((torch.stack(sqs).reshape(shape) - mean * mean * spp) / max(spp - 1, 1)).clamp_min(0.0) / spp
+        return mean, var
+    finally:
+        gs.close()
+
+
+def target_xyz(cfg: PrimaryFitConfig):
+    """XYZ [E, P, 3] of the full-spectrum renders (band_xyz_weights per band)
+    and the variance of that estimate."""
+    import torch
+    lo, hi, n = cfg.target_wavelengths
+    scene = synthetic_scene(wavelengths(lo, hi, n), cfg.data_dir, sun_elevation_deg=10.0, atmosphere=cfg.atmosphere)
+    mean, var = render_band_films(scene, cfg, cfg.target_spp, cfg.seed ^ 0x7A46E7)
+    w = torch.as_tensor(np.asarray(scene.band_xyz, np.float64), device="cuda")
+    return mean @ w, var @ (w * w)
+
+
+def _loss(xyz_hat, target, keep):
+    return (keep * (xyz_hat - target) ** 2).sum() / (keep * target ** 2).sum()
+
+
+def _initial_matrix(films, target, keep):
+    """Least-squares K x 3 matrix of the initial primaries."""
+    import torch
+    a = (films * keep).reshape(-1, films.shape[-1])
+    b = (target * keep).reshape(-1, 3)
+    return torch.linalg.lstsq(a, b).solution
+
+
+def _scene_at(cfg: PrimaryFitConfig, lam_nm):
+    return synthetic_scene(np.asarray(lam_nm, dtype=np.float64), cfg.data_dir, sun_elevation_deg=10.0,
+                           atmosphere=cfg.atmosphere)
+
+
+def evaluate(cfg: PrimaryFitConfig, lam_nm, matrix, target, target_var=None, spp=None) -> dict:
+    """Error of primaries and matrix: plain-tracer renders at the primaries
+    (target_spp unless given), XYZ through the matrix, against the targets.
+    Besides the raw errors, the squared error with both renders' Monte Carlo
+    variance subtracted estimates the reconstruction error itself."""
+    spp = spp or cfg.target_spp
+    mean, var = render_band_films(_scene_at(cfg, lam_nm), cfg, spp, cfg.seed ^ 0x51A7)
+    m = matrix.detach().double()
+    keep = cfg.keep()
+    sel = keep[:, 0].bool()
+    xyz = mean @ m
+    out = {"relative_xyz_error": relative_xyz_error(xyz[:, sel], target[:, sel]),
+           "oklab": oklab_score(xyz[:, sel], target[:, sel])}
+    d2 = (keep * (xyz - target) ** 2).sum()
+    noise = (keep * (var @ (m * m))).sum() + ((keep * target_var).sum() if target_var is not None else 0.0)
+    t2 = (keep * target ** 2).sum()
+    out["relative_rms_error"] = float(math.sqrt(float(d2 / t2)))
+    out["relative_rms_error_debiased"] = float(math.sqrt(max(float((d2 - noise) / t2), 0.0)))
+    out["relative_rms_noise"] = float(math.sqrt(float(noise / t2)))
+    return out
+
+
+def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int = 0) -> dict:
+    """Adam over (lambda, M); every step renders all elevations with the
+    differentiable renderer and back-propagates through the adjoint."""
+    import torch
+    iterations = cfg.iterations if iterations is None else iterations
+    scene = _scene_at(cfg, cfg.primaries_nm)
+    gs = GpuScene(scene)
+    model = BandModel(cfg.data_dir, cfg.primaries_nm)
+    layer = torch.as_tensor(initial_layer_params(scene, cfg.atmosphere.mie_g), device="cuda")
+    suns = _suns(cfg, scene)
+    lam = torch.tensor(cfg.primaries_nm, dtype=torch.float64, device="cuda", requires_grad=True)
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        films0 = torch.stack([render_film(AdjointRenderer(gs, cfg.render_config(cfg.fit_spp, cfg.seed)), layer,
+                                          model.multipliers(lam), sun=s).reshape(-1, scene.band_count)
+                              for s in suns]).double()
+    keep = cfg.keep()
+    matrix = _initial_matrix(films0, target, keep).clone().requires_grad_(True)
+    scale = float(matrix.detach().abs().mean())
+    opt = torch.optim.Adam([{"params": [lam], "lr": cfg.lr_nm},
+                            {"params": [matrix], "lr": cfg.lr_matrix * scale}])
+    history = []
+    for it in range(iterations):
+        # the backward pass traces its own samples: the L2 loss's gradient is
+        # then free of the film noise's correlation with its derivative
+        r = AdjointRenderer(gs, cfg.render_config(cfg.fit_spp, cfg.seed + 1 + it))
+        opt.zero_grad()
+        k = model.multipliers(lam)
+        films = torch.stack([render_film(r, layer, k, sun=s, decorrelate=True).reshape(-1, scene.band_count)
+                             for s in suns])
+        loss = _loss(films.double() @ matrix, target, keep)
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            lam.clamp_(380.0, 780.0)
+        history.append(float(loss.detach()))
+        if log_every and (it % log_every == 0 or it == iterations - 1):
+            print(f"adjoint it {it:4d} loss {history[-1]:.6e} lambda {lam.detach().cpu().numpy().round(2)}")
+    torch.cuda.synchronize()
+    seconds = time.perf_counter() - t0
+    gs.close()
+    return {"lambda_nm": lam.detach().cpu().numpy().tolist(), "matrix": matrix.detach(), "loss": history,
+            "seconds": seconds, "iterations": iterations}
+
+
+def fit_finite_differences(cfg: PrimaryFitConfig, target, iterations=None, log_every: int = 0) -> dict:
+    """The same fit with dLoss/dlambda from central differences of the plain
+    tracer: per step, the K-band scene at lambda and K single-band scenes at
+    lambda_k +- h (shared seed), each rendered at every elevation."""
+    import torch
+    iterations = cfg.iterations if iterations is None else iterations
+    lam = torch.tensor(cfg.primaries_nm, dtype=torch.float64, device="cuda", requires_grad=True)
+    t0 = time.perf_counter()
+    films0 = render_band_films(_scene_at(cfg, cfg.primaries_nm), cfg, cfg.fit_spp, cfg.seed)[0]
+    keep = cfg.keep()
+    matrix = _initial_matrix(films0, target, keep).clone().requires_grad_(True)
+    scale = float(matrix.detach().abs().mean())
+    opt = torch.optim.Adam([{"params": [lam], "lr": cfg.lr_nm},
+                            {"params": [matrix], "lr": cfg.lr_matrix * scale}])
+    h = cfg.fd_step_nm
+    history = []
+    for it in range(iterations):
+        seed = cfg.seed + 1 + it
+        l_now = lam.detach().cpu().numpy()
+        films = render_band_films(_scene_at(cfg, l_now), cfg, cfg.fit_spp, seed)[0]
+        opt.zero_grad()
+        loss = _loss(films @ matrix, target, keep)
+        loss.backward()  # dLoss/dM
+        grad = np.zeros(len(l_now))
+        with torch.no_grad():
+            for kk in range(len(l_now)):
+                js = []
+                for sign in (1.0, -1.0):
+                    one = render_band_films(_scene_at(cfg, [l_now[kk] + sign * h]), cfg, cfg.fit_spp, seed)[0]
+                    f = films.clone()
+                    f[..., kk] = one[..., 0]
+                    js.append(float(_loss(f @ matrix, target, keep)))
+                grad[kk] = (js[0] - js[1]) / (2 * h)
+        lam.grad = torch.as_tensor(grad, dtype=torch.float64, device="cuda")
+        opt.step()
+        with torch.no_grad():
+            lam.clamp_(380.0, 780.0)
+        history.append(float(loss.detach()))
+        if log_every and (it % log_every == 0 or it == iterations - 1):
+            print(f"fd it {it:4d} loss {history[-1]:.6e} lambda {lam.detach().cpu().numpy().round(2)}")
+    torch.cuda.synchronize()
+    seconds = time.perf_counter() - t0
+    return {"lambda_nm": lam.detach().cpu().numpy().tolist(), "matrix": matrix.detach(), "loss": history,
+            "seconds": seconds, "iterations": iterations}

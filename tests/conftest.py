@@ -32,7 +32,7 @@ def ref_scene():
 
 
 @pytest.fixture(scope="session")
-def cfg0_scene():
+def dome_scene():
     """The CPU-runnable benchmark scene: 32 wavelengths 380-780 nm, sun 10 deg."""
     from sky_cuda import synthetic_scene, wavelengths
     return synthetic_scene(wavelengths(380.0, 780.0, 32), DATA_DIR, sun_elevation_deg=10.0)

@@ -84,7 +84,7 @@ def test_version_string(lib_built):
     assert b"sky_cuda" in lib.sky_cuda_version()
 
 
-def test_invalid_arguments_are_rejected_without_a_device(lib_built, cfg0_scene):
+def test_invalid_arguments_are_rejected_without_a_device(lib_built, dome_scene):
     """Argument errors map to InvalidConfig before any device work; with no
     usable device, scene creation reports the NoAdapter-equivalent status."""
     from conftest import gpu_available
@@ -97,7 +97,7 @@ def test_invalid_arguments_are_rejected_without_a_device(lib_built, cfg0_scene):
     assert lib.sky_cuda_render(None, ctypes.byref(cfg), film, 4, None) == _abi.SKY_ERR_INVALID_CONFIG
     assert "scene" in _abi.last_error(lib)
     if not gpu_available():
-        desc = cfg0_scene.desc()
+        desc = dome_scene.desc()
         st = lib.sky_cuda_scene_create(ctypes.byref(desc), ctypes.byref(handle))
         assert st == _abi.SKY_ERR_NO_DEVICE
         with pytest.raises(_abi.SkyCudaError) as e:

@@ -55,33 +55,33 @@ def small_scene(data_dir):
 
 
 @pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
-def test_primal_traces_the_plain_chains(gpu, cfg0_scene, phase):
+def test_primal_traces_the_plain_chains(gpu, dome_scene, phase):
     """One sample per cell: the adjoint primal (residual carry over the
     device-baked uniform layers) and the plain tracer (residual carry over the
     scene's grid) consume the same random numbers; their chains agree except
     where float rounding flips a decision."""
     cfg = RenderConfig(width=32, height=16, spp=1, sample_offset=3, phase_sampling=phase,
                        tracking=_abi.TRACKING_RESIDUAL_CARRY)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         want, _ = plain_sums(gs, dataclasses.replace(cfg, kernel=_abi.KERNEL_PLAIN))
         r = AdjointRenderer(gs, cfg)
-        got = r.forward(_t(initial_layer_params(cfg0_scene, G0)))["cell_sum"].cpu().numpy()
+        got = r.forward(_t(initial_layer_params(dome_scene, G0)))["cell_sum"].cpu().numpy()
     close = np.abs(got - want) <= 1e-3 * np.maximum(np.abs(got), np.abs(want)) + 1e-30
     print("chain agreement", close.mean())
     assert close.mean() >= 0.98
 
 
-def test_primal_statistics_match_plain_tracer(gpu, cfg0_scene):
+def test_primal_statistics_match_plain_tracer(gpu, dome_scene):
     cfg = RenderConfig(width=32, height=16, spp=256, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         s_p, q_p = plain_sums(gs, cfg)
         out = AdjointRenderer(gs, dataclasses.replace(cfg, seed=cfg.seed + 1)).forward(
-            _t(initial_layer_params(cfg0_scene, G0)))
+            _t(initial_layer_params(dome_scene, G0)))
     s_a, q_a = out["cell_sum"].cpu().numpy(), out["cell_sumsq"].cpu().numpy()
-    shape = (cfg.pixels, cfg0_scene.band_count)
-    xa, va = xyz_from_sums(s_a.reshape(shape), q_a.reshape(shape), cfg.spp, cfg0_scene.band_xyz)
-    xp, vp = xyz_from_sums(s_p.reshape(shape), q_p.reshape(shape), cfg.spp, cfg0_scene.band_xyz)
+    shape = (cfg.pixels, dome_scene.band_count)
+    xa, va = xyz_from_sums(s_a.reshape(shape), q_a.reshape(shape), cfg.spp, dome_scene.band_xyz)
+    xp, vp = xyz_from_sums(s_p.reshape(shape), q_p.reshape(shape), cfg.spp, dome_scene.band_xyz)
     rep = parity_report(xa, va, xp, vp)
     print("adjoint primal vs plain", rep)
     assert rep["frac_beyond_3se"] <= 0.02
@@ -112,18 +112,18 @@ def _numpy_bake(scene, params, layers):
     return out
 
 
-def test_device_majorant_bake(gpu, cfg0_scene):
-    layers = cfg0_scene.layer_count
-    theta0 = initial_layer_params(cfg0_scene, G0)
+def test_device_majorant_bake(gpu, dome_scene):
+    layers = dome_scene.layer_count
+    theta0 = initial_layer_params(dome_scene, G0)
     rng = np.random.default_rng(3)
     theta = theta0.copy()
     theta[:3 * layers] = (1.0 + rng.normal(0.0, 0.05, 3 * layers)).astype(np.float32)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         r = AdjointRenderer(gs, RenderConfig(width=4, height=4, spp=1, tracking=_abi.TRACKING_MERGED_LAYERS))
         base = r.bake_majorants(_t(theta0)).cpu().numpy()
         moved = r.bake_majorants(_t(theta)).cpu().numpy()
-    np.testing.assert_allclose(base, cfg0_scene.majorants, rtol=2e-5)
-    np.testing.assert_allclose(moved, _numpy_bake(cfg0_scene, theta, layers), rtol=1e-4)
+    np.testing.assert_allclose(base, dome_scene.majorants, rtol=2e-5)
+    np.testing.assert_allclose(moved, _numpy_bake(dome_scene, theta, layers), rtol=1e-4)
 
 
 def _loss_setup(gs, scene, cfg, target_spp=256):
@@ -155,20 +155,20 @@ def _loss_setup(gs, scene, cfg, target_spp=256):
     return theta0, loss_of, dloss
 
 
-def test_gradient_matches_central_differences(gpu, cfg0_scene):
+def test_gradient_matches_central_differences(gpu, dome_scene):
     """The adjoint benchmark's finite-difference check (h = 1e-3, 16 parameters drawn with
     seed 4) on a 32x16 image, 32 bands, 64 spp."""
     cfg = RenderConfig(width=32, height=16, spp=64, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS)
     h = 1e-3
-    with GpuScene(cfg0_scene) as gs:
-        theta0, loss_of, dloss = _loss_setup(gs, cfg0_scene, cfg)
+    with GpuScene(dome_scene) as gs:
+        theta0, loss_of, dloss = _loss_setup(gs, dome_scene, cfg)
         r = AdjointRenderer(gs, cfg, estimator=NULL_COLLISIONS)
         th0 = _t(theta0)
         grad, _ = r.backward(th0, None, dloss(r.forward(th0)))
         grad = grad.cpu().numpy()
         idx = np.random.default_rng(4).choice(theta0.size, 16, replace=False)
-        names = param_names(cfg0_scene.layer_count)
+        names = param_names(dome_scene.layer_count)
         rows = []
         for i in idx:
             tp, tm = theta0.copy(), theta0.copy()
@@ -240,6 +240,20 @@ def _scene_along(scene, direction, delta):
     return s.bake_majorants(scene.layer_count)
 
 
+def _sun_pixels(scene, cfg):
+    """Panorama pixels whose footprint holds part of the sun disc
+    (panorama_dir, sky_trace.wgsl:614-623, inverted)."""
+    x, y, z = scene.sun_direction
+    u = np.arctan2(x, z) / (2 * np.pi) + 0.5
+    v = 0.5 - np.arcsin(y) / np.pi
+    r = scene.sun_angular_radius_rad
+    px = np.arange(cfg.pixels) % cfg.width
+    py = np.arange(cfg.pixels) // cfg.width
+    du, dv = r / (2 * np.pi * max(np.cos(np.arcsin(y)), 1e-3)), r / np.pi
+    return ((px + 1) / cfg.width >= u - du) & (px / cfg.width <= u + du) & \
+        ((py + 1) / cfg.height >= v - dv) & (py / cfg.height <= v + dv)
+
+
 @pytest.mark.parametrize("estimator", [SEGMENT_INTEGRALS, NULL_COLLISIONS])
 @pytest.mark.parametrize("direction,delta", [("rayleigh", 0.05), ("mie", 0.05), ("ozone", 0.2), ("albedo", 0.02),
                                              ("g", 0.02)])
@@ -247,14 +261,16 @@ def test_gradient_matches_plain_tracer_differences(gpu, small_scene, direction, 
     """The adjoint gradient projected on a whole-atmosphere direction against
     central differences of the plain tracer (scene tables moved along the
     direction, 4096 spp in 16 batches, common seeds), for the linear loss
-    J = sum_cells w_cell film_cell."""
+    J = sum_cells w_cell film_cell (pixels holding the sun disc weighted 0)."""
     import torch
     batches, spp = 16, 256
     L = small_scene.layer_count
     cfg = RenderConfig(width=16, height=8, spp=spp, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS)
     cells = cfg.pixels * small_scene.band_count
-    w = np.random.default_rng(7).uniform(0.5, 1.5, cells) / cells
+    w = np.random.default_rng(7).uniform(0.5, 1.5, (cfg.pixels, small_scene.band_count)) / cells
+    w[_sun_pixels(small_scene, cfg)] = 0.0  # the sun disc's rare hits would dominate both variances
+    w = w.reshape(-1)
     proj = {"rayleigh": lambda g: g[0:3 * L:3].sum(), "mie": lambda g: g[1:3 * L:3].sum(),
             "ozone": lambda g: g[2:3 * L:3].sum(), "albedo": lambda g: g[3 * L], "g": lambda g: g[3 * L + 1]}[direction]
     fd, adj = [], []
@@ -300,21 +316,21 @@ def test_autograd_function_matches_direct_backward(gpu, small_scene):
                                atol=1e-6 * float(bg.abs().max()))
 
 
-def test_adjoint_errors(gpu, ref_scene, cfg0_scene):
+def test_adjoint_errors(gpu, ref_scene, dome_scene):
     import ctypes
     import torch
     with GpuScene(ref_scene) as gs:  # the reference's four aerosol species
         r = AdjointRenderer(gs, RenderConfig(width=4, height=4, spp=1))
         with pytest.raises(SkyCudaError, match="species"):
             r.forward(torch.ones(r.param_count, device="cuda"))
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         lib = gs.lib
         cfg = RenderConfig(width=4, height=4, spp=1, tracking=_abi.TRACKING_SEGMENT_RESTART).to_c()
-        th = _t(initial_layer_params(cfg0_scene, G0))
+        th = _t(initial_layer_params(dome_scene, G0))
         p = _abi.SkyAdjointParams()
         p.layer_params = th.data_ptr()
         st = torch.zeros(1, dtype=torch.int32, device="cuda")
-        s = torch.zeros(16 * cfg0_scene.band_count, dtype=torch.float64, device="cuda")
+        s = torch.zeros(16 * dome_scene.band_count, dtype=torch.float64, device="cuda")
         o = _abi.SkyDeviceOutputs()
         o.cell_sum, o.status = s.data_ptr(), st.data_ptr()
         assert lib.sky_cuda_adjoint_forward(gs.handle, ctypes.byref(cfg), ctypes.byref(p), ctypes.byref(o),
@@ -324,9 +340,9 @@ def test_adjoint_errors(gpu, ref_scene, cfg0_scene):
         other = th.clone()  # a second parameter set is refused by the backward call
         p.sample_layer_params = other.data_ptr()
         g = _abi.SkyAdjointGrads()
-        d = torch.zeros(16 * cfg0_scene.band_count, device="cuda")
+        d = torch.zeros(16 * dome_scene.band_count, device="cuda")
         lg = torch.zeros(r.param_count, dtype=torch.float64, device="cuda")
         g.dloss_dfilm, g.layer_grad, g.status = d.data_ptr(), lg.data_ptr(), st.data_ptr()
         assert lib.sky_cuda_adjoint_backward(gs.handle, ctypes.byref(r._c_config), ctypes.byref(p),
                                              ctypes.byref(g), None) == _abi.SKY_ERR_INVALID_CONFIG
-        assert lib.sky_cuda_adjoint_param_count(gs.handle) == 3 * cfg0_scene.layer_count + 2
+        assert lib.sky_cuda_adjoint_param_count(gs.handle) == 3 * dome_scene.layer_count + 2

@@ -47,18 +47,18 @@ KERNELS = (_abi.KERNEL_PLAIN, _abi.KERNEL_WAVEFRONT)
 
 @pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("tracking,phase", MODES)
-def test_chains_match_oracle(gpu, cfg0_scene, tracking, phase, kernel):
+def test_chains_match_oracle(gpu, dome_scene, tracking, phase, kernel):
     """One sample per cell: each GPU chain against the oracle's chain with the
     same counter-based random stream.  Differences come only from rounding
     (fast-math intrinsics, the impact-parameter geometry), which flips a
     decision in a small fraction of chains."""
     agree = total = 0
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         for offset in (0, 7, 1000):
             cfg = RenderConfig(width=16, height=8, spp=1, sample_offset=offset, seed=0x5EC7_2026_0430 + offset,
                                phase_sampling=phase, tracking=tracking, max_orders=16, kernel=kernel)
             g, _, _, st = gpu_sums(gs, cfg)
-            o, _, _, wd = oracle.render(cfg0_scene, cfg)
+            o, _, _, wd = oracle.render(dome_scene, cfg)
             assert st == 0 and wd == 0
             close = np.abs(g - o) <= 2e-3 * np.maximum(np.abs(g), np.abs(o)) + 1e-9
             agree += int(close.sum())
@@ -70,10 +70,10 @@ def test_chains_match_oracle(gpu, cfg0_scene, tracking, phase, kernel):
 
 @pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
 @pytest.mark.parametrize("tracking", [_abi.TRACKING_RESIDUAL_CARRY, _abi.TRACKING_MERGED_LAYERS])
-def test_wavefront_matches_plain_chains(gpu, cfg0_scene, tracking, phase):
+def test_wavefront_matches_plain_chains(gpu, dome_scene, tracking, phase):
     """The persistent kernel consumes each chain's random stream in the plain
     kernel's order: chain by chain, the two kernels trace the same paths."""
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         cfg = RenderConfig(width=32, height=16, spp=1, sample_offset=3, phase_sampling=phase, tracking=tracking,
                            max_orders=16, rr_start_depth=8)
         a, _, ca, _ = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_PLAIN}))
@@ -85,20 +85,20 @@ def test_wavefront_matches_plain_chains(gpu, cfg0_scene, tracking, phase):
 
 
 @pytest.mark.parametrize("tracking,phase", [MODES[0], MODES[3], MODES[5]])
-def test_statistical_parity_cfg0(gpu, cfg0_scene, tracking, phase):
+def test_statistical_parity_dome(gpu, dome_scene, tracking, phase):
     """The CPU-runnable benchmark scene (64x32, 32 bands, 64 spp): per-pixel
     XYZ of GPU and oracle within 3 combined standard errors, and no bias."""
     cfg = RenderConfig(width=64, height=32, spp=64, sun_elevation_deg=10.0, phase_sampling=phase,
                        tracking=tracking, max_orders=16)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         gs_, gq, _, st = gpu_sums(gs, cfg)
     cfg_o = RenderConfig(**{**cfg.__dict__, "seed": 12345})
-    os_, oq, _, wd = oracle.render(cfg0_scene, cfg_o)
+    os_, oq, _, wd = oracle.render(dome_scene, cfg_o)
     assert st == 0 and wd == 0
-    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, cfg0_scene.band_xyz)
-    xo, vo = xyz_from_sums(os_, oq, cfg.spp, cfg0_scene.band_xyz)
+    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, dome_scene.band_xyz)
+    xo, vo = xyz_from_sums(os_, oq, cfg.spp, dome_scene.band_xyz)
     r = parity_report(xg, vg, xo, vo)
-    print("cfg0 parity", r)
+    print("dome parity", r)
     assert r["frac_beyond_3se"] <= 0.01
     assert abs(r["mean_z"]) < 0.1
     for b, se in zip(r["bias_xyz"], r["bias_se_xyz"]):
@@ -161,14 +161,14 @@ def test_single_scatter_known_answer(gpu, data_dir, tracking):
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
-def test_film_matches_sums_and_progressive_is_exact(gpu, cfg0_scene, kernel):
+def test_film_matches_sums_and_progressive_is_exact(gpu, dome_scene, kernel):
     """Film = clamped mean of the sums; two progressive halves add up to one
     render (bit for bit on the plain kernel, whose sums have a fixed order;
     to FP64 rounding on the persistent kernel, whose cells add in the order
     chains finish)."""
     cfg = RenderConfig(width=16, height=8, spp=64, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS, kernel=kernel)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         film, stats = gs.render(cfg)
         s, q, _, _ = gpu_sums(gs, cfg)
         np.testing.assert_array_equal(film.values, np.maximum((s / 64).astype(np.float32), 0).ravel())
@@ -194,18 +194,18 @@ def test_film_matches_sums_and_progressive_is_exact(gpu, cfg0_scene, kernel):
     assert stats.events["chain"] == stats.chains
 
 
-def test_xyz_outputs(gpu, cfg0_scene):
+def test_xyz_outputs(gpu, dome_scene):
     cfg = RenderConfig(width=16, height=8, spp=64)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         film, xyz, var, _ = gs.render_xyz(cfg)
         s, q, _, _ = gpu_sums(gs, cfg)
-    x_ref, v_ref = xyz_from_sums(s, q, 64, cfg0_scene.band_xyz)
+    x_ref, v_ref = xyz_from_sums(s, q, 64, dome_scene.band_xyz)
     np.testing.assert_allclose(xyz, x_ref, rtol=1e-12, atol=1e-15)
     np.testing.assert_allclose(var, v_ref, rtol=1e-9, atol=1e-20)
 
 
-def test_watchdog_and_errors(gpu, cfg0_scene):
-    with GpuScene(cfg0_scene) as gs:
+def test_watchdog_and_errors(gpu, dome_scene):
+    with GpuScene(dome_scene) as gs:
         # a forced one-event watchdog trips on any scattered path (integrator.rs:301-304)
         with pytest.raises(RenderWatchdog):
             gs.render(RenderConfig(width=8, height=4, spp=4, watchdog_limit=1))
@@ -232,10 +232,10 @@ def test_reference_default_band_count(gpu, ref_scene):
 
 
 @pytest.mark.parametrize("variant,stage,cost", [(0, 0, 0.25), (0, 1, 0.5), (1, 0, 0.1), (1, 1, 1.0)])
-def test_pool_shapes_trace_the_same_chains(gpu, cfg0_scene, variant, stage, cost):
+def test_pool_shapes_trace_the_same_chains(gpu, dome_scene, variant, stage, cost):
     """Every launch shape the autotuner can pick traces the plain kernel's
     paths (the crossing cost changes the tracking grid for both kernels)."""
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         gs.set_tuning(pool_variant=variant, stage_tables=stage, crossing_cost=cost)
         t = gs.get_tuning()
         assert t["pool_variant"] == variant and t["stage_tables"] == stage and abs(t["crossing_cost"] - cost) < 1e-6
@@ -247,11 +247,11 @@ def test_pool_shapes_trace_the_same_chains(gpu, cfg0_scene, variant, stage, cost
     assert close.mean() >= 0.999
 
 
-def test_autotuner_picks_a_measured_shape(gpu, cfg0_scene):
+def test_autotuner_picks_a_measured_shape(gpu, dome_scene):
     from sky_cuda.autotune import autotune
     cfg = RenderConfig(width=64, height=32, spp=64, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         best, results = autotune(gs, cfg, space={"pool_variant": (0, 1), "crossing_cost": (0.25, 0.5)})
         assert len(results) == 4 and all(ms > 0 for _, ms in results)
         assert best == min(results, key=lambda r: r[1])[0]

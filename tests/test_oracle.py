@@ -110,8 +110,8 @@ def test_majorants_dominate_extinction(ref_scene):
             assert ref_scene.minorants[band, layer] <= ext * 1.001 + 1e-8
 
 
-def test_python_bake_matches_oracle_bake(ref_scene, cfg0_scene):
-    for scene in (ref_scene, cfg0_scene):
+def test_python_bake_matches_oracle_bake(ref_scene, dome_scene):
+    for scene in (ref_scene, dome_scene):
         maj, mino = oracle.bake_majorant_grid(scene, scene.layer_count)
         np.testing.assert_array_equal(maj, scene.majorants)
         np.testing.assert_array_equal(mino, scene.minorants)

@@ -1,0 +1,58 @@
+"""Host side of the wavelength-primary fit (no GPU): the band model's
+multipliers against scenes built at the shifted wavelengths, their
+derivatives, and the Oklab scoring."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from sky_cuda import synthetic_scene
+from sky_cuda.primaries import BandModel, oklab_score, xyz_to_oklab
+
+
+def test_band_multipliers_match_rebuilt_scenes(data_dir):
+    lam0 = np.array([450.0, 520.0, 570.0, 630.0])
+    lam1 = lam0 + np.array([-7.3, 4.1, 12.6, -2.2])
+    model = BandModel(data_dir, lam0, device="cpu")
+    k = model.multipliers(torch.as_tensor(lam1)).numpy()
+    s0 = synthetic_scene(lam0, data_dir, sun_elevation_deg=10.0)
+    s1 = synthetic_scene(lam1, data_dir, sun_elevation_deg=10.0)
+    for col, field in ((0, "rayleigh_cross_section_m2"), (2, "ozone_cross_section_cm2"),
+                       (3, "solar_radiance_w_m2_sr")):
+        want = s1.bands[field].astype(np.float64) / s0.bands[field].astype(np.float64)
+        np.testing.assert_allclose(k[:, col], want, rtol=2e-6)
+    np.testing.assert_array_equal(k[:, 1], 1.0)
+    np.testing.assert_allclose(model.multipliers(torch.as_tensor(lam0)).numpy(), 1.0, rtol=1e-7)
+
+
+def test_band_multiplier_derivatives(data_dir):
+    lam0 = np.array([455.0, 610.0])
+    model = BandModel(data_dir, lam0, device="cpu")
+    lam = torch.tensor([458.3, 603.7], dtype=torch.float64, requires_grad=True)
+    k = model.multipliers(lam).double()
+    # Rayleigh: d/dlambda (lambda0/lambda)^4 = -4 k / lambda
+    g = torch.autograd.grad(k[:, 0].sum(), lam, retain_graph=True)[0].numpy()
+    np.testing.assert_allclose(g, -4.0 * k[:, 0].detach().numpy() / lam.detach().numpy(), rtol=1e-6)
+    # ozone / sun: slope of the bands.csv segment holding lambda (piecewise linear)
+    for col, tab in ((2, 1), (3, 2)):
+        g = torch.autograd.grad(k[:, col].sum(), lam, retain_graph=True)[0].numpy()
+        eps = 1e-4
+        ref = model.ref[tab].numpy()
+        hi = model.tables(lam.detach() + eps)[tab].numpy() / ref
+        lo = model.tables(lam.detach() - eps)[tab].numpy() / ref
+        np.testing.assert_allclose(g, (hi - lo) / (2 * eps), rtol=1e-5)
+
+
+def test_oklab_of_d65_white_is_neutral():
+    # Oklab maps the D65 white point (normalised Y = 1) to L = 1, a = b = 0
+    lab = xyz_to_oklab(torch.tensor([[0.95047, 1.0, 1.08883]], dtype=torch.float64)).numpy()[0]
+    np.testing.assert_allclose(lab, [1.0, 0.0, 0.0], atol=2e-4)
+
+
+def test_oklab_score_of_identity_is_zero():
+    xyz = torch.rand(1000, 3, dtype=torch.float64) + 0.01
+    s = oklab_score(xyz, xyz)
+    assert s["rmse"] == 0.0 and s["score"] == 0.0
+    s = oklab_score(xyz * 1.1, xyz)
+    assert s["rmse"] > 0 and s["score"] == pytest.approx(s["rmse"] + 0.25 * s["p95"])

@@ -46,13 +46,13 @@ def _sums(gs, cfg):
 
 
 @pytest.mark.gpu
-def test_batch_equals_separate_renders(gpu, cfg0_scene):
+def test_batch_equals_separate_renders(gpu, dome_scene):
     import torch
     base = RenderConfig(width=24, height=12, spp=32, phase_sampling=_abi.PHASE_TABULATED,
                         tracking=_abi.TRACKING_MERGED_LAYERS, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
     elevations = [-3.0, 2.0, 45.0]
     spp = [32, 64, 16]
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         sweep = Sweep(gs, base, elevations, spp)
         sweep.launch(torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
@@ -60,18 +60,18 @@ def test_batch_equals_separate_renders(gpu, cfg0_scene):
         assert int(sweep.counters[6].item()) == sweep.chains
         got = [(o.cell_sum.cpu().numpy(), o.cell_sumsq.cpu().numpy()) for o in sweep.out]
     for e, n, (s, q) in zip(elevations, spp, got):
-        with GpuScene(cfg0_scene.with_sun(e)) as single:
+        with GpuScene(dome_scene.with_sun(e)) as single:
             rs, rq = _sums(single, RenderConfig(**{**base.__dict__, "spp": n, "sun_elevation_deg": e}))
         np.testing.assert_allclose(s, rs, rtol=1e-12, atol=0)
         np.testing.assert_allclose(q, rq, rtol=1e-12, atol=0)
 
 
 @pytest.mark.gpu
-def test_graph_replay_equals_batch(gpu, cfg0_scene):
+def test_graph_replay_equals_batch(gpu, dome_scene):
     import torch
     base = RenderConfig(width=16, height=16, spp=32, phase_sampling=_abi.PHASE_TABULATED,
                         tracking=_abi.TRACKING_MERGED_LAYERS, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         sweep = Sweep(gs, base, [0.0, 10.0, 60.0], [32, 64, 32])
         stream = torch.cuda.current_stream().cuda_stream
         sweep.launch(stream)
@@ -89,14 +89,14 @@ def test_graph_replay_equals_batch(gpu, cfg0_scene):
 
 
 @pytest.mark.gpu
-def test_pilot_budgets_equalise_errors(gpu, cfg0_scene):
+def test_pilot_budgets_equalise_errors(gpu, dome_scene):
     """Budgets proportional to the pilot's variance give the sweep's jobs
     about the same error (the sun above the horizon, where a 16-spp pilot
     estimates the error well)."""
     import torch
     base = RenderConfig(width=32, height=16, spp=16, phase_sampling=_abi.PHASE_TABULATED,
                         tracking=_abi.TRACKING_MERGED_LAYERS, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         elevations = [3.0, 15.0, 60.0]
         spp, p95 = plan_budgets(gs, base, elevations, pilot_spp=64, lo=32, hi=2048, jitter=0.0)
         sweep = Sweep(gs, RenderConfig(**{**base.__dict__, "seed": 99}), elevations, spp)

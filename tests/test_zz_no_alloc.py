@@ -51,12 +51,12 @@ def _outputs_struct(bufs, status=None, counters=None):
     return o
 
 
-def test_noalloc_batch_matches_render_device(gpu, cfg0_scene):
+def test_noalloc_batch_matches_render_device(gpu, dome_scene):
     import torch
     lib = _abi.load_library()
     configs = _configs()
     stream = torch.cuda.current_stream().cuda_stream
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         bands = gs.band_count
         reference = []
         for cfg in configs:
@@ -90,12 +90,12 @@ def test_noalloc_batch_matches_render_device(gpu, cfg0_scene):
                 np.testing.assert_allclose(got["film"].cpu().numpy(), ref["film"], rtol=1e-6, atol=0)
 
 
-def test_noalloc_rejects_oversized_batch(gpu, cfg0_scene):
+def test_noalloc_rejects_oversized_batch(gpu, dome_scene):
     import torch
     lib = _abi.load_library()
     n = _abi.NOALLOC_MAX_JOBS + 1
     cfg = RenderConfig(width=4, height=4, spp=4, tracking=_abi.TRACKING_MERGED_LAYERS)
-    with GpuScene(cfg0_scene) as gs:
+    with GpuScene(dome_scene) as gs:
         bufs = _buffers(torch, cfg, gs.band_count)
         status = torch.zeros(1, dtype=torch.int32, device="cuda")
         c_configs = (_abi.SkyRenderConfig * n)(*[cfg.to_c() for _ in range(n)])
