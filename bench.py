@@ -39,6 +39,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "sky-tracer_gb300"))
 DATA_DIR = ROOT / "tests" / "golden" / "data"
 
+# DRAM bytes (read + write) of one launch of the tracer on the production
+# render, from a 1-pass ncu capture (profiles/pool_kernel_plain-512x256-81wl-256spp_dram.txt).
+POOL_LAUNCH_DRAM_BYTES = {"plain-512x256-81wl-256spp": 13.24e6 + 183.27e6}
+
 # Frozen per-event FP32 work weights (FLOP, an FMA counted as 2), counted
 # from the reference shader's arithmetic for each event type.
 EVENT_FLOPS = {"track_step": 72, "segment": 48, "boundary": 40, "scatter": 200, "nee": 40, "ground": 150,
@@ -719,7 +723,9 @@ def main():
                     "d2h_bytes_per_step": int(cells * 4 + 8 * 8 + 4)},
             "time_to_1pct_xyz_s": t1pct, "p95_rel_se_at_spp": p95,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "frac": achieved / peak if peak else None,
+                         "traffic": POOL_LAUNCH_DRAM_BYTES.get(args.workload) if cfg.kernel != 1 else None,
+                         "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                          "peak_source": "measured: cuBLAS SGEMM 8192^3 with TF32 off (MEASURED_PEAKS.json "
                                         "has no FP32 figure)",
                          "flops_per_step": flops_per_step, "events_per_step": ev},
