@@ -84,10 +84,11 @@ void host_orthonormal_basis(const float n_in[3], float t[3], float b[3]) {
 }
 
 void build_phase_sampling_tables(const float* values, uint32_t band_count, uint32_t bins, std::vector<float>& cdf,
-                                 std::vector<float>& bin_pdf) {
+                                 std::vector<float>& bin_pdf, std::vector<uint16_t>* guide) {
     size_t n = size_t(kSpecies) * band_count * bins;
     cdf.assign(n, 0.0f);
     bin_pdf.assign(n, 0.0f);
+    if (guide) guide->assign(n, 0);
     auto edge = [bins](uint32_t e) {
         float u = float(e) / float(bins);
         return 1.0f - 2.0f * u * u * u;
@@ -107,6 +108,17 @@ void build_phase_sampling_tables(const float* values, uint32_t band_count, uint3
                 bin_pdf[base + bin] = value / norm;
             }
             cdf[base + bins - 1] = 1.0f;
+            if (!guide) continue;
+            // guide[j]: the first bin whose CDF exceeds (j - 1) / bins, a lower
+            // bound of the bin of every xi with floor(xi * bins) = j even when
+            // that product rounds up; a forward scan from it finds the same bin
+            // as a binary search of the whole row
+            uint32_t first = 0;
+            for (uint32_t j = 0; j < bins; ++j) {
+                const double threshold = (double(j) - 1.0) / double(bins);
+                while (first + 1 < bins && double(cdf[base + first]) <= threshold) ++first;
+                (*guide)[base + j] = uint16_t(first);
+            }
         }
     }
 }
@@ -221,7 +233,7 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
     }
     out.optics.assign(d->aerosol_optics, d->aerosol_optics + size_t(B) * kSpecies);
     out.sigma_t.assign(size_t(B) * K, float2{0.0f, 0.0f});
-    uint32_t mie_mask = 0;
+    uint32_t aerosol_mask = 0;
     for (uint32_t b = 0; b < B; ++b) {
         std::vector<double> ext(K);
         for (uint32_t k = 0; k < K; ++k) {
@@ -231,7 +243,8 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
                 const SkyAerosolOptics& o = d->aerosol_optics[b * kSpecies + i];
                 double m = mass[size_t(k) * kSpecies + i];
                 e += std::max(m * o.scattering_km_inv_per_g_m3, 0.0) + std::max(m * o.absorption_km_inv_per_g_m3, 0.0);
-                if (m > 0.0 && o.scattering_km_inv_per_g_m3 > 0.0f) mie_mask |= 1u << i;
+                if (m > 0.0 && (o.scattering_km_inv_per_g_m3 != 0.0f || o.absorption_km_inv_per_g_m3 != 0.0f))
+                    aerosol_mask |= 1u << i;
             }
             ext[k] = e;
         }
@@ -286,7 +299,8 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
 
     // Phase tables and their sampling CDFs.
     out.phase_values.assign(d->phase_values, d->phase_values + nphase);
-    build_phase_sampling_tables(d->phase_values, B, d->phase_bins, out.phase_cdf, out.phase_bin_pdf);
+    if (d->phase_bins > 65535u) return fail("phase tables have more than 65535 bins");
+    build_phase_sampling_tables(d->phase_values, B, d->phase_bins, out.phase_cdf, out.phase_bin_pdf, &out.phase_guide);
 
     // Constants.
     DevScene& S = out.scene;
@@ -309,7 +323,7 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
     S.cos_max = std::cos(d->sun_angular_radius_rad);
     S.one_minus_cos_max = 1.0f - S.cos_max;
     S.light_pdf = 1.0f / (kTauF * (1.0f - S.cos_max));
-    S.mie_mask = mie_mask;
+    S.aerosol_mask = aerosol_mask;
     return SKY_OK;
 }
 

@@ -20,6 +20,7 @@ struct HostTables {
     std::vector<DevProfileKnot> profile;
     std::vector<SkyAerosolOptics> optics;
     std::vector<float> phase_values, phase_cdf, phase_bin_pdf;
+    std::vector<uint16_t> phase_guide;
     std::vector<float> trk_radius, trk_maj;
     std::vector<uint16_t> trk_map;
     std::vector<uint32_t> trk_count, trk_off;
@@ -45,7 +46,7 @@ int build_host_tables(const SkySceneDesc* desc, HostTables& out, std::string& er
 // MiePhaseTable sampling tables (phase.rs:105-135): per (species, band) the
 // CDF over the cube-root mu bins and the per-bin pdf.
 void build_phase_sampling_tables(const float* values, uint32_t band_count, uint32_t bins, std::vector<float>& cdf,
-                                 std::vector<float>& bin_pdf);
+                                 std::vector<float>& bin_pdf, std::vector<uint16_t>* guide = nullptr);
 
 // orthonormal_basis (sky_trace.wgsl:512-520) evaluated on the host.
 void host_orthonormal_basis(const float n_in[3], float t[3], float b[3]);

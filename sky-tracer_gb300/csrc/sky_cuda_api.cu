@@ -448,6 +448,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     size_t o_pv = reserve(h.phase_values.size() * sizeof(float));
     size_t o_pc = reserve(h.phase_cdf.size() * sizeof(float));
     size_t o_pp = reserve(h.phase_bin_pdf.size() * sizeof(float));
+    size_t o_pg = reserve(h.phase_guide.size() * sizeof(uint16_t));
 
     std::vector<unsigned char> host(off, 0);
     auto put = [&](size_t at, const void* src, size_t bytes) { std::memcpy(host.data() + at, src, bytes); };
@@ -461,6 +462,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     put(o_pv, h.phase_values.data(), h.phase_values.size() * sizeof(float));
     put(o_pc, h.phase_cdf.data(), h.phase_cdf.size() * sizeof(float));
     put(o_pp, h.phase_bin_pdf.data(), h.phase_bin_pdf.size() * sizeof(float));
+    put(o_pg, h.phase_guide.data(), h.phase_guide.size() * sizeof(uint16_t));
 
     if ((e = cudaMalloc(&s->blob, off)) != cudaSuccess) {
         delete s;
@@ -483,6 +485,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->dev.phase_values = reinterpret_cast<const float*>(base + o_pv);
     s->dev.phase_cdf = reinterpret_cast<const float*>(base + o_pc);
     s->dev.phase_bin_pdf = reinterpret_cast<const float*>(base + o_pp);
+    s->dev.phase_guide = reinterpret_cast<const uint16_t*>(base + o_pg);
     s->host_majorants = h.majorants;
     s->host_layers = desc->majorant_layers;
     s->host_ground_radius = desc->ground_radius_km;

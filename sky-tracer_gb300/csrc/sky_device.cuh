@@ -305,12 +305,15 @@ __device__ __forceinline__ float cbrt_pos(float x) { return x > 0.0f ? exp2f(__l
 
 __device__ __forceinline__ float rayleigh_phase(float mu) { return kRayleighNorm * (1.0f + mu * mu); }
 
+// Position of mu on the cube-root phase grid: u = ((1 - mu) / 2)^(1/3).
+__device__ __forceinline__ float phase_grid_u(float mu) {
+    return cbrt_pos((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
+}
+
 // mie_phase (sky_trace.wgsl:485-494): lerp between bin centres on the
-// cube-root mu grid.
-__device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, uint32_t band, float mu) {
+// cube-root mu grid, at grid position u.
+__device__ __forceinline__ float mie_phase_u(const DevScene& S, uint32_t species, uint32_t band, float u) {
     uint32_t bins = S.phase_bins;
-    float x = (1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f;
-    float u = cbrt_pos(x);
     float f = u * float(bins) - 0.5f;
     uint32_t i0 = min(uint32_t(fminf(fmaxf(floorf(f), 0.0f), float(bins - 1u))), bins - 1u);
     uint32_t i1 = min(i0 + 1u, bins - 1u);
@@ -320,14 +323,23 @@ __device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, 
     return fmaxf(fmaf(t, p1 - p0, p0), 0.0f);
 }
 
-// mixed_phase_value (sky_trace.wgsl:496-510)
-__device__ __forceinline__ float mixed_phase(const DevScene& S, const Coeffs& c, uint32_t band, float mu) {
+__device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, uint32_t band, float mu) {
+    return mie_phase_u(S, species, band, phase_grid_u(mu));
+}
+
+// mixed_phase_value (sky_trace.wgsl:496-510), at grid position u of mu.
+__device__ __forceinline__ float mixed_phase_u(const DevScene& S, const Coeffs& c, uint32_t band, float mu, float u) {
     if (c.scattering <= 0.0f) return 0.0f;
     float acc = c.rayleigh * rayleigh_phase(mu);
 #pragma unroll
     for (int i = 0; i < int(kSpecies); ++i)
-        if (c.sca[i] > 0.0f) acc = fmaf(c.sca[i], mie_phase(S, uint32_t(i), band, mu), acc);
+        if (c.sca[i] > 0.0f) acc = fmaf(c.sca[i], mie_phase_u(S, uint32_t(i), band, u), acc);
     return acc / c.scattering;
+}
+
+__device__ __forceinline__ float mixed_phase(const DevScene& S, const Coeffs& c, uint32_t band, float mu) {
+    if (c.scattering <= 0.0f) return 0.0f;
+    return mixed_phase_u(S, c, band, mu, phase_grid_u(mu));
 }
 
 // phase.rs:137-140
@@ -336,17 +348,16 @@ __device__ __forceinline__ float mu_edge(uint32_t edge, uint32_t bins) {
     return 1.0f - 2.0f * u * u * u;
 }
 
-// MiePhaseTable::sample_mu_pdf (phase.rs:53-69): binary search of the CDF.
+// MiePhaseTable::sample_mu_pdf (phase.rs:53-69): the first CDF entry above
+// xi (a binary search of the row in the reference), found by a forward scan
+// from the guide table's lower bound for xi's 1/bins cell.
 __device__ __forceinline__ float sample_mie_mu(const DevScene& S, uint32_t species, uint32_t band, float xi) {
     uint32_t bins = S.phase_bins;
-    const float* cdf = S.phase_cdf + (size_t(species) * S.band_count + band) * bins;
+    const size_t row = (size_t(species) * S.band_count + band) * bins;
+    const float* cdf = S.phase_cdf + row;
     xi = fminf(fmaxf(xi, 0.0f), 1.0f - kF32Epsilon);
-    uint32_t lo = 0, hi = bins;  // first index with cdf > xi
-    while (lo < hi) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(cdf + mid) <= xi) lo = mid + 1u;
-        else hi = mid;
-    }
+    uint32_t lo = __ldg(S.phase_guide + row + min(uint32_t(xi * float(bins)), bins - 1u));
+    while (lo < bins && __ldg(cdf + lo) <= xi) ++lo;
     uint32_t bin = min(lo, bins - 1u);
     float prev = bin == 0u ? 0.0f : __ldg(cdf + bin - 1u);
     float next = __ldg(cdf + bin);
@@ -355,10 +366,9 @@ __device__ __forceinline__ float sample_mie_mu(const DevScene& S, uint32_t speci
     return e0 * (1.0f - t) + e1 * t;
 }
 
-// MiePhaseTable::sampling_pdf (phase.rs:71-75, mu_to_bin :142-146)
-__device__ __forceinline__ float mie_sampling_pdf(const DevScene& S, uint32_t species, uint32_t band, float mu) {
+// MiePhaseTable::sampling_pdf (phase.rs:71-75, mu_to_bin :142-146), at grid position u.
+__device__ __forceinline__ float mie_sampling_pdf_u(const DevScene& S, uint32_t species, uint32_t band, float u) {
     uint32_t bins = S.phase_bins;
-    float u = cbrt_pos((1.0f - fminf(fmaxf(mu, -1.0f), 1.0f)) * 0.5f);
     uint32_t bin = min(uint32_t(floorf(u * float(bins))), bins - 1u);
     return fmaxf(__ldg(S.phase_bin_pdf + (size_t(species) * S.band_count + band) * bins + bin), 1.0e-12f);
 }
@@ -460,11 +470,12 @@ __device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeff
     float xi_phi = rng.next();
     out_dir = direction_from_axis_mu(axis, mu, xi_phi);
     float inv_s = 1.0f / c.scattering;
+    const float u = phase_grid_u(mu);  // shared by the pdf and the phase lookups
     float pdf = c.rayleigh * inv_s * rayleigh_phase(mu);
 #pragma unroll
     for (int i = 0; i < int(kSpecies); ++i)
-        if (c.sca[i] > 0.0f) pdf = fmaf(c.sca[i] * inv_s, mie_sampling_pdf(S, uint32_t(i), band, mu), pdf);
-    return mixed_phase(S, c, band, mu) / pdf;
+        if (c.sca[i] > 0.0f) pdf = fmaf(c.sca[i] * inv_s, mie_sampling_pdf_u(S, uint32_t(i), band, u), pdf);
+    return mixed_phase_u(S, c, band, mu, u) / pdf;
 }
 
 // ---- cameras (sky_trace.wgsl:610-689) --------------------------------------------------

@@ -69,7 +69,7 @@ struct DevScene {
     float cos_max;           // cos(sun angular radius)
     float one_minus_cos_max;
     float light_pdf;         // 1 / (2 pi (1 - cos_max))
-    uint32_t mie_mask;       // bit i set when species i scatters in some band
+    uint32_t aerosol_mask;   // bit i set when species i has mass and optics: the others add exactly 0
     // device tables
     const float* knot_z;               // [K]
     const uint16_t* finder;            // [kFinderCells] knot interval of each cell's lower edge
@@ -81,6 +81,7 @@ struct DevScene {
     const float* phase_values;         // [species][B][bins]
     const float* phase_cdf;            // [species][B][bins]
     const float* phase_bin_pdf;        // [species][B][bins]
+    const uint16_t* phase_guide;       // [species][B][bins]: search start of the CDF inversion
     // Merged tracking grid (SKY_TRACKING_MERGED_LAYERS): per band, the
     // merged layers' shell radii, majorants, and the map from a uniform
     // majorant layer to the merged layer that contains it.
