@@ -216,6 +216,11 @@ typedef struct SkyRenderStats {
  *   xyz_var    [pixels][3]      variance of that XYZ estimate (FP64)
  *   counters   [SKY_EVENT_COUNT] event counts, added to (not overwritten)
  *   status     [1]              nonzero after a watchdog; left for the caller
+ *   rgb        [pixels][3]      linear sRGB of that XYZ after the Bradford
+ *                               solar-white-to-D65 white balance, non-finite
+ *                               values as 0 (SpectralRgbConverter::new_solar_d65
+ *                               and to_linear_srgb, spectrum.rs:132-165)
+ * xyz, xyz_var and rgb need the scene's band_xyz_weights.
  */
 typedef struct SkyDeviceOutputs {
     double* cell_sum;
@@ -225,6 +230,7 @@ typedef struct SkyDeviceOutputs {
     double* xyz_var;
     unsigned long long* counters;
     uint32_t* status;
+    float* rgb;
 } SkyDeviceOutputs;
 
 /*
@@ -289,6 +295,15 @@ int sky_cuda_render_xyz(const SkyScene* scene, const SkyRenderConfig* config,
  * renders, copies the film back and frees the device tables, all inside the
  * call (integrator.rs:125-317).
  */
+/*
+ * Film and per-pixel linear sRGB (white-balanced as in SkyDeviceOutputs.rgb)
+ * to host buffers: what sky-reference-render writes to its band EXRs and its
+ * RGB EXR/PNG (film_output.rs:12-124).  film_out may be NULL.
+ */
+int sky_cuda_render_rgb(const SkyScene* scene, const SkyRenderConfig* config,
+                        float* film_out, size_t film_len,
+                        float* rgb_out, size_t pixel_count, SkyRenderStats* stats);
+
 int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config,
                          float* film_out, size_t film_len, SkyRenderStats* stats);
 

@@ -4,7 +4,8 @@
 // variance of that XYZ estimate from the per-band sums of squares.
 //
 // One warp per pixel: lanes stride over the bands (coalesced film stores),
-// then a shuffle reduction forms XYZ and its variance.
+// then a shuffle reduction forms XYZ and its variance, and the white-balanced
+// linear sRGB of that XYZ (film_output.rs:96-124 on the host in the reference).
 
 #include "trace_kernels.h"
 
@@ -22,7 +23,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevBand* __restrict
                                                        const double* __restrict__ cell_sum,
                                                        const double* __restrict__ cell_sumsq,
                                                        float* __restrict__ film, double* __restrict__ xyz,
-                                                       double* __restrict__ xyz_var) {
+                                                       double* __restrict__ xyz_var, float* __restrict__ rgb,
+                                                       RgbMatrix m) {
     const uint64_t pixel = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const uint32_t lane = threadIdx.x & 31u;
     if (pixel >= pixels) return;
@@ -57,19 +59,21 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevBand* __restrict
             for (int c = 0; c < 3; ++c) xyz[pixel * 3 + c] = acc[c];
         if (xyz_var)
             for (int c = 0; c < 3; ++c) xyz_var[pixel * 3 + c] = var[c];
+        if (rgb) store_rgb(m, acc, rgb + pixel * 3);
     }
 }
 
 }  // namespace
 
 cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_spp, const double* cell_sum,
-                            const double* cell_sumsq, float* film, double* xyz, double* xyz_var,
+                            const double* cell_sumsq, float* film, double* xyz, double* xyz_var, float* rgb,
                             cudaStream_t stream) {
-    if (!film && !xyz && !xyz_var) return cudaSuccess;
+    if (!film && !xyz && !xyz_var && !rgb) return cudaSuccess;
     const uint32_t block = 256;
     const uint64_t blocks = (pixels * 32u + block - 1) / block;
     finalize_kernel<<<dim3(uint32_t(blocks)), block, 0, stream>>>(S.bands, S.band_count, pixels, total_spp, cell_sum,
-                                                                 cell_sumsq, film, xyz, xyz_var);
+                                                                 cell_sumsq, film, xyz, xyz_var, rgb,
+                                                                 rgb_matrix(S));
     return cudaGetLastError();
 }
 

@@ -65,6 +65,55 @@ bool finite_all(const float* v, size_t n) {
 
 }  // namespace
 
+// ---- colorimetry: spectrum.rs:13-19, :84-109, :132-165, :297-351 ----------------------
+//
+// Standard published matrices: linear sRGB from XYZ (D65), the Bradford cone
+// response and its inverse, the D65 white at Y = 1.
+namespace {
+using Mat3f = float[3][3];
+constexpr float kSrgbFromXyz[3][3] = {{3.2404542f, -1.5371385f, -0.4985314f},
+                                      {-0.969266f, 1.8760108f, 0.041556f},
+                                      {0.0556434f, -0.2040259f, 1.0572252f}};
+constexpr float kBradfordLmsFromXyz[3][3] = {{0.8951f, 0.2664f, -0.1614f},
+                                             {-0.7502f, 1.7135f, 0.0367f},
+                                             {0.0389f, -0.0685f, 1.0296f}};
+constexpr float kXyzFromBradfordLms[3][3] = {{0.9869929f, -0.1470543f, 0.1599627f},
+                                             {0.4323053f, 0.5183603f, 0.0492912f},
+                                             {-0.0085287f, 0.0400428f, 0.9684867f}};
+constexpr float kD65WhiteY1[3] = {0.9504559f, 1.0f, 1.0890578f};
+
+void mat3_vec(const float m[3][3], const float v[3], float out[3]) {
+    for (int r = 0; r < 3; ++r) out[r] = m[r][0] * v[0] + m[r][1] * v[1] + m[r][2] * v[2];
+}
+void mat3_mul(const float a[3][3], const float b[3][3], float out[3][3]) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[r][c] = a[r][0] * b[0][c] + a[r][1] * b[1][c] + a[r][2] * b[2][c];
+}
+void normalized_to_y1(const float v[3], float out[3]) {
+    if (std::fabs(v[1]) <= 1.1920929e-7f) {
+        for (int i = 0; i < 3; ++i) out[i] = kD65WhiteY1[i];
+        return;
+    }
+    const float inv = 1.0f / v[1];
+    out[0] = v[0] * inv;
+    out[1] = 1.0f;
+    out[2] = v[2] * inv;
+}
+}  // namespace
+
+void solar_d65_white_balance(const float* solar, const float* band_xyz, uint32_t bands, float wb[3][3]) {
+    float white[3] = {0.0f, 0.0f, 0.0f};  // spectrum_to_xyz_with_weights of the solar spectrum
+    for (uint32_t b = 0; b < bands; ++b)
+        for (int c = 0; c < 3; ++c) white[c] += solar[b] * band_xyz[b * 3 + c];
+    float src[3], s_lms[3], t_lms[3], scale[3][3] = {}, tmp[3][3];
+    normalized_to_y1(white, src);
+    mat3_vec(kBradfordLmsFromXyz, src, s_lms);
+    mat3_vec(kBradfordLmsFromXyz, kD65WhiteY1, t_lms);
+    for (int i = 0; i < 3; ++i) scale[i][i] = std::fabs(s_lms[i]) > 1.0e-12f ? t_lms[i] / s_lms[i] : 1.0f;
+    mat3_mul(scale, kBradfordLmsFromXyz, tmp);
+    mat3_mul(kXyzFromBradfordLms, tmp, wb);
+}
+
 void host_orthonormal_basis(const float n_in[3], float t[3], float b[3]) {
     float len = std::sqrt(n_in[0] * n_in[0] + n_in[1] * n_in[1] + n_in[2] * n_in[2]);
     float n[3] = {0.0f, 1.0f, 0.0f};
@@ -320,6 +369,15 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
                          d->sun_direction[2] * d->sun_direction[2]);
     for (int i = 0; i < 3; ++i) S.sun[i] = sl > 0.0f ? d->sun_direction[i] / sl : (i == 1 ? 1.0f : 0.0f);
     host_orthonormal_basis(S.sun, S.sun_t, S.sun_b);
+    if (out.has_xyz) {  // rgb = sRGB * (white balance * xyz), folded into one matrix
+        std::vector<float> solar(B);
+        for (uint32_t b = 0; b < B; ++b) solar[b] = d->bands[b].solar_radiance_w_m2_sr;
+        float wb[3][3], m[3][3];
+        solar_d65_white_balance(solar.data(), d->band_xyz_weights, B, wb);
+        mat3_mul(kSrgbFromXyz, wb, m);
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) S.rgb_from_xyz[r * 3 + c] = m[r][c];
+    }
     S.cos_max = std::cos(d->sun_angular_radius_rad);
     S.one_minus_cos_max = 1.0f - S.cos_max;
     S.light_pdf = 1.0f / (kTauF * (1.0f - S.cos_max));

@@ -51,4 +51,9 @@ void build_phase_sampling_tables(const float* values, uint32_t band_count, uint3
 // orthonormal_basis (sky_trace.wgsl:512-520) evaluated on the host.
 void host_orthonormal_basis(const float n_in[3], float t[3], float b[3]);
 
+// Bradford white balance from the solar spectrum's white to D65
+// (SpectralRgbConverter::new_solar_d65, spectrum.rs:132-147): a 3x3 XYZ->XYZ
+// matrix from per-band solar values and CIE weights [bands][3].
+void solar_d65_white_balance(const float* solar, const float* band_xyz, uint32_t bands, float wb[3][3]);
+
 }  // namespace sky

@@ -38,6 +38,7 @@ struct SkyScene {
     float* ws_film = nullptr;
     double* ws_xyz = nullptr;
     double* ws_xyz_var = nullptr;
+    float* ws_rgb = nullptr;
     unsigned long long* ws_counters = nullptr;
     uint32_t* ws_status = nullptr;
     uint64_t ws_cells = 0, ws_pixels = 0;
@@ -86,6 +87,8 @@ void free_workspace(SkyScene* s) {
     cudaFree(s->ws_film);
     cudaFree(s->ws_xyz);
     cudaFree(s->ws_xyz_var);
+    cudaFree(s->ws_rgb);
+    s->ws_rgb = nullptr;
     cudaFree(s->ws_counters);
     cudaFree(s->ws_status);
     s->ws_sum = s->ws_sumsq = nullptr;
@@ -106,6 +109,7 @@ int ensure_workspace(SkyScene* s, uint64_t pixels) {
         (e = cudaMalloc(&s->ws_film, cells * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc(&s->ws_xyz, pixels * 3 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&s->ws_xyz_var, pixels * 3 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&s->ws_rgb, pixels * 3 * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc(&s->ws_counters, SKY_EVENT_COUNT * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMalloc(&s->ws_status, sizeof(uint32_t))) != cudaSuccess) {
         free_workspace(s);
@@ -204,12 +208,14 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     const uint32_t total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
     double* xyz = s->has_xyz ? o->xyz : nullptr;
     double* xyz_var = s->has_xyz ? o->xyz_var : nullptr;
+    float* rgb = s->has_xyz ? o->rgb : nullptr;
     if (c->kernel == SKY_KERNEL_PLAIN) {
         if (timed) cudaEventRecord(s->ev_start, stream);
         e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate, stream);
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "tracing kernel launch", e);
         if (timed) cudaEventRecord(s->ev_stop, stream);
-        e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, stream);
+        e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, rgb,
+                            stream);
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
         return SKY_OK;
     }
@@ -222,6 +228,7 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     job.film = o->film;
     job.xyz = xyz;
     job.xyz_var = xyz_var;
+    job.rgb = rgb;
     job.accumulate = accumulate ? 1u : 0u;
     job.total_spp = total_spp;
     job.pixels_per_group = s->tuning.pixels_per_group
@@ -257,7 +264,7 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
 
 // Synchronous render into the scene workspace, with host copies.
 int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t film_len, double* xyz_out,
-                double* xyz_var_out, size_t pixel_count, SkyRenderStats* stats) {
+                double* xyz_var_out, size_t pixel_count, SkyRenderStats* stats, float* rgb_out = nullptr) {
     auto t0 = std::chrono::steady_clock::now();
     int st = validate_config(s, c);
     if (st) return st;
@@ -265,9 +272,9 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
     const uint64_t cells = pixels * s->dev.band_count;
     if (film_out && film_len < cells)
         return set_error(SKY_ERR_INVALID_CONFIG, "film buffer is smaller than width*height*bands");
-    if ((xyz_out || xyz_var_out) && pixel_count < pixels)
-        return set_error(SKY_ERR_INVALID_CONFIG, "xyz buffer is smaller than width*height");
-    if ((xyz_out || xyz_var_out) && !s->has_xyz)
+    if ((xyz_out || xyz_var_out || rgb_out) && pixel_count < pixels)
+        return set_error(SKY_ERR_INVALID_CONFIG, "xyz / rgb buffer is smaller than width*height");
+    if ((xyz_out || xyz_var_out || rgb_out) && !s->has_xyz)
         return set_error(SKY_ERR_INVALID_CONFIG, "scene has no band_xyz_weights");
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
     if ((st = ensure_workspace(s, pixels))) return st;
@@ -276,7 +283,8 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
     if (e == cudaSuccess) e = cudaMemsetAsync(s->ws_status, 0, sizeof(uint32_t), s->stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "clearing counters", e);
     SkyDeviceOutputs o{s->ws_sum, s->ws_sumsq, film_out ? s->ws_film : nullptr, xyz_out ? s->ws_xyz : nullptr,
-                       xyz_var_out ? s->ws_xyz_var : nullptr, s->ws_counters, s->ws_status};
+                       xyz_var_out ? s->ws_xyz_var : nullptr, s->ws_counters, s->ws_status,
+                       rgb_out ? s->ws_rgb : nullptr};
     if ((st = launch_render(s, c, &o, s->stream, true))) return st;
     uint32_t status = 0;
     unsigned long long counters[SKY_EVENT_COUNT] = {};
@@ -289,6 +297,9 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
     if (xyz_var_out && (e = cudaMemcpyAsync(xyz_var_out, s->ws_xyz_var, pixels * 3 * sizeof(double),
                                             cudaMemcpyDeviceToHost, s->stream)))
         return cuda_fail(SKY_ERR_COPY, "xyz variance readback", e);
+    if (rgb_out &&
+        (e = cudaMemcpyAsync(rgb_out, s->ws_rgb, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, s->stream)))
+        return cuda_fail(SKY_ERR_COPY, "rgb readback", e);
     if ((e = cudaMemcpyAsync(counters, s->ws_counters, sizeof(counters), cudaMemcpyDeviceToHost, s->stream)) ||
         (e = cudaMemcpyAsync(&status, s->ws_status, sizeof(status), cudaMemcpyDeviceToHost, s->stream)))
         return cuda_fail(SKY_ERR_COPY, "diagnostics readback", e);
@@ -556,6 +567,13 @@ int sky_cuda_render_xyz(const SkyScene* scene, const SkyRenderConfig* config, fl
                        stats);
 }
 
+int sky_cuda_render_rgb(const SkyScene* scene, const SkyRenderConfig* config, float* film_out, size_t film_len,
+                        float* rgb_out, size_t pixel_count, SkyRenderStats* stats) {
+    if (!rgb_out) return set_error(SKY_ERR_INVALID_CONFIG, "rgb_out is null");
+    return render_host(const_cast<SkyScene*>(scene), config, film_out, film_len, nullptr, nullptr, pixel_count, stats,
+                       rgb_out);
+}
+
 int sky_cuda_render_desc(const SkySceneDesc* desc, const SkyRenderConfig* config, float* film_out, size_t film_len,
                          SkyRenderStats* stats) {
     SkyScene* s = nullptr;
@@ -632,6 +650,7 @@ int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* o
         job.film = jobs[i].outputs.film;
         job.xyz = s->has_xyz ? jobs[i].outputs.xyz : nullptr;
         job.xyz_var = s->has_xyz ? jobs[i].outputs.xyz_var : nullptr;
+        job.rgb = s->has_xyz ? jobs[i].outputs.rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
         job.pixels_per_group = s->tuning.pixels_per_group ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
@@ -875,7 +894,8 @@ extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderCo
                               outputs->status, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
     e = launch_finalize(A.S, pixels, total_spp, outputs->cell_sum, outputs->cell_sumsq, outputs->film,
-                        s->has_xyz ? outputs->xyz : nullptr, s->has_xyz ? outputs->xyz_var : nullptr, stream);
+                        s->has_xyz ? outputs->xyz : nullptr, s->has_xyz ? outputs->xyz_var : nullptr,
+                        s->has_xyz ? outputs->rgb : nullptr, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
     return SKY_OK;
 }
@@ -1000,6 +1020,7 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
         job.film = outputs[i].film;
         job.xyz = s->has_xyz ? outputs[i].xyz : nullptr;
         job.xyz_var = s->has_xyz ? outputs[i].xyz_var : nullptr;
+        job.rgb = s->has_xyz ? outputs[i].rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
         job.pixels_per_group = s->tuning.pixels_per_group

@@ -92,6 +92,9 @@ struct DevScene {
     const uint32_t* trk_off;           // [B]: row offset of the band in trk_radius / trk_maj
     uint32_t trk_total;                // entries in trk_radius / trk_maj
     float inv_layer_dz;                // layers / top
+    // linear sRGB from XYZ: the sRGB matrix times the Bradford solar-white-to-
+    // D65 white balance (row-major; zero when the scene has no XYZ weights)
+    float rgb_from_xyz[9];
 };
 
 // Per-launch constants.
@@ -127,6 +130,7 @@ struct DevJob {
     float* film;
     double* xyz;
     double* xyz_var;
+    float* rgb;
     uint32_t accumulate;
     uint32_t total_spp;         // samples behind the sums after this launch
     uint32_t pixels_per_group;

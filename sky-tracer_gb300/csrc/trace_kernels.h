@@ -48,10 +48,32 @@ cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream);
 PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables, uint32_t variant);
 uint32_t pool_slots_per_thread(uint32_t variant);
 
-// Mean film, XYZ and XYZ variance from the per-cell sums (any output may be
-// null; xyz_var needs cell_sumsq).
+// Mean film, XYZ, XYZ variance and linear sRGB from the per-cell sums (any
+// output may be null; xyz_var needs cell_sumsq).
 cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_spp, const double* cell_sum,
-                            const double* cell_sumsq, float* film, double* xyz, double* xyz_var,
+                            const double* cell_sumsq, float* film, double* xyz, double* xyz_var, float* rgb,
                             cudaStream_t stream);
+
+// XYZ -> white-balanced linear sRGB of a scene (kernel argument copy).
+struct RgbMatrix {
+    float m[9];
+};
+__host__ __device__ inline RgbMatrix rgb_matrix(const DevScene& S) {
+    RgbMatrix r;
+    for (int i = 0; i < 9; ++i) r.m[i] = S.rgb_from_xyz[i];
+    return r;
+}
+
+// rgb = M xyz in FP64, stored as float; black when any component is not
+// finite (Rgb::finite_or_black, math.rs:137-143).
+__device__ __forceinline__ void store_rgb(const RgbMatrix& M, const double xyz[3], float* out) {
+    float f[3];
+    bool finite = true;
+    for (int r = 0; r < 3; ++r) {
+        f[r] = float(double(M.m[r * 3]) * xyz[0] + double(M.m[r * 3 + 1]) * xyz[1] + double(M.m[r * 3 + 2]) * xyz[2]);
+        finite = finite && isfinite(f[r]);
+    }
+    for (int r = 0; r < 3; ++r) out[r] = finite ? f[r] : 0.0f;
+}
 
 }  // namespace sky

@@ -510,19 +510,20 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) pool_kernel(const DevJob
                         var[ch] += var_mean * w * w;
                     }
                 }
-                if (J.xyz || J.xyz_var) {
+                if (J.xyz || J.xyz_var || J.rgb) {
 #pragma unroll
                     for (int ch = 0; ch < 3; ++ch) {
                         xyz[ch] = warp_sum_d(xyz[ch]);
                         var[ch] = warp_sum_d(var[ch]);
                     }
+                    const unsigned long long pix = R.pixel0 + px;
                     if (lane < 3u) {
                         const double vx = lane == 0 ? xyz[0] : (lane == 1 ? xyz[1] : xyz[2]);
                         const double vv = lane == 0 ? var[0] : (lane == 1 ? var[1] : var[2]);
-                        const unsigned long long pix = R.pixel0 + px;
                         if (J.xyz) J.xyz[pix * 3 + lane] = vx;
                         if (J.xyz_var) J.xyz_var[pix * 3 + lane] = vv;
                     }
+                    if (J.rgb && lane == 0) store_rgb(rgb_matrix(J.S), xyz, J.rgb + pix * 3);
                 }
             }
             __syncthreads();

@@ -99,7 +99,7 @@ class SkyRenderStats(ctypes.Structure):
 class SkyDeviceOutputs(ctypes.Structure):
     _fields_ = [
         ("cell_sum", _vp), ("cell_sumsq", _vp), ("film", _vp), ("xyz", _vp), ("xyz_var", _vp),
-        ("counters", _vp), ("status", _vp),
+        ("counters", _vp), ("status", _vp), ("rgb", _vp),
     ]
 
 
@@ -149,6 +149,8 @@ _SIGNATURES = {
                                        ctypes.POINTER(SkyRenderStats)]),
     "sky_cuda_render_xyz": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
+    "sky_cuda_render_rgb": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig), _fp, ctypes.c_size_t, _fp,
                                            ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),
     "sky_cuda_render_desc": (ctypes.c_int, [ctypes.POINTER(SkySceneDesc), ctypes.POINTER(SkyRenderConfig), _fp,
                                             ctypes.c_size_t, ctypes.POINTER(SkyRenderStats)]),

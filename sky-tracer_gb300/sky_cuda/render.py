@@ -166,6 +166,19 @@ class GpuScene:
         f = Film(config.width, config.height, self.band_count, film) if film is not None else None
         return f, xyz, var, RenderStats.from_c(stats)
 
+    def render_rgb(self, config: RenderConfig, with_film: bool = True):
+        """Film and per-pixel white-balanced linear sRGB [pixels, 3] (float32,
+        from the kernel epilogue), and stats."""
+        film = np.empty(config.pixels * self.band_count, dtype=np.float32) if with_film else None
+        rgb = np.empty((config.pixels, 3), dtype=np.float32)
+        stats = SkyRenderStats()
+        check(self.lib.sky_cuda_render_rgb(self.handle, ctypes.byref(config.to_c()),
+                                           _fptr(film) if film is not None else None,
+                                           film.size if film is not None else 0, _fptr(rgb), config.pixels,
+                                           ctypes.byref(stats)), self.lib)
+        f = Film(config.width, config.height, self.band_count, film) if film is not None else None
+        return f, rgb, RenderStats.from_c(stats)
+
     def render_batch(self, jobs, stream: int = 0) -> None:
         """One persistent launch over [(RenderConfig, sun_direction or None, outputs), ...]."""
         arr = batch_jobs(jobs)
