@@ -454,6 +454,32 @@ int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderConfig* conf
 int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* params, float* majorants_out,
                             void* cuda_stream);
 
+/* ---- Optimizer scoring --------------------------------------------------- */
+
+/*
+ * The wavelength optimizer's score of primary-band combinations
+ * (sky-wavelength-optimizer/src/main.rs:414-488, 1121-1156), on the GPU.
+ * Combination c rebuilds each sample's XYZ as
+ *     xyz[s] = sum_ch bands[combo_bands[c][ch]][s] * combo_xyz[c][ch]
+ * (combo_xyz = the channel's quadrature weight / band width * CIE at its
+ * centre), maps it and the reference to Oklab after dividing by
+ * reference_scale, and summarises the per-sample distances: mean, rmse, the
+ * order statistics p50/p90/p95/p99 (element round((n - 1) q) of the sorted
+ * finite distances, exact) and the maximum; score = rmse + 0.25 p95.
+ *   bands      device, float [band_count][samples]
+ *   ref_oklab  device, float [samples][3]: Oklab of reference XYZ / scale
+ *   combo_bands, combo_xyz   host, [combo_count][channels] and [..][3]
+ *   results    host, [combo_count]
+ * Synchronous on `cuda_stream`; device scratch is allocated per call.
+ */
+typedef struct SkyComboScore {
+    double mean, rmse, p50, p90, p95, p99, max, score;
+    uint64_t finite;  /* samples with a finite distance */
+} SkyComboScore;
+int sky_cuda_score_combos(const float* bands, uint32_t band_count, uint64_t samples, const float* ref_oklab,
+                          float reference_scale, const uint32_t* combo_bands, const float* combo_xyz,
+                          uint32_t combo_count, uint32_t channels, SkyComboScore* results, void* cuda_stream);
+
 /*
  * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
  * single launch of the persistent tracer.  No counterpart in the reference.

@@ -21,6 +21,7 @@
 #include "../../include/sky_cuda.h"
 #include "adjoint_kernels.h"
 #include "scene_build.h"
+#include "score_kernels.h"
 #include "trace_kernels.h"
 
 using namespace sky;
@@ -949,6 +950,136 @@ extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointPa
     e = cudaMemcpyAsync(majorants_out, W.layer_maj, size_t(s->dev.band_count) * s->dev.layer_count * sizeof(float),
                         cudaMemcpyDeviceToDevice, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "majorant copy", e);
+    return SKY_OK;
+}
+
+// ---- optimizer scoring ---------------------------------------------------------------
+
+namespace {
+
+struct DeviceScratch {  // frees what it allocated when the call returns
+    std::vector<void*> ptrs;
+    ~DeviceScratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <class T>
+    cudaError_t alloc(T** out, size_t count) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) ptrs.push_back(p);
+        *out = static_cast<T*>(p);
+        return e;
+    }
+};
+
+}  // namespace
+
+extern "C" int sky_cuda_score_combos(const float* bands, uint32_t band_count, uint64_t samples,
+                                     const float* ref_oklab, float reference_scale, const uint32_t* combo_bands,
+                                     const float* combo_xyz, uint32_t combo_count, uint32_t channels,
+                                     SkyComboScore* results, void* cuda_stream) {
+    if (!bands || !ref_oklab || !combo_bands || !combo_xyz || !results)
+        return set_error(SKY_ERR_INVALID_CONFIG, "bands, ref_oklab, combos and results are required");
+    if (samples == 0 || band_count == 0 || channels == 0 || combo_count == 0)
+        return set_error(SKY_ERR_INVALID_CONFIG, "samples, band_count, channels and combo_count must be positive");
+    if (!(reference_scale > 0.0f) || !std::isfinite(reference_scale))
+        return set_error(SKY_ERR_INVALID_CONFIG, "reference_scale must be positive and finite");
+    for (size_t i = 0; i < size_t(combo_count) * channels; ++i)
+        if (combo_bands[i] >= band_count) return set_error(SKY_ERR_INVALID_CONFIG, "combo band index out of range");
+    int device = 0, sms = 1;
+    if (cudaGetDevice(&device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "no usable CUDA device");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    // combinations per pass: distances of at most 2^28 (1 GB) and 8192 combinations
+    const uint32_t chunk =
+        uint32_t(std::max<uint64_t>(1, std::min<uint64_t>({combo_count, 8192u, (1ull << 28) / samples})));
+    constexpr uint32_t kTargets = 5;  // p50, p90, p95, p99, max
+    const double quantiles[kTargets] = {0.50, 0.90, 0.95, 0.99, 1.0};
+    DeviceScratch mem;
+    float* dist;
+    double* sums;
+    uint32_t *d_bands, *d_tcombo, *d_tprefix, *d_hist;
+    float* d_xyz;
+    cudaError_t e;
+    if ((e = mem.alloc(&dist, size_t(chunk) * samples)) || (e = mem.alloc(&sums, size_t(chunk) * 3)) ||
+        (e = mem.alloc(&d_bands, size_t(chunk) * channels)) || (e = mem.alloc(&d_xyz, size_t(chunk) * channels * 3)) ||
+        (e = mem.alloc(&d_tcombo, size_t(chunk) * kTargets)) || (e = mem.alloc(&d_tprefix, size_t(chunk) * kTargets)) ||
+        (e = mem.alloc(&d_hist, size_t(chunk) * kTargets * kScoreHistBins)))
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "scoring scratch allocation", e);
+    std::vector<double> h_sums(size_t(chunk) * 3);
+    std::vector<uint32_t> h_hist(size_t(chunk) * kTargets * kScoreHistBins), tcombo(size_t(chunk) * kTargets),
+        tprefix(size_t(chunk) * kTargets);
+    std::vector<uint64_t> rank(size_t(chunk) * kTargets);
+    for (uint32_t c0 = 0; c0 < combo_count; c0 += chunk) {
+        const uint32_t nc = std::min(chunk, combo_count - c0);
+        if ((e = cudaMemcpyAsync(d_bands, combo_bands + size_t(c0) * channels, size_t(nc) * channels * 4,
+                                 cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemcpyAsync(d_xyz, combo_xyz + size_t(c0) * channels * 3, size_t(nc) * channels * 12,
+                                 cudaMemcpyHostToDevice, stream)) ||
+            (e = cudaMemsetAsync(sums, 0, size_t(nc) * 3 * sizeof(double), stream)))
+            return cuda_fail(SKY_ERR_COPY, "scoring upload", e);
+        if ((e = launch_score_distances(bands, samples, ref_oklab, 1.0f / reference_scale, d_bands, d_xyz, nc,
+                                        channels, dist, sums, stream)))
+            return cuda_fail(SKY_ERR_LAUNCH, "distance kernel launch", e);
+        if ((e = cudaMemcpyAsync(h_sums.data(), sums, size_t(nc) * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 stream)) ||
+            (e = cudaStreamSynchronize(stream)))
+            return cuda_fail(SKY_ERR_SYNC, "distance sums", e);
+        uint32_t targets = 0;
+        for (uint32_t c = 0; c < nc; ++c) {
+            const uint64_t n = uint64_t(h_sums[c * 3 + 2] + 0.5);
+            SkyComboScore& r = results[c0 + c];
+            r = SkyComboScore{};
+            r.finite = n;
+            if (n == 0) {
+                r.mean = r.rmse = r.p50 = r.p90 = r.p95 = r.p99 = r.max = r.score = std::nan("");
+                continue;
+            }
+            r.mean = h_sums[c * 3] / double(n);
+            r.rmse = std::sqrt(h_sums[c * 3 + 1] / double(n));
+            for (uint32_t q = 0; q < kTargets; ++q) {  // percentile_sorted: round((n - 1) q), half away from 0
+                tcombo[targets] = c;
+                tprefix[targets] = 0;
+                rank[targets] = uint64_t(std::floor(double(n - 1) * quantiles[q] + 0.5));
+                ++targets;
+            }
+        }
+        // three radix-selection passes over the bits of the non-negative distances
+        const uint32_t shifts[3] = {21u, 10u, 0u}, widths[3] = {11u, 11u, 10u};
+        for (int pass = 0; pass < 3 && targets > 0; ++pass) {
+            if ((e = cudaMemcpyAsync(d_tcombo, tcombo.data(), targets * 4, cudaMemcpyHostToDevice, stream)) ||
+                (e = cudaMemcpyAsync(d_tprefix, tprefix.data(), targets * 4, cudaMemcpyHostToDevice, stream)) ||
+                (e = cudaMemsetAsync(d_hist, 0, size_t(targets) * kScoreHistBins * 4, stream)))
+                return cuda_fail(SKY_ERR_COPY, "selection upload", e);
+            if ((e = launch_select_hist(dist, samples, d_tcombo, d_tprefix, targets, shifts[pass], widths[pass], d_hist,
+                                        uint32_t(sms), stream)))
+                return cuda_fail(SKY_ERR_LAUNCH, "selection kernel launch", e);
+            if ((e = cudaMemcpyAsync(h_hist.data(), d_hist, size_t(targets) * kScoreHistBins * 4,
+                                     cudaMemcpyDeviceToHost, stream)) ||
+                (e = cudaStreamSynchronize(stream)))
+                return cuda_fail(SKY_ERR_SYNC, "selection histogram", e);
+            const uint32_t bins = 1u << widths[pass];
+            for (uint32_t t = 0; t < targets; ++t) {
+                const uint32_t* h = h_hist.data() + size_t(t) * kScoreHistBins;
+                uint64_t below = 0;
+                uint32_t b = 0;
+                for (; b + 1 < bins && below + h[b] <= rank[t]; ++b) below += h[b];
+                rank[t] -= below;
+                tprefix[t] = (tprefix[t] << widths[pass]) | b;
+            }
+        }
+        for (uint32_t t = 0; t < targets; ++t) {
+            float v;
+            std::memcpy(&v, &tprefix[t], 4);
+            SkyComboScore& r = results[c0 + tcombo[t]];
+            double* slot[kTargets] = {&r.p50, &r.p90, &r.p95, &r.p99, &r.max};
+            *slot[t % kTargets] = double(v);
+        }
+        for (uint32_t c = 0; c < nc; ++c) {
+            SkyComboScore& r = results[c0 + c];
+            if (r.finite) r.score = r.rmse + 0.25 * r.p95;
+        }
+    }
     return SKY_OK;
 }
 

@@ -129,6 +129,11 @@ class SkyAdjointGrads(ctypes.Structure):
     ]
 
 
+class SkyComboScore(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("mean", "rmse", "p50", "p90", "p95", "p99", "max", "score")] + [
+        ("finite", ctypes.c_uint64)]
+
+
 ADJOINT_BAND_PARAMS = 4
 ADJOINT_SEGMENT_INTEGRALS = 0
 ADJOINT_NULL_COLLISIONS = 1
@@ -169,6 +174,9 @@ _SIGNATURES = {
                                                  ctypes.POINTER(SkyAdjointParams), ctypes.POINTER(SkyAdjointGrads),
                                                  _vp]),
     "sky_cuda_bake_majorants": (ctypes.c_int, [_vp, ctypes.POINTER(SkyAdjointParams), _vp, _vp]),
+    "sky_cuda_score_combos": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, ctypes.c_float,
+                                             ctypes.POINTER(ctypes.c_uint32), _fp, ctypes.c_uint32, ctypes.c_uint32,
+                                             ctypes.POINTER(SkyComboScore), _vp]),
     "sky_cuda_render_batch_noalloc": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                                      ctypes.POINTER(SkyDeviceOutputs), ctypes.c_uint32, _vp]),
 }

@@ -106,6 +106,13 @@ def _percentile_sorted(values, q: float) -> float:
 
 
 def oklab_score(xyz, xyz_ref) -> dict:
+    """The reference optimizer's score of a reconstruction, on the GPU
+    (sky_cuda_score_combos; host restatement: oklab_score_host)."""
+    from .scoring import score_xyz
+    return score_xyz(xyz, xyz_ref)
+
+
+def oklab_score_host(xyz, xyz_ref) -> dict:
     """The reference optimizer's score of a reconstruction: XYZ / p99(Y_ref)
     to Oklab, per-sample distance, rmse, p50..p99 and rmse + 0.25 p95
     (evaluate_combo, main.rs:414-488)."""

@@ -8,7 +8,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from sky_cuda import synthetic_scene
-from sky_cuda.primaries import BandModel, oklab_score, xyz_to_oklab
+from sky_cuda.primaries import BandModel, oklab_score_host as oklab_score, xyz_to_oklab
 
 
 def test_band_multipliers_match_rebuilt_scenes(data_dir):
