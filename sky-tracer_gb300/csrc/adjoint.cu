@@ -571,13 +571,17 @@ __device__ __forceinline__ void flush_counters(const Counters& n, unsigned long 
 }
 
 // Primal: one warp per (pixel, band) cell, 32 samples per round, FP64 cell
-// sums in a fixed order (as the plain tracer).
-template <int kPhase>
+// sums in a fixed order (as the plain tracer).  chain_out, when given,
+// receives every chain's radiance at unit solar multiplier ([cell][sample]),
+// which the adjoint kernel replays against.
+template <int kPhase, bool kShared>
 __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_constant__ AdjCtx A,
-                                                             const __grid_constant__ DevLaunch L, double* __restrict__ cell_sum,
+                                                             const __grid_constant__ DevLaunch L,
+                                                             double* __restrict__ cell_sum,
                                                              double* __restrict__ cell_sumsq, uint32_t accumulate,
                                                              unsigned long long* __restrict__ counters,
-                                                             uint32_t* __restrict__ status, uint64_t cells) {
+                                                             uint32_t* __restrict__ status, uint64_t cells,
+                                                             float* __restrict__ chain_out) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
@@ -591,21 +595,26 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
     n.clear();
     bool watchdog = false;
     double sum = 0.0, sumsq = 0.0;
-    if (accumulate) {
+    if (accumulate && cell_sum) {
         sum = cell_sum[cell];
         if (cell_sumsq) sumsq = cell_sumsq[cell];
     }
     for (uint32_t base = 0; base < L.spp; base += 32u) {
         const uint32_t s = base + lane;
         float r = 0.0f;
-        if (s < L.spp)
-            r = P.kS * adj_chain<kPhase, false>(A, P, Q, L, x, y, band, L.sample_offset + s, false, 0.0f, 0.0f, acc, n,
-                                         watchdog);
-        const double rd = double(r);
-        sum += warp_sum_d(rd);
-        sumsq += warp_sum_d(rd * rd);
+        if (s < L.spp) {
+            const float unit = adj_chain<kPhase, kShared>(A, P, Q, L, x, y, band, L.sample_offset + s, false, 0.0f,
+                                                          0.0f, acc, n, watchdog);
+            if (chain_out) chain_out[cell * L.spp + s] = unit;
+            r = P.kS * unit;
+        }
+        if (cell_sum) {
+            const double rd = double(r);
+            sum += warp_sum_d(rd);
+            sumsq += warp_sum_d(rd * rd);
+        }
     }
-    if (lane == 0) {
+    if (cell_sum && lane == 0) {
         cell_sum[cell] = sum;
         if (cell_sumsq) cell_sumsq[cell] = sumsq;
     }
@@ -613,8 +622,8 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
 }
 
-// Adjoint: warps take cells one at a time; each chain is traced (pass 1) and
-// replayed (pass 2).  Layer gradients gather in shared memory (FP32, one copy
+// Adjoint: warps take cells one at a time and replay each chain against the
+// radiance the primal pass stored for it.  Layer gradients gather in shared memory (FP32, one copy
 // per warp when they fit, so that only a warp's own lanes contend), the
 // albedo, g and band gradients in registers reduced per cell; each block adds
 // its totals to the FP64 outputs once at the end.
@@ -626,7 +635,8 @@ __global__ void __launch_bounds__(256) adjoint_grad_kernel(const __grid_constant
                                                            double* __restrict__ band_grad,
                                                            unsigned long long* __restrict__ counters,
                                                            uint32_t* __restrict__ status, uint64_t cells,
-                                                           uint32_t copies, uint32_t* __restrict__ next_cell) {
+                                                           uint32_t copies, uint32_t* __restrict__ next_cell,
+                                                           const float* __restrict__ chain_in) {
     extern __shared__ float smem[];
     const uint32_t Lc = A.S.layer_count, B = A.S.band_count;
     const uint32_t nlayer = 3u * Lc + 2u;
@@ -657,18 +667,12 @@ __global__ void __launch_bounds__(256) adjoint_grad_kernel(const __grid_constant
         for (uint32_t base = 0; base < L.spp; base += 32u) {
             const uint32_t s = base + lane;
             if (s >= L.spp) continue;
-            // pass 0 traces the chain, pass 1 replays it: one call site, so
-            // lanes in different passes run the same instructions
-            float total = 0.0f;
-            for (int pass = 0; pass < 2; ++pass) {
-                const float r = adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, pass == 1, w, total,
-                                                  acc, n, watchdog);
-                if (pass == 0) {
-                    total = r;
-                    gS = fmaf(wcell, total, gS);
-                    if (!(total > 0.0f)) break;
-                }
-            }
+            // the chain's radiance from the primal pass, then its replay
+            const float total = __ldg(chain_in + cell * L.spp + s);
+            gS = fmaf(wcell, total, gS);
+            if (total > 0.0f)
+                adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, true, w, total, acc, n,
+                                        watchdog);
         }
         const float r = warp_sum_f(acc.gR), m = warp_sum_f(acc.gM), o = warp_sum_f(acc.gO), s = warp_sum_f(gS);
         const float gw = warp_sum_f(acc.gW), gg = warp_sum_f(acc.gG);
@@ -872,26 +876,38 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  cudaStream_t stream) {
+                                  cudaStream_t stream, float* chain_out) {
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
     const uint64_t blocks = (cells * 32u + 255u) / 256u;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     const dim3 grid(static_cast<uint32_t>(blocks));
     const uint32_t acc = accumulate ? 1u : 0u;
-    if (L.phase_sampling == SKY_PHASE_TABULATED)
-        adjoint_primal_kernel<SKY_PHASE_TABULATED>
-            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
-    else
-        adjoint_primal_kernel<SKY_PHASE_ISOTROPIC>
-            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+    // the pass before an adjoint uses the adjoint's out-of-line tracker, so
+    // that its chains are the ones the replay recomputes
+    if (L.phase_sampling == SKY_PHASE_TABULATED) {
+        if (chain_out)
+            adjoint_primal_kernel<SKY_PHASE_TABULATED, true>
+                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, chain_out);
+        else
+            adjoint_primal_kernel<SKY_PHASE_TABULATED, false>
+                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, nullptr);
+    } else {
+        if (chain_out)
+            adjoint_primal_kernel<SKY_PHASE_ISOTROPIC, true>
+                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, chain_out);
+        else
+            adjoint_primal_kernel<SKY_PHASE_ISOTROPIC, false>
+                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, nullptr);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
-                                uint32_t* next_cell, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream);
+                                uint32_t* next_cell, float* chains, cudaStream_t stream) {
+    cudaError_t e = launch_adjoint_primal(A, L, nullptr, nullptr, false, counters, status, stream, chains);
     if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
     const size_t nlayer = size_t(3u * A.S.layer_count + 2u), nband = size_t(kAdjBandParams) * A.S.band_count;
     // one layer-gradient copy per warp while it stays within the default 48 KB
@@ -903,13 +919,13 @@ cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
         adjoint_grad_kernel<SKY_PHASE_TABULATED><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
                                                                                 band_grad, counters, status, cells,
-                                                                                copies, next_cell);
+                                                                                copies, next_cell, chains);
     } else {
         const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
         adjoint_grad_kernel<SKY_PHASE_ISOTROPIC><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
                                                                                 band_grad, counters, status, cells,
-                                                                                copies, next_cell);
+                                                                                copies, next_cell, chains);
     }
     return cudaGetLastError();
 }
