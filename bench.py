@@ -433,7 +433,7 @@ def adjoint_report(args, steps, warmup, checks=True):
            "forward_ms": f_ms, "backward_ms": b_ms, "step_ms": f_ms + b_ms,
            "forward_chains_per_s": chains / (f_ms * 1e-3), "backward_chains_per_s": chains / (b_ms * 1e-3),
            "step_chains_per_s": chains / ((f_ms + b_ms) * 1e-3), "estimator": "segment integrals",
-           "gpu_launches_per_step": 6}
+           "gpu_launches_per_step": 5}
     if not checks:
         gs.close()
         return rep
@@ -542,7 +542,7 @@ def run_adjoint(args):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": ADJOINT_WORKLOAD, "width": 128, "height": 64, "wavelengths": 32, "spp": 64,
                       "l2": "tables < 1 MB; compute-bound"},
-           "adjoint": rep, "clocks": clocks.summary(), "gpu_launches": 6 * args.steps}
+           "adjoint": rep, "clocks": clocks.summary(), "gpu_launches": 5 * args.steps}
     print(json.dumps(out))
 
 

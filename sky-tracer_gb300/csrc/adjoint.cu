@@ -202,10 +202,10 @@ __device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_
 // the plain tracer with the parameterised medium).  w_eval collects the
 // null-collision ratios of P over Q; with gw != 0 and the null-collision
 // estimator every null collision adds gw * d log(mu_bar - sigma_t).
-__device__ __forceinline__ bool adj_track_body(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
-                                               const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
-                                               float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
-                                               bool& watchdog) {
+__device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
+                                          const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
+                                          float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
+                                          bool& watchdog) {
     const DevScene& S = A.S;
     const uint32_t L = S.layer_count;
     MergedGrid G;
@@ -258,26 +258,6 @@ __device__ __forceinline__ bool adj_track_body(const AdjCtx& A, const AdjSet& P,
     }
 }
 
-// The adjoint kernel calls the tracker through one out-of-line copy (four
-// call sites, two passes: a smaller instruction footprint); the primal
-// kernel inlines it.
-__device__ __noinline__ bool adj_track_shared(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
-                                              const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
-                                              float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
-                                              bool& watchdog) {
-    return adj_track_body(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
-}
-
-template <bool kShared>
-__device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
-                                          const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
-                                          float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
-                                          bool& watchdog) {
-    if (kShared)
-        return adj_track_shared(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
-    return adj_track_body(A, P, Q, band, g, t_max, rng, t_hit, hit, w_eval, tau_bar, gw, acc, n, watchdog);
-}
-
 // Estimate of -integral d(sigma_t) over [0, t_end] of a ray, times weight:
 // N points stratified in the majorant optical depth of Q's tracking grid
 // (density mu_bar / tau_bar along the ray; tau_bar as the tracker summed
@@ -288,8 +268,8 @@ __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, cons
 // draws are untouched.
 constexpr int kMaxSegmentPoints = 4;
 
-__device__ __noinline__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, const RayGeo& g,
-                                           float t_end, float tau, float weight, const Rng& rng, AdjAcc& acc) {
+__device__ __forceinline__ void segment_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, const RayGeo& g,
+                                              float t_end, float tau, float weight, const Rng& rng, AdjAcc& acc) {
     if (weight == 0.0f || !(t_end > 0.0f) || !(tau > 0.0f)) return;
     const DevScene& S = A.S;
     const uint32_t L = S.layer_count;
@@ -354,57 +334,29 @@ __device__ __forceinline__ float hg_sampling_pdf(const AdjSet& X, uint32_t bins,
 }
 
 // Shadow ray of an NEE sample: the P/Q weight of a ray that reaches the sun,
-// 0 when it hits the ground, leaves through no sun or collides.  dim0 is the
-// random-number index at which its tracking started, tau_bar its majorant
-// optical depth.
-template <bool kShared>
+// 0 when it hits the ground, leaves through no sun or collides.
 __device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band, V3 pos,
-                                            V3 ldir, Rng& rng, AdjAcc& acc, Counters& n, bool& watchdog,
-                                            uint32_t& dim0, float& tau_bar) {
+                                            V3 ldir, Rng& rng, AdjAcc& acc, Counters& n, bool& watchdog) {
     const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
     float st;
     uint32_t sk;
     ++n.e[SKY_EVENT_BOUNDARY];
     if (!(next_boundary(A.S, sg, st, sk) && sk == 1u)) return 0.0f;
-    dim0 = rng.dim;
-    float th, w = 1.0f;
+    float th, w = 1.0f, tau_bar;
     AdjBase bh;
-    if (adj_track<kShared>(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
+    if (adj_track(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
     return w;
 }
 
-// Gradient terms of an unblocked shadow ray: its segment integral, or (null
-// collisions) the same ray traced again from dim0 for its null collisions.
-__device__ __forceinline__ void adj_shadow_terms(const AdjCtx& A, const AdjSet& Q, uint32_t band, V3 pos, V3 ldir,
-                                                 Rng& rng, uint32_t dim0, float tau_bar, float weight, AdjAcc& acc,
-                                                 Counters& n, bool& watchdog) {
-    if (weight == 0.0f) return;
-    const RayGeo sg = ray_geo(madd(pos, ldir, kRayEpsilonKm), ldir);
-    float st;
-    uint32_t sk;
-    next_boundary(A.S, sg, st, sk);
-    if (A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
-        segment_terms(A, Q, band, sg, st, tau_bar, weight, rng, acc);
-        return;
-    }
-    const uint32_t dim1 = rng.dim;
-    rng.dim = dim0;
-    float th, w = 1.0f, tb;
-    AdjBase bh;
-    adj_track<true>(A, Q, Q, band, sg, st, rng, th, bh, w, tb, weight, acc, n, watchdog);
-    rng.dim = dim1;
-}
-
 // One chain of the parameterised medium (trace_path, sky_trace.wgsl:703-776)
-// at unit solar multiplier.  With `grad` it replays a chain whose radiance
-// `total` the first pass returned and accumulates w * dL/dparams (a run-time
-// flag, so that both passes share one copy of the code).
-template <int kPhase, bool kShared>
+// at unit solar multiplier: sampled under Q, evaluated under P.
+template <int kPhase>
 __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, const DevLaunch& L,
-                                           uint32_t x, uint32_t y, uint32_t band, uint32_t sample, bool grad,
-                                           float w, float total, AdjAcc& acc, Counters& n, bool& watchdog) {
+                                           uint32_t x, uint32_t y, uint32_t band, uint32_t sample, Counters& n,
+                                           bool& watchdog) {
     const DevScene& S = A.S;
     const uint32_t bins = S.phase_bins;
+    AdjAcc acc{nullptr, 0u, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // no gradient terms in a primal render
     Rng rng;
     rng.init(y * L.width + x, sample, band, L.seed_lo, L.seed_hi);
     V3 dir = camera_dir(L, x, y, rng);
@@ -425,18 +377,9 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
         uint32_t kind;
         ++n.e[SKY_EVENT_BOUNDARY];
         if (!next_boundary(S, g, t_b, kind)) break;
-        float t_hit, w_eval = 1.0f;
+        float t_hit, w_eval = 1.0f, tau_bar;
         AdjBase hb;
-        const float gw = grad ? w * (total - rad) : 0.0f;
-        const uint32_t dim_seg = rng.dim;
-        float tau_bar;
-        const bool hit =
-            adj_track<kShared>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, gw, acc, n, watchdog);
-        if (grad && A.estimator != SKY_ADJOINT_NULL_COLLISIONS) {
-            Rng at = rng;
-            at.dim = dim_seg;
-            segment_terms(A, Q, band, g, hit ? t_hit : t_b, tau_bar, gw, at, acc);
-        }
+        const bool hit = adj_track(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, 0.0f, acc, n, watchdog);
         thr *= w_eval;
         if (hit) {
             ++n.e[SKY_EVENT_SCATTER];
@@ -452,20 +395,11 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
             for (uint32_t ls = 0; ls < L.direct_light_samples; ++ls) {
                 const V3 ldir = sample_sun_cone(S, rng);
                 ++n.e[SKY_EVENT_NEE];
-                uint32_t dim0 = 0;
-                float tau_s = 0.0f;
-                const float trans =
-                    adj_shadow<kShared>(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0, tau_s);
+                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog);
                 if (!(trans != 0.0f)) continue;
                 const float mu = dot3(dir, ldir);
                 const float ph = mp.s > 0.0f ? vertex_phase(P, bins, mp, mu) / mp.s : 0.0f;
-                const float term = l_sun * trans * ph / S.light_pdf;
-                nee += term;
-                if (grad) {
-                    const float c = w * thr * term * inv_lights;
-                    vertex_terms(acc, Q, bins, hb, mq, mu, c);
-                    adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, tau_s, c, acc, n, watchdog);
-                }
+                nee += l_sun * trans * ph / S.light_pdf;
             }
             rad += thr * (nee * inv_lights);
             V3 nd;
@@ -490,7 +424,6 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
             }
             thr_q *= fq;
             thr = A.distinct ? thr * fp : thr_q;
-            if (grad) vertex_terms(acc, Q, bins, hb, mq, mu_c, w * (total - rad));
             if (depth >= L.rr_start_depth) {  // russian_roulette (sky_trace.wgsl:691-701)
                 const float q = fminf(fmaxf(thr_q, 0.05f), 0.95f);
                 if (rng.next() > q) break;
@@ -513,15 +446,9 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
                 ++n.e[SKY_EVENT_NEE];
                 const float cos_sun = fmaxf(dot3(normal, ldir), 0.0f);
                 if (!(cos_sun > 0.0f)) continue;
-                uint32_t dim0 = 0;
-                float tau_s = 0.0f;
-                const float trans =
-                    adj_shadow<kShared>(A, P, Q, band, pos, ldir, rng, acc, n, watchdog, dim0, tau_s);
+                const float trans = adj_shadow(A, P, Q, band, pos, ldir, rng, acc, n, watchdog);
                 if (!(trans != 0.0f)) continue;
-                const float term = S.ground_albedo * kInvPi * l_sun * trans * cos_sun / S.light_pdf;
-                ground += term;
-                if (grad) adj_shadow_terms(A, Q, band, pos, ldir, rng, dim0, tau_s, w * thr * term * inv_lights, acc, n,
-                                             watchdog);
+                ground += S.ground_albedo * kInvPi * l_sun * trans * cos_sun / S.light_pdf;
             }
             rad += thr * (ground * inv_lights);
             float pdf;
@@ -550,11 +477,6 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-__device__ __forceinline__ float warp_sum_f(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 __device__ __forceinline__ uint32_t warp_sum_u(uint32_t v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -571,17 +493,14 @@ __device__ __forceinline__ void flush_counters(const Counters& n, unsigned long 
 }
 
 // Primal: one warp per (pixel, band) cell, 32 samples per round, FP64 cell
-// sums in a fixed order (as the plain tracer).  chain_out, when given,
-// receives every chain's radiance at unit solar multiplier ([cell][sample]),
-// which the adjoint kernel replays against.
-template <int kPhase, bool kShared>
+// sums in a fixed order (as the plain tracer).
+template <int kPhase>
 __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_constant__ AdjCtx A,
                                                              const __grid_constant__ DevLaunch L,
                                                              double* __restrict__ cell_sum,
                                                              double* __restrict__ cell_sumsq, uint32_t accumulate,
                                                              unsigned long long* __restrict__ counters,
-                                                             uint32_t* __restrict__ status, uint64_t cells,
-                                                             float* __restrict__ chain_out) {
+                                                             uint32_t* __restrict__ status, uint64_t cells) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
@@ -590,31 +509,23 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
     const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
     const AdjSet P = resolve(A.P, A.S.layer_count, band);
     const AdjSet Q = A.distinct ? resolve(A.Q, A.S.layer_count, band) : P;
-    AdjAcc acc{nullptr, 0u, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     Counters n;
     n.clear();
     bool watchdog = false;
     double sum = 0.0, sumsq = 0.0;
-    if (accumulate && cell_sum) {
+    if (accumulate) {
         sum = cell_sum[cell];
         if (cell_sumsq) sumsq = cell_sumsq[cell];
     }
     for (uint32_t base = 0; base < L.spp; base += 32u) {
         const uint32_t s = base + lane;
         float r = 0.0f;
-        if (s < L.spp) {
-            const float unit = adj_chain<kPhase, kShared>(A, P, Q, L, x, y, band, L.sample_offset + s, false, 0.0f,
-                                                          0.0f, acc, n, watchdog);
-            if (chain_out) chain_out[cell * L.spp + s] = unit;
-            r = P.kS * unit;
-        }
-        if (cell_sum) {
-            const double rd = double(r);
-            sum += warp_sum_d(rd);
-            sumsq += warp_sum_d(rd * rd);
-        }
+        if (s < L.spp) r = P.kS * adj_chain<kPhase>(A, P, Q, L, x, y, band, L.sample_offset + s, n, watchdog);
+        const double rd = double(r);
+        sum += warp_sum_d(rd);
+        sumsq += warp_sum_d(rd * rd);
     }
-    if (cell_sum && lane == 0) {
+    if (lane == 0) {
         cell_sum[cell] = sum;
         if (cell_sumsq) cell_sumsq[cell] = sumsq;
     }
@@ -622,69 +533,327 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
 }
 
-// Adjoint: warps take cells one at a time and replay each chain against the
-// radiance the primal pass stored for it.  Layer gradients gather in shared memory (FP32, one copy
-// per warp when they fit, so that only a warp's own lanes contend), the
-// albedo, g and band gradients in registers reduced per cell; each block adds
-// its totals to the FP64 outputs once at the end.
+// ---------------------------------------------------------------------------
+// Path replay as a ray loop.  A chain is a sequence of rays: the primary
+// segment from each vertex, the shadow ray of each NEE sample and, with the
+// null-collision estimator, the second trace of an unblocked shadow ray.
+// Each iteration of the kernel's loop traces one ray per lane through the one
+// inlined tracker and adds that ray's segment integral; the event code then
+// runs up to the lane's next ray.  The lanes of a warp therefore enter the
+// tracker together whatever vertex, pass or chain each is at, and a lane
+// whose chain ends takes the next sample of its warp's cell (the warp takes a
+// new cell from a counter when the samples run out) instead of waiting for
+// the other lanes.
+//
+// Every chain runs twice on the same code: pass 0 for its radiance L (the
+// C_after of the factors needs it), pass 1 for the gradient terms; both take
+// the same path.  Random numbers are drawn in adj_chain's order, so the
+// replay follows the primal render's paths.  P = Q (a gradient is taken at
+// the sampling parameters).
+enum : uint32_t { kRayPrimary = 0u, kRayShadow = 1u, kRayRetrace = 2u };
+enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLights = 3u, kNextEnd = 4u,
+                  kNextIdle = 5u };
+
 template <int kPhase>
-__global__ void __launch_bounds__(256) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
-                                                           const __grid_constant__ DevLaunch L,
-                                                           const float* __restrict__ dloss,
-                                                           double* __restrict__ layer_grad,
-                                                           double* __restrict__ band_grad,
-                                                           unsigned long long* __restrict__ counters,
-                                                           uint32_t* __restrict__ status, uint64_t cells,
-                                                           uint32_t copies, uint32_t* __restrict__ next_cell,
-                                                           const float* __restrict__ chain_in) {
+__global__ void __launch_bounds__(256, 2) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
+                                                              const __grid_constant__ DevLaunch L,
+                                                              const float* __restrict__ dloss,
+                                                              double* __restrict__ layer_grad,
+                                                              double* __restrict__ band_grad,
+                                                              unsigned long long* __restrict__ counters,
+                                                              uint32_t* __restrict__ status, uint32_t cells,
+                                                              uint32_t copies, uint32_t* __restrict__ next_cell) {
     extern __shared__ float smem[];
-    const uint32_t Lc = A.S.layer_count, B = A.S.band_count;
+    const DevScene& S = A.S;
+    const uint32_t Lc = S.layer_count, B = S.band_count, bins = S.phase_bins;
     const uint32_t nlayer = 3u * Lc + 2u;
-    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    // layer gradients: one FP32 copy per warp when they fit (only a warp's own
+    // lanes contend); band gradients: one copy per block
     float* sg = layer_grad ? smem + (warp % copies) * nlayer : nullptr;
     float* sb = smem + copies * nlayer;
     for (uint32_t i = threadIdx.x; i < copies * nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
     __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u;
     Counters n;
     n.clear();
     bool watchdog = false;
-    const float inv_spp = 1.0f / float(L.spp);
-    for (;;) {  // warps take cells from a shared counter: no tail of unequal fixed shares
-        uint32_t next = 0;
-        if (lane == 0) next = atomicAdd(next_cell, 1u);
-        const uint64_t cell = __shfl_sync(0xffffffffu, next, 0);
-        if (cell >= cells) break;
-        const float wcell = __ldg(dloss + cell) * inv_spp;
-        if (wcell == 0.0f) continue;  // uniform across the warp
-        const uint32_t band = uint32_t(cell % L.band_count);
-        const uint64_t pixel = cell / L.band_count;
-        const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
-        const AdjSet P = resolve(A.P, Lc, band);
-        const float w = wcell * P.kS;
-        AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-        float gS = 0.0f;
-        for (uint32_t base = 0; base < L.spp; base += 32u) {
-            const uint32_t s = base + lane;
-            if (s >= L.spp) continue;
-            // the chain's radiance from the primal pass, then its replay
-            const float total = __ldg(chain_in + cell * L.spp + s);
-            gS = fmaf(wcell, total, gS);
-            if (total > 0.0f)
-                adj_chain<kPhase, true>(A, P, P, L, x, y, band, L.sample_offset + s, true, w, total, acc, n,
-                                        watchdog);
+    const float inv_spp = 1.0f / float(L.spp), inv_lights = 1.0f / float(L.direct_light_samples);
+    const bool seg_est = A.estimator != SKY_ADJOINT_NULL_COLLISIONS;
+    AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    // the warp's cell and its next unclaimed sample (warp-uniform)
+    uint32_t claim_cell = 0u, claim_next = L.spp;
+    bool exhausted = false;
+    // the lane's chain
+    uint32_t next = kNextIdle, pass = 0u, cell = 0u, sample = 0u, band = 0u, ray = kRayPrimary, depth = 0u,
+             ls = 0u, boundary = 0u, dim0 = 0u, dim1 = 0u;
+    bool ground = false;
+    Rng rng;
+    rng.k0 = rng.k1 = rng.k2 = rng.dim = 0u;
+    V3 org = mk(0.0f, 0.0f, 0.0f), dir = org;  // org is the vertex position between rays
+    float thr = 0.0f, rad = 0.0f, nee = 0.0f, total = 0.0f, wc = 0.0f;
+    float term = 0.0f, mu = 0.0f, c = 0.0f, t_max = 0.0f;  // pending shadow ray: its NEE term, cosine, weight
+    AdjBase hb{0.0f, 0.0f, 0.0f, 0};
+    RayGeo g{0.0f, 0.0f, 0.0f};
+
+    for (;;) {
+#pragma unroll 1
+        for (int round = 0; round < 2; ++round) {
+            // idle lanes take the next samples of the warp's cell
+#pragma unroll 1
+            for (;;) {
+                const uint32_t need = __ballot_sync(0xffffffffu, next == kNextIdle);
+                if (need == 0u || exhausted) break;
+                if (claim_next >= L.spp) {
+                    uint32_t cn = 0u;
+                    if (lane == 0u) {
+                        do cn = atomicAdd(next_cell, 1u);
+                        while (cn < cells && __ldg(dloss + cn) == 0.0f);  // no loss: no gradient
+                    }
+                    cn = __shfl_sync(0xffffffffu, cn, 0);
+                    if (cn >= cells) {
+                        exhausted = true;
+                        break;
+                    }
+                    claim_cell = cn;
+                    claim_next = 0u;
+                }
+                const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+                if (next == kNextIdle && claim_next + rank < L.spp) {
+                    cell = claim_cell;
+                    sample = claim_next + rank;
+                    pass = 0u;
+                    next = kNextStart;
+                }
+                claim_next = min(L.spp, claim_next + uint32_t(__popc(need)));
+            }
+            // event code up to the lane's next ray
+#pragma unroll 1
+            while (next != kNextIdle && next != kNextTrace) {
+                if (next == kNextEnd) {
+                    if (pass == 0u) {
+                        total = rad;
+                        if (total > 0.0f) {
+                            pass = 1u;
+                            next = kNextStart;
+                        } else {
+                            if (total != 0.0f) atomicAdd(sb + band * kAdjBandParams + 3u, wc * total);
+                            next = kNextIdle;
+                        }
+                    } else {
+                        float* bg = sb + band * kAdjBandParams;
+                        atomicAdd(bg, acc.gR);
+                        atomicAdd(bg + 1, acc.gM);
+                        atomicAdd(bg + 2, acc.gO);
+                        atomicAdd(bg + 3, wc * total);
+                        if (sg) {
+                            atomicAdd(sg + 3u * Lc, acc.gW);
+                            atomicAdd(sg + 3u * Lc + 1u, acc.gG);
+                        }
+                        acc.gR = acc.gM = acc.gO = acc.gW = acc.gG = 0.0f;
+                        next = kNextIdle;
+                    }
+                    continue;
+                }
+                if (next == kNextStart) {
+                    band = cell % L.band_count;
+                    const uint32_t pixel = cell / L.band_count;
+                    const uint32_t x = pixel % L.width, y = pixel / L.width;
+                    wc = __ldg(dloss + cell) * inv_spp;
+                    rng.init(pixel, L.sample_offset + sample, band, L.seed_lo, L.seed_hi);
+                    dir = camera_dir(L, x, y, rng);
+                    org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
+                    ++n.e[SKY_EVENT_CHAIN];
+                    thr = 1.0f;
+                    rad = 0.0f;
+                    depth = 0u;
+                    next = kNextPrimary;
+                }
+                if (next == kNextPrimary) {
+                    if (depth >= L.watchdog_limit) {
+                        watchdog = true;
+                        next = kNextEnd;
+                        continue;
+                    }
+                    g = ray_geo(org, dir);
+                    ++n.e[SKY_EVENT_BOUNDARY];
+                    if ((L.max_orders != 0u && depth >= L.max_orders) || !next_boundary(S, g, t_max, boundary)) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kNextEnd;
+                        continue;
+                    }
+                    ray = kRayPrimary;
+                    next = kNextTrace;
+                    continue;
+                }
+                // kNextLights: the vertex's next NEE sample that needs a shadow
+                // ray (direct_sun_at_scatter, sky_trace.wgsl:566-585; ground
+                // radiance, :587-608), else its continuation
+                const AdjSet P = resolve(A.P, Lc, band);
+                const float l_sun = __ldg(&S.bands[band].solar_radiance);
+                const float w = wc * P.kS;
+                bool shadow = false;
+                while (ls < L.direct_light_samples) {
+                    ++ls;
+                    const V3 ldir = sample_sun_cone(S, rng);
+                    ++n.e[SKY_EVENT_NEE];
+                    float cos_sun = 0.0f;
+                    if (ground) {
+                        cos_sun = fmaxf(dot3(normalize_or_y(org), ldir), 0.0f);
+                        if (!(cos_sun > 0.0f)) continue;
+                    }
+                    g = ray_geo(madd(org, ldir, kRayEpsilonKm), ldir);
+                    uint32_t sk;
+                    ++n.e[SKY_EVENT_BOUNDARY];
+                    if (!(next_boundary(S, g, t_max, sk) && sk == 1u)) continue;
+                    dim0 = rng.dim;
+                    if (ground) {
+                        term = S.ground_albedo * kInvPi * l_sun * cos_sun / S.light_pdf;
+                    } else {
+                        mu = dot3(dir, ldir);
+                        const AdjMed mp = adj_med(P, hb);
+                        const float ph = mp.s > 0.0f ? vertex_phase(P, bins, mp, mu) / mp.s : 0.0f;
+                        term = l_sun * ph / S.light_pdf;
+                    }
+                    c = w * thr * term * inv_lights;
+                    shadow = true;
+                    break;
+                }
+                if (shadow) {
+                    ray = kRayShadow;
+                    next = kNextTrace;
+                    continue;
+                }
+                rad += thr * (nee * inv_lights);
+                V3 nd;
+                if (!ground) {
+                    const AdjMed mq = adj_med(P, hb);
+                    float mu_c, fq;
+                    if (kPhase == SKY_PHASE_TABULATED) {
+                        const float target = rng.next() * mq.s;
+                        const bool rayleigh = target < mq.R || !(mq.Ms > 0.0f);
+                        const float xi_mu = rng.next();
+                        mu_c = rayleigh ? invert_rayleigh_cdf(xi_mu) : hg_sample_mu(P, bins, xi_mu);
+                        const float xi_phi = rng.next();
+                        nd = direction_from_axis_mu(dir, mu_c, xi_phi);
+                        const float pdf = mq.R * rayleigh_phase(mu_c) +
+                                          (mq.Ms > 0.0f ? mq.Ms * hg_sampling_pdf(P, bins, mu_c) : 0.0f);
+                        fq = vertex_phase(P, bins, mq, mu_c) / pdf;
+                    } else {
+                        nd = sample_isotropic(rng);
+                        mu_c = dot3(dir, nd);
+                        fq = vertex_phase(P, bins, mq, mu_c) / mq.s / kIsotropicPdf;
+                    }
+                    thr *= fq;
+                    if (pass == 1u) vertex_terms(acc, P, bins, hb, mq, mu_c, w * (total - rad));
+                } else {
+                    // the Lambert bounce (sky_trace.wgsl:750-766)
+                    const V3 normal = normalize_or_y(org);
+                    float pdf;
+                    nd = sample_cosine_hemisphere(normal, rng, pdf);
+                    const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+                    if (pdf <= 0.0f || cos_out <= 0.0f) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kNextEnd;
+                        continue;
+                    }
+                    const float f = S.ground_albedo * kInvPi * cos_out / pdf;
+                    thr *= f;
+                }
+                if (depth >= L.rr_start_depth) {  // russian_roulette (sky_trace.wgsl:691-701)
+                    const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
+                    if (rng.next() > q) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kNextEnd;
+                        continue;
+                    }
+                    thr = thr / q;
+                }
+                org = madd(org, nd, kRayEpsilonKm);
+                dir = nd;
+                if (rad < 0.0f || rad != rad || thr < 0.0f || thr != thr) {
+                    rad = 0.0f;
+                    next = kNextEnd;
+                    continue;
+                }
+                ++depth;
+                next = kNextPrimary;
+            }
         }
-        const float r = warp_sum_f(acc.gR), m = warp_sum_f(acc.gM), o = warp_sum_f(acc.gO), s = warp_sum_f(gS);
-        const float gw = warp_sum_f(acc.gW), gg = warp_sum_f(acc.gG);
-        if (lane == 0) {
-            float* b = sb + band * kAdjBandParams;
-            atomicAdd(b, r);
-            atomicAdd(b + 1, m);
-            atomicAdd(b + 2, o);
-            atomicAdd(b + 3, s);
-            if (sg) {
-                atomicAdd(sg + 3u * Lc, gw);
-                atomicAdd(sg + 3u * Lc + 1u, gg);
+        const bool tracing = next == kNextTrace;
+        if (!__any_sync(0xffffffffu, tracing)) {
+            if (exhausted) break;  // every lane idle and no cell left
+            continue;
+        }
+        if (tracing) {
+            const AdjSet P = resolve(A.P, Lc, band);
+            const float w = wc * P.kS;
+            const bool grad = pass == 1u;
+            const float gw = ray == kRayPrimary ? (grad ? w * (total - rad) : 0.0f) : (ray == kRayRetrace ? c : 0.0f);
+            const uint32_t dim_seg = rng.dim;
+            float t_hit = 0.0f, w_eval = 1.0f, tau_bar = 0.0f;
+            AdjBase hit_b;
+            const bool hit = adj_track(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar, gw, acc, n, watchdog);
+            if (grad && seg_est) {
+                // the segment integral of the traced part: a primary segment
+                // from its first random number, an unblocked shadow ray from
+                // the position after its tracking
+                float sw = 0.0f, t_end = t_max;
+                Rng at = rng;
+                if (ray == kRayPrimary) {
+                    sw = gw;
+                    at.dim = dim_seg;
+                    if (hit) t_end = t_hit;
+                } else if (ray == kRayShadow && !hit) {
+                    sw = c;
+                }
+                segment_terms(A, P, band, g, t_end, tau_bar, sw, at, acc);
+            }
+            if (ray == kRayPrimary) {
+                if (hit) {
+                    ++n.e[SKY_EVENT_SCATTER];
+                    org = madd(org, dir, t_hit);
+                    hb = hit_b;
+                    const AdjMed mq = adj_med(P, hb);
+                    if (mq.t > 0.0f && mq.s > 0.0f) thr *= fminf(fmaxf(mq.s / mq.t, 0.0f), 1.0f);
+                    if (!(mq.t > 0.0f && mq.s > 0.0f) || thr <= 0.0f) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kNextEnd;
+                    } else {
+                        ground = false;
+                        ls = 0u;
+                        nee = 0.0f;
+                        next = kNextLights;
+                    }
+                } else if (boundary == 1u) {
+                    if (depth == 0u && dot3(dir, load3(S.sun)) >= S.cos_max)
+                        rad += thr * __ldg(&S.bands[band].solar_radiance);
+                    rad = fmaxf(rad, 0.0f);
+                    next = kNextEnd;
+                } else {
+                    ++n.e[SKY_EVENT_GROUND];
+                    org = madd(org, dir, t_max);
+                    ground = true;
+                    ls = 0u;
+                    nee = 0.0f;
+                    next = kNextLights;
+                }
+            } else if (ray == kRayShadow) {
+                next = kNextLights;
+                if (!hit) {
+                    nee += term;
+                    if (grad) {
+                        if (!ground) vertex_terms(acc, P, bins, hb, adj_med(P, hb), mu, c);
+                        if (!seg_est && c != 0.0f) {  // trace it again for its null collisions
+                            dim1 = rng.dim;
+                            rng.dim = dim0;
+                            ray = kRayRetrace;
+                            next = kNextTrace;
+                        }
+                    }
+                }
+            } else {
+                rng.dim = dim1;
+                next = kNextLights;
             }
         }
     }
@@ -693,7 +862,7 @@ __global__ void __launch_bounds__(256) adjoint_grad_kernel(const __grid_constant
     __syncthreads();
     for (uint32_t i = threadIdx.x; layer_grad && i < nlayer; i += blockDim.x) {
         float v = 0.0f;
-        for (uint32_t c = 0; c < copies; ++c) v += smem[c * nlayer + i];
+        for (uint32_t k = 0; k < copies; ++k) v += smem[k * nlayer + i];
         if (v != 0.0f) atomicAdd(layer_grad + i, double(v));
     }
     if (band_grad)
@@ -876,56 +1045,44 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  cudaStream_t stream, float* chain_out) {
+                                  cudaStream_t stream) {
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
     const uint64_t blocks = (cells * 32u + 255u) / 256u;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     const dim3 grid(static_cast<uint32_t>(blocks));
     const uint32_t acc = accumulate ? 1u : 0u;
-    // the pass before an adjoint uses the adjoint's out-of-line tracker, so
-    // that its chains are the ones the replay recomputes
-    if (L.phase_sampling == SKY_PHASE_TABULATED) {
-        if (chain_out)
-            adjoint_primal_kernel<SKY_PHASE_TABULATED, true>
-                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, chain_out);
-        else
-            adjoint_primal_kernel<SKY_PHASE_TABULATED, false>
-                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, nullptr);
-    } else {
-        if (chain_out)
-            adjoint_primal_kernel<SKY_PHASE_ISOTROPIC, true>
-                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, chain_out);
-        else
-            adjoint_primal_kernel<SKY_PHASE_ISOTROPIC, false>
-                <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells, nullptr);
-    }
+    if (L.phase_sampling == SKY_PHASE_TABULATED)
+        adjoint_primal_kernel<SKY_PHASE_TABULATED>
+            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+    else
+        adjoint_primal_kernel<SKY_PHASE_ISOTROPIC>
+            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
     return cudaGetLastError();
 }
 
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
-                                uint32_t* next_cell, float* chains, cudaStream_t stream) {
-    cudaError_t e = launch_adjoint_primal(A, L, nullptr, nullptr, false, counters, status, stream, chains);
-    if (e != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
+                                uint32_t* next_cell, cudaStream_t stream) {
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    if (cells > 0xffffffffull) return cudaErrorInvalidConfiguration;  // the cell counter is 32-bit
+    cudaError_t e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
     const size_t nlayer = size_t(3u * A.S.layer_count + 2u), nband = size_t(kAdjBandParams) * A.S.band_count;
     // one layer-gradient copy per warp while it stays within the default 48 KB
     const uint32_t copies = (8 * nlayer + nband) * sizeof(float) <= 48u * 1024u ? 8u : 1u;
     const size_t smem = (copies * nlayer + nband) * sizeof(float);
     const uint64_t want = (cells * 32u + 255u) / 256u;
+    const uint32_t n = static_cast<uint32_t>(cells);
     if (L.phase_sampling == SKY_PHASE_TABULATED) {
         const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_TABULATED><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
-                                                                                band_grad, counters, status, cells,
-                                                                                copies, next_cell, chains);
+        adjoint_grad_kernel<SKY_PHASE_TABULATED><<<blocks, 256, smem, stream>>>(
+            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell);
     } else {
         const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC><<<blocks, 256, smem, stream>>>(A, L, dloss_dfilm, layer_grad,
-                                                                                band_grad, counters, status, cells,
-                                                                                copies, next_cell, chains);
+        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC><<<blocks, 256, smem, stream>>>(
+            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell);
     }
     return cudaGetLastError();
 }

@@ -75,13 +75,12 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 // of the radiance of P, sampled with Q.
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  cudaStream_t stream, float* chain_out = nullptr);
+                                  cudaStream_t stream);
 
 // Path-replay gradient (P == Q): adds dLoss/dparams to layer_grad [3 L + 2]
-// and band_grad [B][4] (may be null) given dLoss/dfilm [pixels][B].  A primal
-// pass first stores every chain's radiance in `chains` [cells * spp].
+// and band_grad [B][4] (may be null) given dLoss/dfilm [pixels][B].
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
-                                uint32_t* next_cell, float* chains, cudaStream_t stream);
+                                uint32_t* next_cell, cudaStream_t stream);
 
 }  // namespace sky

@@ -60,8 +60,6 @@ struct SkyScene {
     uint32_t host_layers = 0;
     // differentiable rendering: tables rebuilt per call, allocated on first use
     void* adj_ws = nullptr;
-    float* adj_chains = nullptr;  // chain radiances of the backward's primal pass, grown on demand
-    uint64_t adj_chains_len = 0;
     std::string adjoint_unsupported;  // empty when the scene's medium can be parameterised
 };
 
@@ -548,7 +546,6 @@ void sky_cuda_scene_destroy(SkyScene* s) {
     cudaFree(s->batch_counter);
     cudaFree(s->trk_blob);
     cudaFree(s->adj_ws);
-    cudaFree(s->adj_chains);
     cudaFree(s->jobs);
     cudaFree(s->work_counter);
     cudaFree(s->blob);
@@ -923,20 +920,10 @@ extern "C" int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderC
                          "grads.dloss_dfilm and at least one of grads.layer_grad, grads.band_grad are required");
     if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
-    const uint64_t chains = uint64_t(config->width) * config->height * s->dev.band_count * config->spp;
-    if (chains > s->adj_chains_len) {
-        cudaStreamSynchronize(stream);  // an earlier backward may still read the old buffer
-        cudaFree(s->adj_chains);
-        s->adj_chains = nullptr;
-        s->adj_chains_len = 0;
-        cudaError_t ea = cudaMalloc(&s->adj_chains, chains * sizeof(float));
-        if (ea != cudaSuccess) return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "chain radiance buffer", ea);
-        s->adj_chains_len = chains;
-    }
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = launch_adjoint_grad(A, L, grads->dloss_dfilm, grads->layer_grad, grads->band_grad, grads->counters,
-                            grads->status, W.next_cell, s->adj_chains, stream);
+                            grads->status, W.next_cell, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);
     return SKY_OK;
 }
