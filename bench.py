@@ -39,9 +39,10 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "sky-tracer_gb300"))
 DATA_DIR = ROOT / "tests" / "golden" / "data"
 
-# DRAM bytes (read + write) of one launch of the tracer on the production
-# render, from a 1-pass ncu capture (profiles/pool_kernel_plain-512x256-81wl-256spp_dram.txt).
-POOL_LAUNCH_DRAM_BYTES = {"plain-512x256-81wl-256spp": 13.24e6 + 183.27e6}
+# DRAM bytes (read + write) of one launch of the wavefront tracing kernel on
+# the production render, from a 1-pass ncu capture
+# (profiles/wave_kernel_plain-512x256-81wl-256spp_dram.txt).
+WAVE_LAUNCH_DRAM_BYTES = {"plain-512x256-81wl-256spp": 183.77e6 + 143.90e6}
 
 # Frozen per-event FP32 work weights (FLOP, an FMA counted as 2), counted
 # from the reference shader's arithmetic for each event type.
@@ -245,7 +246,7 @@ def run_reference(args):
 
 
 def run_sweep(args):
-    """Batched elevation sweep (one persistent launch, CUDA graph, per-elevation
+    """Batched elevation sweep (one wavefront launch, CUDA graph, per-elevation
     budgets) against 32 separate plain-kernel launches, at equal error."""
     import torch
     from sky_cuda import GpuScene, RenderConfig, synthetic_scene, wavelengths
@@ -336,7 +337,7 @@ def run_sweep(args):
             "plain_chains_per_s": chains_batched / t_plain_budget,
         },
         "clocks": clocks.summary(),
-        "gpu_launches": args.steps,
+        "gpu_launches": 3 * args.steps,  # prepare, trace, finalize per replay
     }
     print(json.dumps(out))
     for g in singles:
@@ -627,7 +628,7 @@ def main():
         t0 = time.perf_counter()
         best, trials = autotune(gs, cfg)
         tuning_log = {"chosen": best, "seconds": round(time.perf_counter() - t0, 2),
-                      "trials": [[t["pool_variant"], t["stage_tables"], round(t["crossing_cost"], 3), round(ms, 3)]
+                      "trials": [[t["variant"], round(t["crossing_cost"], 3), round(ms, 3)]
                                  for t, ms in trials]}
     stream = torch.cuda.current_stream(dev)
     s = torch.zeros(cells, dtype=torch.float64, device=dev)
@@ -715,7 +716,7 @@ def main():
             "config": {"workload": args.workload, "width": cfg.width, "height": cfg.height, "wavelengths": B,
                        "spp": cfg.spp, "chains_per_step": chains, "sun_elevation_deg": w["sun"],
                        "tracking": ("segment-restart", "residual-carry", "merged-layers")[cfg.tracking],
-                       "phase_sampling": "tabulated", "kernel": ("persistent", "plain", "persistent")[cfg.kernel],
+                       "phase_sampling": "tabulated", "kernel": ("wavefront", "plain", "wavefront")[cfg.kernel],
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas{world}",
                        "tuning": gs.get_tuning(), "autotune": tuning_log},
             "e2e": {"value": world * chains / e2e_s if e2e_times else None, "unit": "chains/s",
@@ -724,7 +725,7 @@ def main():
             "time_to_1pct_xyz_s": t1pct, "p95_rel_se_at_spp": p95,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
-                         "traffic": POOL_LAUNCH_DRAM_BYTES.get(args.workload) if cfg.kernel != 1 else None,
+                         "traffic": WAVE_LAUNCH_DRAM_BYTES.get(args.workload) if cfg.kernel != 1 else None,
                          "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                          "peak_source": "measured: cuBLAS SGEMM 8192^3 with TF32 off (MEASURED_PEAKS.json "
                                         "has no FP32 figure)",
@@ -732,7 +733,7 @@ def main():
             "cpu_baseline": cpu,
             "adjoint": adjoint,
             "clocks": clocks.summary(),
-            "gpu_launches": (2 if cfg.kernel == 1 else 1) * args.steps,
+            "gpu_launches": (2 if cfg.kernel == 1 else 3) * args.steps,
         }
         print(json.dumps(out))
     gs.close()

@@ -147,9 +147,11 @@ typedef enum SkyTracking {
 } SkyTracking;
 
 typedef enum SkyKernel {
-    SKY_KERNEL_AUTO = 0,       /* the persistent regenerating kernel */
-    SKY_KERNEL_PLAIN = 1,      /* one thread per chain, one launch   */
-    SKY_KERNEL_WAVEFRONT = 2   /* persistent, per-lane regeneration  */
+    SKY_KERNEL_AUTO = 0,       /* the wavefront kernel                                   */
+    SKY_KERNEL_PLAIN = 1,      /* one chain per lane, a warp per cell; cell sums in a
+                                  fixed order                                            */
+    SKY_KERNEL_WAVEFRONT = 2   /* persistent ray loop: one ray per lane per iteration,
+                                  per-lane chain regeneration                            */
 } SkyKernel;
 
 /* Add into the sums already held by the outputs instead of overwriting them
@@ -234,16 +236,16 @@ typedef struct SkyDeviceOutputs {
 } SkyDeviceOutputs;
 
 /*
- * Launch shape of the persistent tracer, per scene.  No counterpart in the
+ * Launch shape of the wavefront tracer, per scene.  No counterpart in the
  * reference, whose dispatch shape is fixed (workgroup 8x8x1, one dispatch per
  * 2 samples, integrator.rs:254-283).  The Python package's autotuner times
  * candidates of these on the caller's workload and keeps the fastest.
  */
 typedef struct SkyTuning {
-    uint32_t pool_variant;       /* 0: 1024 resident paths, 2 blocks/SM; 1: 512 paths, 3 blocks/SM */
+    uint32_t variant;            /* resident blocks of 256 threads per SM the kernel is compiled
+                                    for: 0 = 3 (80 registers), 1 = 2 (128), 2 = 4 (64)         */
     uint32_t max_blocks_per_sm;  /* 0 = occupancy limit                                          */
-    uint32_t stage_tables;       /* 1 = stage the scene tables in shared memory when they fit     */
-    uint32_t pixels_per_group;   /* pixels per work group; 0 = automatic                          */
+    uint32_t _unused[2];         /* zero                                                         */
     float crossing_cost;         /* merged tracking grid: cost of a layer crossing relative to a
                                     null collision; <= 0 leaves the grid as it is              */
     uint32_t _reserved[3];
@@ -333,17 +335,19 @@ typedef struct SkyBatchJob {
 } SkyBatchJob;
 
 /*
- * Render every job of the batch in ONE persistent launch on `cuda_stream`
- * (asynchronous).  All jobs must share tracking and phase sampling.  The
- * batch's watchdog bits go to jobs[0].outputs.status, its event counts to
+ * Render every job of the batch in ONE wavefront launch on `cuda_stream`
+ * (asynchronous; three kernels: prepare, trace, finalize).  All jobs must
+ * share tracking and phase sampling; at most 65535 jobs.  The batch's
+ * watchdog bits go to jobs[0].outputs.status, its event counts to
  * jobs[0].outputs.counters.
  */
 int sky_cuda_render_batch(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count, void* cuda_stream);
 
 /*
- * A batch captured once into a CUDA graph (job-table upload, work-counter
- * reset and the persistent launch) and replayed with one graph launch per
- * sweep.  The outputs named in `jobs` must stay valid while the graph lives.
+ * A batch captured once into a CUDA graph (job-table upload and the wavefront
+ * launch) and replayed with one graph launch per sweep.  The outputs named in
+ * `jobs` and the scene must stay valid while the graph is launched; destroy
+ * the graph before the scene.
  */
 typedef struct SkyBatchGraph SkyBatchGraph;
 int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatchJob* jobs, uint32_t job_count,
@@ -482,7 +486,7 @@ int sky_cuda_score_combos(const float* bands, uint32_t band_count, uint64_t samp
 
 /*
  * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
- * single launch of the persistent tracer.  No counterpart in the reference.
+ * single launch of the wavefront tracer.  No counterpart in the reference.
  *
  * For callers that must not allocate device memory while rendering: engines
  * that reserve all device memory up front through their own allocator, or

@@ -18,16 +18,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) finalize_kernel(const DevBand* __restrict__ bands, uint32_t band_count,
-                                                       uint64_t pixels, uint32_t total_spp,
-                                                       const double* __restrict__ cell_sum,
-                                                       const double* __restrict__ cell_sumsq,
-                                                       float* __restrict__ film, double* __restrict__ xyz,
-                                                       double* __restrict__ xyz_var, float* __restrict__ rgb,
-                                                       RgbMatrix m) {
-    const uint64_t pixel = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t lane = threadIdx.x & 31u;
-    if (pixel >= pixels) return;
+// One pixel by one warp: lanes stride over the bands.
+__device__ __forceinline__ void finalize_pixel(const DevBand* __restrict__ bands, uint32_t band_count,
+                                               uint64_t pixel, uint32_t total_spp, const double* __restrict__ cell_sum,
+                                               const double* __restrict__ cell_sumsq, float* __restrict__ film,
+                                               double* __restrict__ xyz, double* __restrict__ xyz_var,
+                                               float* __restrict__ rgb, const RgbMatrix& m, uint32_t lane) {
     const double n = double(total_spp);
     const double inv_n = 1.0 / n;
     double acc[3] = {0.0, 0.0, 0.0}, var[3] = {0.0, 0.0, 0.0};
@@ -63,6 +59,40 @@ __global__ void __launch_bounds__(256) finalize_kernel(const DevBand* __restrict
     }
 }
 
+__global__ void __launch_bounds__(256) finalize_kernel(const DevBand* __restrict__ bands, uint32_t band_count,
+                                                       uint64_t pixels, uint32_t total_spp,
+                                                       const double* __restrict__ cell_sum,
+                                                       const double* __restrict__ cell_sumsq,
+                                                       float* __restrict__ film, double* __restrict__ xyz,
+                                                       double* __restrict__ xyz_var, float* __restrict__ rgb,
+                                                       RgbMatrix m) {
+    const uint64_t pixel = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (pixel >= pixels) return;
+    finalize_pixel(bands, band_count, pixel, total_spp, cell_sum, cell_sumsq, film, xyz, xyz_var, rgb, m,
+                   threadIdx.x & 31u);
+}
+
+// Pixels of all jobs in a row; the job of a pixel by binary search over the
+// jobs' first cells (every job's cell range is a whole number of pixels).
+__global__ void __launch_bounds__(256) finalize_jobs_kernel(const DevBand* __restrict__ bands, uint32_t band_count,
+                                                            const DevJob* __restrict__ jobs, uint32_t num_jobs,
+                                                            uint64_t total_pixels, RgbMatrix m) {
+    const uint64_t gp = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (gp >= total_pixels) return;
+    const uint64_t gc = gp * band_count;
+    uint32_t lo = 0u, hi = num_jobs;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (jobs[mid].cell_begin <= gc) lo = mid;
+        else hi = mid;
+    }
+    const DevJob& J = jobs[lo];
+    if (!J.film && !J.xyz && !J.xyz_var && !J.rgb) return;
+    const uint64_t pixel = (gc - J.cell_begin) / band_count;
+    finalize_pixel(bands, band_count, pixel, J.total_spp, J.cell_sum, J.cell_sumsq, J.film, J.xyz, J.xyz_var, J.rgb,
+                   m, threadIdx.x & 31u);
+}
+
 }  // namespace
 
 cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_spp, const double* cell_sum,
@@ -74,6 +104,17 @@ cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_s
     finalize_kernel<<<dim3(uint32_t(blocks)), block, 0, stream>>>(S.bands, S.band_count, pixels, total_spp, cell_sum,
                                                                  cell_sumsq, film, xyz, xyz_var, rgb,
                                                                  rgb_matrix(S));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_jobs(const DevScene& S, const DevJob* jobs, uint32_t num_jobs, uint32_t total_cells,
+                                 cudaStream_t stream) {
+    const uint64_t pixels = uint64_t(total_cells) / S.band_count;
+    if (pixels == 0) return cudaSuccess;
+    const uint32_t block = 256;
+    const uint64_t blocks = (pixels * 32u + block - 1) / block;
+    finalize_jobs_kernel<<<dim3(uint32_t(blocks)), block, 0, stream>>>(S.bands, S.band_count, jobs, num_jobs, pixels,
+                                                                       rgb_matrix(S));
     return cudaGetLastError();
 }
 

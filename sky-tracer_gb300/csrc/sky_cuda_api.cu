@@ -43,7 +43,7 @@ struct SkyScene {
     unsigned long long* ws_counters = nullptr;
     uint32_t* ws_status = nullptr;
     uint64_t ws_cells = 0, ws_pixels = 0;
-    // persistent-kernel job table and work counter (one job per render call)
+    // wavefront-kernel job table and work counter (one job per render call)
     DevJob* jobs = nullptr;
     uint32_t* work_counter = nullptr;
     // batch job tables: device table + pinned host staging, grown on demand
@@ -51,7 +51,6 @@ struct SkyScene {
     DevJob* batch_host = nullptr;
     uint32_t* batch_counter = nullptr;
     uint32_t batch_capacity = 0;
-    int smem_optin = 0;
     SkyTuning tuning{};
     // merged tracking grid in its own allocation (rebuilt by set_tuning)
     void* trk_blob = nullptr;
@@ -191,17 +190,49 @@ DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
     return L;
 }
 
-// Pixels per work group of the persistent kernel: enough chains per group
-// (>= 4 pools) to keep the ring short, at most kPoolMaxCells cells.
-uint32_t pixels_per_group(uint32_t bands, uint32_t spp, uint32_t variant) {
-    const uint32_t want = 4u * kPoolThreads * pool_slots_per_thread(variant);
-    uint32_t p = (want + bands * spp - 1u) / (bands * spp);
-    p = std::max(1u, std::min(p, kPoolMaxCells / bands));
-    return p;
+// Cells a wavefront launch may hold: the 32-bit work counter also counts the
+// claims that find no cell left (one per warp), so stay well below 2^32.
+constexpr uint64_t kMaxLaunchCells = 0xF0000000ull;
+
+// Place a job in the launch's cell space after the cells already placed.
+int place_job(DevJob& job, uint64_t pixels, uint32_t bands, uint64_t& cells_so_far, uint32_t& max_cells) {
+    const uint64_t cells = pixels * bands;
+    if (cells_so_far + cells > kMaxLaunchCells)
+        return set_error(SKY_ERR_INVALID_CONFIG, "a launch holds at most 4026531840 (pixel, band) cells");
+    job.cell_begin = uint32_t(cells_so_far);
+    job.cell_count = uint32_t(cells);
+    cells_so_far += cells;
+    max_cells = std::max(max_cells, uint32_t(cells));
+    return SKY_OK;
 }
+
+WaveLaunch wave_launch(const SkyScene* s, const DevJob* dev_jobs, uint32_t n, uint64_t cells, uint32_t max_cells,
+                       uint32_t tracking, uint32_t phase_sampling, uint32_t* counter, unsigned long long* counters,
+                       uint32_t* status) {
+    WaveLaunch w{};
+    w.scene = s->dev;
+    w.jobs = dev_jobs;
+    w.num_jobs = n;
+    w.total_cells = uint32_t(cells);
+    w.max_job_cells = max_cells;
+    w.variant = s->tuning.variant;
+    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
+    w.tracking = tracking;
+    w.phase_sampling = phase_sampling;
+    w.work_counter = counter;
+    w.counters = counters;
+    w.status = status;
+    return w;
+}
+
+// The launch checks read cudaGetLastError(), which also returns an error that
+// an unrelated runtime call of the calling thread left behind; clear it
+// before launching so that only this call's own errors are reported.
+void clear_stale_error() { (void)cudaGetLastError(); }
 
 int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs* o, cudaStream_t stream,
                   bool timed) {
+    clear_stale_error();
     DevLaunch L = make_launch(s, c);
     const uint64_t pixels = uint64_t(c->width) * c->height;
     cudaError_t e;
@@ -220,7 +251,6 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
         return SKY_OK;
     }
-    const uint32_t B = s->dev.band_count;
     DevJob job{};
     job.S = s->dev;
     job.L = L;
@@ -232,33 +262,17 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     job.rgb = rgb;
     job.accumulate = accumulate ? 1u : 0u;
     job.total_spp = total_spp;
-    job.pixels_per_group = s->tuning.pixels_per_group
-                               ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
-                               : pixels_per_group(B, c->spp, s->tuning.pool_variant);
-    job.pixels_per_group = std::max(1u, job.pixels_per_group);
-    job.group_begin = 0;
-    job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
-    PoolLaunch w{};
-    w.jobs = s->jobs;
-    w.num_jobs = 1;
-    w.total_groups = job.group_count;
-    w.tracking = c->tracking;
-    w.phase_sampling = c->phase_sampling;
-    w.work_counter = s->work_counter;
-    w.counters = o->counters;
-    w.status = o->status;
-    const bool with_maj = c->tracking != SKY_TRACKING_MERGED_LAYERS;
-    w.variant = s->tuning.pool_variant;
-    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
-    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
-    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
+    uint64_t cells = 0;
+    uint32_t max_cells = 0;
+    int st = place_job(job, pixels, s->dev.band_count, cells, max_cells);
+    if (st) return st;
+    const WaveLaunch w = wave_launch(s, s->jobs, 1, cells, max_cells, c->tracking, c->phase_sampling,
+                                     s->work_counter, o->counters, o->status);
     if ((e = cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
         return cuda_fail(SKY_ERR_COPY, "job upload", e);
-    if ((e = cudaMemsetAsync(s->work_counter, 0, sizeof(uint32_t), stream)) != cudaSuccess)
-        return cuda_fail(SKY_ERR_LAUNCH, "work counter reset", e);
     if (timed) cudaEventRecord(s->ev_start, stream);
-    e = launch_trace_pool(w, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "persistent tracing kernel launch", e);
+    e = launch_trace_wave(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "wavefront tracing launch", e);
     if (timed) cudaEventRecord(s->ev_stop, stream);
     return SKY_OK;
 }
@@ -396,10 +410,8 @@ extern "C" {
 
 int sky_cuda_scene_set_tuning(SkyScene* s, const SkyTuning* t) {
     if (!s || !t) return set_error(SKY_ERR_INVALID_CONFIG, "scene and tuning must not be null");
-    if (t->pool_variant > 1) return set_error(SKY_ERR_INVALID_CONFIG, "unknown pool variant");
+    if (t->variant >= kWaveVariants) return set_error(SKY_ERR_INVALID_CONFIG, "unknown wavefront kernel variant");
     if (t->max_blocks_per_sm > 64) return set_error(SKY_ERR_INVALID_CONFIG, "max_blocks_per_sm out of range");
-    if (t->pixels_per_group > kPoolMaxCells)
-        return set_error(SKY_ERR_INVALID_CONFIG, "pixels_per_group out of range");
     if (!(t->crossing_cost <= 0.0f) && !(t->crossing_cost < 1e6f))
         return set_error(SKY_ERR_INVALID_CONFIG, "crossing_cost out of range");
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
@@ -503,7 +515,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->host_ground_radius = desc->ground_radius_km;
     s->host_top = desc->top_altitude_km;
     s->tuning.crossing_cost = float(kDefaultCrossingCost);
-    s->tuning.pool_variant = 1;  // 512 resident paths, 3 blocks per SM: the autotuner's usual pick
+    s->tuning.variant = 2;  // 4 blocks per SM: the fastest shape on the production render
     if ((st = upload_tracking_grid(s, h))) {
         sky_cuda_scene_destroy(s);
         return st;
@@ -521,7 +533,6 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
             s->adjoint_unsupported = "differentiable renders need a scene whose only aerosol is species 0; species " +
                                      std::to_string(sp) + " has mass and optics";
     }
-    cudaDeviceGetAttribute(&s->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
     if ((e = cudaMalloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
         (e = cudaMalloc(&s->work_counter, sizeof(uint32_t))) != cudaSuccess) {
         sky_cuda_scene_destroy(s);
@@ -604,7 +615,7 @@ int sky_cuda_render_device(const SkyScene* scene, const SkyRenderConfig* config,
 // ---- batched sweeps ----------------------------------------------------------------
 
 struct SkyBatchGraph {
-    SkyScene* scene = nullptr;
+    int device = 0;                // the scene's device, kept: the graph may outlive its scene handle
     DevJob* jobs = nullptr;        // device job table owned by the graph
     DevJob* host = nullptr;        // pinned copy the graph's memcpy node reads
     uint32_t* counter = nullptr;
@@ -615,12 +626,14 @@ struct SkyBatchGraph {
 
 namespace {
 
-// Fill DevJob rows for a batch; returns the total number of work groups.
-int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* out, uint32_t& groups) {
+// Fill DevJob rows for a batch; returns the batch's cells and its largest job.
+int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* out, uint64_t& cells,
+                     uint32_t& max_cells) {
     if (!s || !jobs || n == 0) return set_error(SKY_ERR_INVALID_CONFIG, "scene and at least one job are required");
     if (!jobs[0].outputs.status) return set_error(SKY_ERR_INVALID_CONFIG, "jobs[0].outputs.status is required");
-    const uint32_t B = s->dev.band_count;
-    groups = 0;
+    if (n > 65535u) return set_error(SKY_ERR_INVALID_CONFIG, "a batch holds at most 65535 jobs");
+    cells = 0;
+    max_cells = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const SkyRenderConfig* c = &jobs[i].config;
         int st = validate_config(s, c);
@@ -654,36 +667,9 @@ int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* o
         job.rgb = s->has_xyz ? jobs[i].outputs.rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
-        job.pixels_per_group = s->tuning.pixels_per_group ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
-                                                           : pixels_per_group(B, c->spp, s->tuning.pool_variant);
-        job.pixels_per_group = std::max(1u, job.pixels_per_group);
-        const uint64_t pixels = uint64_t(c->width) * c->height;
-        job.group_begin = groups;
-        job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
-        if (uint64_t(groups) + job.group_count > 0xffffffffull)
-            return set_error(SKY_ERR_INVALID_CONFIG, "batch has too many work groups");
-        groups += job.group_count;
+        if ((st = place_job(job, uint64_t(c->width) * c->height, s->dev.band_count, cells, max_cells))) return st;
     }
     return SKY_OK;
-}
-
-PoolLaunch batch_launch(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, const DevJob* dev_jobs, uint32_t groups,
-                        uint32_t* counter) {
-    PoolLaunch w{};
-    w.jobs = dev_jobs;
-    w.num_jobs = n;
-    w.total_groups = groups;
-    w.tracking = jobs[0].config.tracking;
-    w.phase_sampling = jobs[0].config.phase_sampling;
-    w.work_counter = counter;
-    w.counters = jobs[0].outputs.counters;
-    w.status = jobs[0].outputs.status;
-    const bool with_maj = w.tracking != SKY_TRACKING_MERGED_LAYERS;
-    w.variant = s->tuning.pool_variant;
-    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
-    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
-    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
-    return w;
 }
 
 int ensure_batch_capacity(SkyScene* s, uint32_t n) {
@@ -717,15 +703,18 @@ extern "C" int sky_cuda_render_batch(const SkyScene* scene, const SkyBatchJob* j
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
     // the previous batch may still read the pinned staging table
     cudaStreamSynchronize(stream);
-    uint32_t groups = 0;
-    if ((st = build_batch_jobs(s, jobs, job_count, s->batch_host, groups))) return st;
+    uint64_t cells = 0;
+    uint32_t max_cells = 0;
+    if ((st = build_batch_jobs(s, jobs, job_count, s->batch_host, cells, max_cells))) return st;
+    clear_stale_error();
     cudaError_t e = cudaMemcpyAsync(s->batch_jobs, s->batch_host, size_t(job_count) * sizeof(DevJob),
                                     cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->batch_counter, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "batch job table upload", e);
-    PoolLaunch w = batch_launch(s, jobs, job_count, s->batch_jobs, groups, s->batch_counter);
-    e = launch_trace_pool(w, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "batched persistent launch", e);
+    const WaveLaunch w = wave_launch(s, s->batch_jobs, job_count, cells, max_cells, jobs[0].config.tracking,
+                                     jobs[0].config.phase_sampling, s->batch_counter, jobs[0].outputs.counters,
+                                     jobs[0].outputs.status);
+    e = launch_trace_wave(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "batched wavefront launch", e);
     return SKY_OK;
 }
 
@@ -737,9 +726,10 @@ extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatch
     if (!s) return set_error(SKY_ERR_INVALID_CONFIG, "scene is null");
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
     SkyBatchGraph* g = new SkyBatchGraph();
-    g->scene = s;
+    g->device = s->device;
     g->job_count = job_count;
-    uint32_t groups = 0;
+    uint64_t cells = 0;
+    uint32_t max_cells = 0;
     cudaError_t e;
     int st = SKY_OK;
     cudaStream_t cap = nullptr;
@@ -747,16 +737,19 @@ extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatch
         (e = cudaMalloc(&g->jobs, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
         (e = cudaMalloc(&g->counter, sizeof(uint32_t))) != cudaSuccess) {
         st = cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch graph allocation", e);
-    } else if ((st = build_batch_jobs(s, jobs, job_count, g->host, groups)) == SKY_OK) {
-        PoolLaunch w = batch_launch(s, jobs, job_count, g->jobs, groups, g->counter);
+    } else if ((st = build_batch_jobs(s, jobs, job_count, g->host, cells, max_cells)) == SKY_OK) {
+        const WaveLaunch w = wave_launch(s, g->jobs, job_count, cells, max_cells, jobs[0].config.tracking,
+                                         jobs[0].config.phase_sampling, g->counter, jobs[0].outputs.counters,
+                                         jobs[0].outputs.status);
+        clear_stale_error();
         if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
             st = cuda_fail(SKY_ERR_DEVICE_INIT, "graph capture", e);
         } else {
             cudaError_t e1 = cudaMemcpyAsync(g->jobs, g->host, size_t(job_count) * sizeof(DevJob),
                                              cudaMemcpyHostToDevice, cap);
-            cudaError_t e2 = cudaMemsetAsync(g->counter, 0, sizeof(uint32_t), cap);
-            cudaError_t e3 = launch_trace_pool(w, cap);
+            cudaError_t e2 = cudaSuccess;
+            cudaError_t e3 = launch_trace_wave(w, cap);
             e = cudaStreamEndCapture(cap, &g->graph);
             if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e != cudaSuccess)
                 st = cuda_fail(SKY_ERR_LAUNCH, "graph capture of the batch",
@@ -776,7 +769,8 @@ extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatch
 
 extern "C" int sky_cuda_batch_graph_launch(SkyBatchGraph* g, void* cuda_stream) {
     if (!g || !g->exec) return set_error(SKY_ERR_INVALID_CONFIG, "graph is null");
-    if (cudaSetDevice(g->scene->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    if (cudaSetDevice(g->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    clear_stale_error();
     cudaError_t e = cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(cuda_stream));
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "graph launch", e);
     return SKY_OK;
@@ -784,7 +778,7 @@ extern "C" int sky_cuda_batch_graph_launch(SkyBatchGraph* g, void* cuda_stream) 
 
 extern "C" void sky_cuda_batch_graph_destroy(SkyBatchGraph* g) {
     if (!g) return;
-    if (g->scene) cudaSetDevice(g->scene->device);
+    cudaSetDevice(g->device);
     cudaDeviceSynchronize();
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
@@ -889,6 +883,7 @@ extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderCo
     const bool accumulate = (config->flags & SKY_FLAG_ACCUMULATE) != 0;
     const uint32_t total_spp = accumulate ? config->sample_offset + config->spp : config->spp;
     const uint64_t pixels = uint64_t(config->width) * config->height;
+    clear_stale_error();
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = launch_adjoint_primal(A, L, outputs->cell_sum, outputs->cell_sumsq, accumulate, outputs->counters,
@@ -920,6 +915,7 @@ extern "C" int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderC
                          "grads.dloss_dfilm and at least one of grads.layer_grad, grads.band_grad are required");
     if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    clear_stale_error();
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = launch_adjoint_grad(A, L, grads->dloss_dfilm, grads->layer_grad, grads->band_grad, grads->counters,
@@ -945,6 +941,7 @@ extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointPa
     int st = adjoint_setup(s, params ? &p : nullptr, A, W);
     if (st) return st;
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+    clear_stale_error();
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = cudaMemcpyAsync(majorants_out, W.layer_maj, size_t(s->dev.band_count) * s->dev.layer_count * sizeof(float),
@@ -1010,6 +1007,7 @@ extern "C" int sky_cuda_score_combos(const float* bands, uint32_t band_count, ui
     std::vector<uint32_t> h_hist(size_t(chunk) * kTargets * kScoreHistBins), tcombo(size_t(chunk) * kTargets),
         tprefix(size_t(chunk) * kTargets);
     std::vector<uint64_t> rank(size_t(chunk) * kTargets);
+    clear_stale_error();
     for (uint32_t c0 = 0; c0 < combo_count; c0 += chunk) {
         const uint32_t nc = std::min(chunk, combo_count - c0);
         if ((e = cudaMemcpyAsync(d_bands, combo_bands + size_t(c0) * channels, size_t(nc) * channels * 4,
@@ -1130,10 +1128,10 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
                                                      std::to_string(SKY_NOALLOC_MAX_JOBS) + ")");
     if (!outputs[0].status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[0].status is required");
     SkyScene* s = const_cast<SkyScene*>(scene);
-    const uint32_t B = s->dev.band_count;
     NoAllocScratch image;
     std::memset(&image, 0, sizeof(image));
-    uint32_t groups = 0;
+    uint64_t cells = 0;
+    uint32_t max_cells = 0;
     for (uint32_t i = 0; i < job_count; ++i) {
         const SkyRenderConfig* c = &job_configs[i];
         int st = validate_config(s, c);
@@ -1154,40 +1152,23 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
         job.rgb = s->has_xyz ? outputs[i].rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
-        job.pixels_per_group = s->tuning.pixels_per_group
-                                   ? std::min(s->tuning.pixels_per_group, kPoolMaxCells / B)
-                                   : pixels_per_group(B, c->spp, s->tuning.pool_variant);
-        job.pixels_per_group = std::max(1u, job.pixels_per_group);
-        job.group_begin = groups;
-        job.group_count = uint32_t((pixels + job.pixels_per_group - 1) / job.pixels_per_group);
-        if (uint64_t(groups) + job.group_count > 0xffffffffull)
-            return set_error(SKY_ERR_INVALID_CONFIG, "batch has too many work groups");
-        groups += job.group_count;
+        if ((st = place_job(job, pixels, s->dev.band_count, cells, max_cells))) return st;
     }
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
     void* scratch = nullptr;
     int st = noalloc_scratch(s->device, &scratch);
     if (st) return st;
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
-    // job table and a zeroed work counter, in one copy (the counter must start at zero)
+    clear_stale_error();
+    // the job table (the launch resets the work counter itself)
     cudaError_t e = cudaMemcpyAsync(scratch, &image, sizeof(image), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "job table upload", e);
-    PoolLaunch w{};
-    w.jobs = static_cast<const DevJob*>(scratch);
-    w.num_jobs = job_count;
-    w.total_groups = groups;
-    w.tracking = job_configs[0].tracking;
-    w.phase_sampling = job_configs[0].phase_sampling;
-    w.work_counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
-                                                 offsetof(NoAllocScratch, work_counter));
-    w.counters = outputs[0].counters;
-    w.status = outputs[0].status;
-    const bool with_maj = job_configs[0].tracking != SKY_TRACKING_MERGED_LAYERS;
-    w.variant = s->tuning.pool_variant;
-    w.layout = plan_pool_layout(s->dev, with_maj, s->tuning.stage_tables != 0, w.variant);
-    if (w.layout.total > uint32_t(s->smem_optin)) w.layout = plan_pool_layout(s->dev, with_maj, false, w.variant);
-    w.max_blocks_per_sm = s->tuning.max_blocks_per_sm;
-    e = launch_trace_pool(w, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "persistent tracing kernel launch", e);
+    uint32_t* counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
+                                                    offsetof(NoAllocScratch, work_counter));
+    const WaveLaunch w = wave_launch(s, static_cast<const DevJob*>(scratch), job_count, cells, max_cells,
+                                     job_configs[0].tracking, job_configs[0].phase_sampling, counter,
+                                     outputs[0].counters, outputs[0].status);
+    e = launch_trace_wave(w, stream);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "wavefront tracing launch", e);
     return SKY_OK;
 }

@@ -120,8 +120,9 @@ struct DevLaunch {
 
 // One render inside a persistent launch: its scene (tables may be shared
 // with other jobs; only the sun differs across an elevation sweep), its
-// launch constants, its outputs and its range of work groups.  A work group
-// is `pixels_per_group` consecutive pixels x all bands x all samples.
+// launch constants, its outputs and its range of the launch's cells.  Cells
+// are (pixel, band) pairs, pixel-major; job j owns the global cells
+// [cell_begin, cell_begin + cell_count).
 struct DevJob {
     DevScene S;
     DevLaunch L;
@@ -132,11 +133,9 @@ struct DevJob {
     double* xyz_var;
     float* rgb;
     uint32_t accumulate;
-    uint32_t total_spp;         // samples behind the sums after this launch
-    uint32_t pixels_per_group;
-    uint32_t group_begin;       // first global group index of the job
-    uint32_t group_count;
-    uint32_t _pad;
+    uint32_t total_spp;   // samples behind the sums after this launch
+    uint32_t cell_begin;  // first global cell of the job
+    uint32_t cell_count;  // width * height * bands
 };
 
 }  // namespace sky

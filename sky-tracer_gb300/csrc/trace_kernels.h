@@ -15,44 +15,41 @@ cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* ce
                                unsigned long long* counters, uint32_t* status, bool accumulate,
                                cudaStream_t stream);
 
-// Block path pool of the persistent wavefront kernel (trace_pool.cu).
-constexpr uint32_t kPoolThreads = 256;
-constexpr uint32_t kPoolMaxSlotsPerThread = 4;  // variant 0: 4 slots/thread, 2 blocks/SM; 1: 2 and 3
-constexpr uint32_t kPoolRing = 4;         // work groups in flight per block
-constexpr uint32_t kPoolMaxCells = 256;   // (pixel, band) cells per work group
+// Persistent wavefront tracer (trace_wave.cu): a ray loop with per-lane chain
+// regeneration over a job table.
+constexpr uint32_t kWaveThreads = 256;
+constexpr uint32_t kWaveVariants = 3;  // resident blocks per SM: variant 0 -> 3, 1 -> 2, 2 -> 4
 
-struct PoolLayout {
-    uint32_t header, jobs, acc, slots, lists, staged;
-    uint32_t knot_z, finder, sigma_t, bands, trk_radius, trk_maj, trk_map, trk_count, trk_off, majorants;
-    uint32_t knot_z_bytes, finder_bytes, sigma_t_bytes, bands_bytes, trk_bytes, trk_map_bytes, trk_count_bytes,
-        majorants_bytes;
-    uint32_t total;
-};
-
-struct PoolLaunch {
-    const DevJob* jobs;            // device array, ascending group_begin
-    uint32_t num_jobs;
-    uint32_t total_groups;
-    PoolLayout layout;
+struct WaveLaunch {
+    DevScene scene;                // tables and constants of every job (jobs differ in their sun frame only)
+    const DevJob* jobs;            // device array, ascending cell_begin
+    uint32_t num_jobs;             // at most 65535
+    uint32_t total_cells;          // sum of the jobs' cell counts
+    uint32_t max_job_cells;        // cells of the largest job
+    uint32_t variant;              // kernel shape, < kWaveVariants
     uint32_t max_blocks_per_sm;    // 0 = as many as fit
-    uint32_t variant;              // pool shape (slots per thread, blocks per SM)
     uint32_t tracking, phase_sampling;
-    uint32_t* work_counter;        // zeroed before the launch
+    uint32_t* work_counter;        // reset by the launch itself
     unsigned long long* counters;  // may be null
     uint32_t* status;
 };
 
-// Persistent wavefront tracer over a job table.  Writes the cell sums, film
-// and XYZ of every job directly (no finalize launch needed).
-cudaError_t launch_trace_pool(const PoolLaunch& w, cudaStream_t stream);
-PoolLayout plan_pool_layout(const DevScene& S, bool with_majorants, bool stage_tables, uint32_t variant);
-uint32_t pool_slots_per_thread(uint32_t variant);
+// Prepare, trace and finalize every job of `w` (three kernels on `stream`):
+// the jobs' cell sums (zeroed first unless a job accumulates), film, XYZ,
+// XYZ variance and linear sRGB.
+cudaError_t launch_trace_wave(const WaveLaunch& w, cudaStream_t stream);
+uint32_t wave_blocks_per_sm(uint32_t variant);
 
 // Mean film, XYZ, XYZ variance and linear sRGB from the per-cell sums (any
 // output may be null; xyz_var needs cell_sumsq).
 cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_spp, const double* cell_sum,
                             const double* cell_sumsq, float* film, double* xyz, double* xyz_var, float* rgb,
                             cudaStream_t stream);
+
+// The same for every job of a job table (one warp per pixel of the jobs'
+// concatenated pixels; jobs without film / XYZ / RGB outputs are skipped).
+cudaError_t launch_finalize_jobs(const DevScene& S, const DevJob* jobs, uint32_t num_jobs, uint32_t total_cells,
+                                 cudaStream_t stream);
 
 // XYZ -> white-balanced linear sRGB of a scene (kernel argument copy).
 struct RgbMatrix {

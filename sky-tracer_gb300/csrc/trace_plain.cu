@@ -15,111 +15,6 @@
 namespace sky {
 namespace {
 
-// Layered delta tracking along one ray (sample_real_collision and
-// delta_transmittance, sky_trace.wgsl:405-475).  Returns true at a real
-// collision (t_hit set).  kTracking selects the reference's per-segment
-// restart or the residual carry (same distribution, fewer draws).
-// Residual-carry delta tracking over the band's merged tracking grid.
-__device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo& g, float t_max, uint32_t band,
-                                                 Rng& rng, float& t_hit, Counters& n, bool& watchdog) {
-    const MergedGrid G = merged_grid(S, band);
-    const float2* sig_row = S.sigma_t + band * S.knot_count;
-    float t = 0.0f;
-    int m = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_max), S.ground_radius));
-    int dir;
-    float t_seg = merged_crossing(G, g, m, t, t_max, dir);
-    float maj = __ldg(G.maj + m);
-    ++n.e[SKY_EVENT_SEGMENT];
-    float tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
-    uint32_t guard = 0;
-    for (;;) {
-        float dt = tau / maj;
-        if (t + dt < t_seg) {
-            t = t + dt;
-            ++n.e[SKY_EVENT_TRACK_STEP];
-            float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
-            if (rng.next() * maj < sig) {
-                t_hit = t;
-                return true;
-            }
-            tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
-        } else {
-            if (dir == 0) return false;
-            if (++guard > 100000u) {
-                watchdog = true;
-                return false;
-            }
-            tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
-            t = t_seg;
-            m += dir;
-            t_seg = merged_crossing(G, g, m, t, t_max, dir);
-            maj = __ldg(G.maj + m);
-            ++n.e[SKY_EVENT_SEGMENT];
-        }
-    }
-}
-
-template <int kTracking>
-__device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, float t_max, uint32_t band, Rng& rng,
-                                          float& t_hit, Counters& n, bool& watchdog) {
-    if (kTracking == SKY_TRACKING_MERGED_LAYERS) return track_ray_merged(S, g, t_max, band, rng, t_hit, n, watchdog);
-    const float* maj_row = S.majorants + band * S.layer_count;
-    const float2* sig_row = S.sigma_t + band * S.knot_count;
-    float t = 0.0f;
-    uint32_t guard = 0;
-    float tau = 0.0f;
-    bool need_draw = true;
-    for (;;) {
-        if (t >= t_max) return false;
-        if (guard > 100000u) {
-            watchdog = true;
-            return false;
-        }
-        ++guard;
-        uint32_t layer;
-        float seg_end = next_segment_end(S, g, t, t_max, layer);
-        ++n.e[SKY_EVENT_SEGMENT];
-        float maj = fmaxf(__ldg(maj_row + layer), 0.00000001f);
-        if (kTracking == SKY_TRACKING_RESIDUAL_CARRY) {
-            for (;;) {
-                if (need_draw) {
-                    tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
-                    need_draw = false;
-                }
-                float dt = tau / maj;
-                if (t + dt >= seg_end) {
-                    tau = fmaxf(tau - (seg_end - t) * maj, 0.0f);
-                    break;
-                }
-                t = t + dt;
-                need_draw = true;
-                ++n.e[SKY_EVENT_TRACK_STEP];
-                float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, alt);
-                if (rng.next() * maj < sig) {
-                    t_hit = t;
-                    return true;
-                }
-            }
-        } else {
-            for (;;) {
-                if (t >= seg_end) break;
-                float u = fmaxf(1.0f - rng.next(), 0.0000001f);
-                t = t - __logf(u) / maj;
-                if (t >= seg_end) break;
-                ++n.e[SKY_EVENT_TRACK_STEP];
-                float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, alt);
-                if (rng.next() * maj < sig) {
-                    t_hit = t;
-                    return true;
-                }
-            }
-        }
-        t = seg_end;
-    }
-}
-
 // Binary transmittance of a shadow ray from `pos` towards `ldir` (sky_trace.wgsl:574-577):
 // 0 when the ray hits the ground or collides, 1 otherwise.
 template <int kTracking>

@@ -105,7 +105,7 @@ class SkyDeviceOutputs(ctypes.Structure):
 
 class SkyTuning(ctypes.Structure):
     _fields_ = [
-        ("pool_variant", _u32), ("max_blocks_per_sm", _u32), ("stage_tables", _u32), ("pixels_per_group", _u32),
+        ("variant", _u32), ("max_blocks_per_sm", _u32), ("_unused", _u32 * 2),
         ("crossing_cost", _f), ("_reserved", _u32 * 3),
     ]
 

@@ -1,14 +1,13 @@
-"""Autotuner of the persistent tracer's launch shape.
+"""Autotuner of the wavefront tracer's launch shape.
 
 The reference dispatches a fixed 8x8x1 workgroup per (pixel block, band) and
 two samples per dispatch (integrator.rs:254-283); nothing is tuned.  Here the
-shape of the persistent kernel is a per-scene setting (SkyTuning): the
-resident path pool per block and blocks per SM (queue depth), table staging
-in shared memory, pixels per work group (regeneration granularity) and the
-crossing cost that sets how far the tracking grid is merged.  `autotune`
-times each candidate on a reduced-sample probe of the caller's own render
-(same image, same scene, fewer samples per pixel) with CUDA events and keeps
-the fastest on the scene.
+shape of the wavefront kernel is a per-scene setting (SkyTuning): the
+resident blocks per SM it is compiled for (registers per lane against lanes
+in flight) and the crossing cost that sets how far the tracking grid is
+merged.  `autotune` times each candidate on a reduced-sample probe of the
+caller's own render (same image, same scene, fewer samples per pixel) with
+CUDA events and keeps the fastest on the scene.
 """
 
 from __future__ import annotations
@@ -19,8 +18,7 @@ from dataclasses import replace
 from .render import GpuScene, RenderConfig
 
 DEFAULT_SPACE = {
-    "pool_variant": (0, 1),
-    "stage_tables": (0, 1),
+    "variant": (0, 1, 2),
     "crossing_cost": (0.1, 0.25, 0.5, 1.0),
 }
 

@@ -13,6 +13,7 @@ and frees inside the call, like the reference.
 from __future__ import annotations
 
 import ctypes
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -112,9 +113,12 @@ class GpuScene:
         handle = ctypes.c_void_p()
         check(self.lib.sky_cuda_scene_create(ctypes.byref(self._desc), ctypes.byref(handle)), self.lib)
         self.handle = handle
+        self._graphs = weakref.WeakSet()  # batch graphs replay this scene's tables
 
     def close(self) -> None:
         if getattr(self, "handle", None) and self.handle.value:
+            for g in list(getattr(self, "_graphs", ())):
+                g.close()
             self.lib.sky_cuda_scene_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
@@ -133,8 +137,7 @@ class GpuScene:
     def get_tuning(self) -> dict:
         t = SkyTuning()
         check(self.lib.sky_cuda_scene_get_tuning(self.handle, ctypes.byref(t)), self.lib)
-        return {"pool_variant": t.pool_variant, "max_blocks_per_sm": t.max_blocks_per_sm,
-                "stage_tables": t.stage_tables, "pixels_per_group": t.pixels_per_group,
+        return {"variant": t.variant, "max_blocks_per_sm": t.max_blocks_per_sm,
                 "crossing_cost": float(t.crossing_cost)}
 
     def set_tuning(self, **kw) -> None:
@@ -225,6 +228,7 @@ class BatchGraph:
         check(self.lib.sky_cuda_batch_graph_create(gs.handle, self._jobs, len(jobs), ctypes.byref(handle)),
               self.lib)
         self.handle = handle
+        gs._graphs.add(self)
 
     def launch(self, stream: int = 0) -> None:
         check(self.lib.sky_cuda_batch_graph_launch(self.handle, ctypes.c_void_p(stream)), self.lib)

@@ -231,14 +231,14 @@ def test_reference_default_band_count(gpu, ref_scene):
     assert st == 0 and r["frac_beyond_3se"] <= 0.03
 
 
-@pytest.mark.parametrize("variant,stage,cost", [(0, 0, 0.25), (0, 1, 0.5), (1, 0, 0.1), (1, 1, 1.0)])
-def test_pool_shapes_trace_the_same_chains(gpu, dome_scene, variant, stage, cost):
+@pytest.mark.parametrize("variant,cost", [(0, 0.25), (1, 0.5), (2, 0.1), (2, 1.0)])
+def test_wavefront_shapes_trace_the_same_chains(gpu, dome_scene, variant, cost):
     """Every launch shape the autotuner can pick traces the plain kernel's
     paths (the crossing cost changes the tracking grid for both kernels)."""
     with GpuScene(dome_scene) as gs:
-        gs.set_tuning(pool_variant=variant, stage_tables=stage, crossing_cost=cost)
+        gs.set_tuning(variant=variant, crossing_cost=cost)
         t = gs.get_tuning()
-        assert t["pool_variant"] == variant and t["stage_tables"] == stage and abs(t["crossing_cost"] - cost) < 1e-6
+        assert t["variant"] == variant and abs(t["crossing_cost"] - cost) < 1e-6
         cfg = RenderConfig(width=32, height=16, spp=2, sample_offset=5, phase_sampling=_abi.PHASE_TABULATED,
                            tracking=_abi.TRACKING_MERGED_LAYERS, max_orders=16)
         a, _, _, _ = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_PLAIN}))
@@ -252,7 +252,7 @@ def test_autotuner_picks_a_measured_shape(gpu, dome_scene):
     cfg = RenderConfig(width=64, height=32, spp=64, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS)
     with GpuScene(dome_scene) as gs:
-        best, results = autotune(gs, cfg, space={"pool_variant": (0, 1), "crossing_cost": (0.25, 0.5)})
+        best, results = autotune(gs, cfg, space={"variant": (0, 2), "crossing_cost": (0.25, 0.5)})
         assert len(results) == 4 and all(ms > 0 for _, ms in results)
         assert best == min(results, key=lambda r: r[1])[0]
         assert gs.get_tuning() == best
