@@ -555,7 +555,7 @@ enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLigh
                   kNextIdle = 5u };
 
 template <int kPhase>
-__global__ void __launch_bounds__(256, 2) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
+__global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
                                                               double* __restrict__ layer_grad,
