@@ -91,95 +91,75 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
             if (lane == 0u) atomicOr(status, 2u);
             break;
         }
+        // a chain that ended after its last ray: its radiance joins the cell's sums
+        if (next == kEnd) {
+            const double rd = double(rad);
+            acc_sum += rd;
+            acc_sq += rd * rd;
+            next = kIdle;
+        }
+        // idle lanes take the next samples of the warp's cell
 #pragma unroll 1
-        for (int round = 0; round < 2; ++round) {
-            // idle lanes take the next samples of the warp's cell
-#pragma unroll 1
-            for (;;) {
-                const uint32_t need = __ballot_sync(kFull, next == kIdle);
-                if (need == 0u || exhausted) break;
-                if (claim_next >= claim_spp) {
-                    uint32_t gc = 0u;
-                    if (lane == 0u) gc = atomicAdd(work_counter, 1u);
-                    gc = __shfl_sync(kFull, gc, 0);
-                    if (gc >= total_cells) {
-                        exhausted = true;
-                        break;
-                    }
-                    claim_job = job_of(jobs, num_jobs, gc);
-                    claim_cell = gc - __ldg(&jobs[claim_job].cell_begin);
-                    claim_spp = __ldg(&jobs[claim_job].L.spp);
-                    claim_next = 0u;
+        for (;;) {
+            const uint32_t need = __ballot_sync(kFull, next == kIdle);
+            if (need == 0u || exhausted) break;
+            if (claim_next >= claim_spp) {
+                uint32_t gc = 0u;
+                if (lane == 0u) gc = atomicAdd(work_counter, 1u);
+                gc = __shfl_sync(kFull, gc, 0);
+                if (gc >= total_cells) {
+                    exhausted = true;
+                    break;
                 }
-                const uint32_t rank = __popc(need & ((1u << lane) - 1u));
-                if (next == kIdle && claim_next + rank < claim_spp) {
-                    job = claim_job;
-                    cell = claim_cell;
-                    sample = claim_next + rank;
-                    next = kStart;
-                }
-                claim_next = min(claim_spp, claim_next + uint32_t(__popc(need)));
+                claim_job = job_of(jobs, num_jobs, gc);
+                claim_cell = gc - __ldg(&jobs[claim_job].cell_begin);
+                claim_spp = __ldg(&jobs[claim_job].L.spp);
+                claim_next = 0u;
             }
-            // event code up to the lane's next ray
-#pragma unroll 1
-            while (next != kIdle && next != kTrace) {
-                const DevJob& J = jobs[job];
-                if (next == kEnd) {
-                    const double rd = double(rad);
-                    acc_sum += rd;
-                    acc_sq += rd * rd;
-                    next = kIdle;
-                    continue;
-                }
-                if (next == kStart) {
-                    if (cell != acc_cell || job != acc_job) {
-                        if (acc_cell != kNoCell) {
-                            const DevJob& A = jobs[acc_job];
-                            atomicAdd(A.cell_sum + acc_cell, acc_sum);
-                            double* sq = A.cell_sumsq;
-                            if (sq) atomicAdd(sq + acc_cell, acc_sq);
-                        }
-                        acc_job = job;
-                        acc_cell = cell;
-                        acc_sum = acc_sq = 0.0;
+            const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+            if (next == kIdle && claim_next + rank < claim_spp) {
+                job = claim_job;
+                cell = claim_cell;
+                sample = claim_next + rank;
+                next = kStart;
+            }
+            claim_next = min(claim_spp, claim_next + uint32_t(__popc(need)));
+        }
+        // event code up to the lane's next ray, one pass in flow order (start,
+        // lights / continuation, outgoing ray), so that each block runs once
+        // per iteration for every lane that needs it
+        if (next != kIdle && next != kTrace) {
+            const DevJob& J = jobs[job];
+            if (next == kStart) {
+                if (cell != acc_cell || job != acc_job) {
+                    if (acc_cell != kNoCell) {
+                        const DevJob& A = jobs[acc_job];
+                        atomicAdd(A.cell_sum + acc_cell, acc_sum);
+                        double* sq = A.cell_sumsq;
+                        if (sq) atomicAdd(sq + acc_cell, acc_sq);
                     }
-                    band = cell % S.band_count;
-                    const uint32_t pixel = cell / S.band_count;
-                    const uint32_t width = __ldg(&J.L.width);
-                    const uint32_t x = pixel % width, y = pixel / width;
-                    rng.init(pixel, __ldg(&J.L.sample_offset) + sample, band, __ldg(&J.L.seed_lo),
-                             __ldg(&J.L.seed_hi));
-                    dir = camera_dir(J.L, x, y, rng);
-                    org = mk(0.0f, S.ground_radius + fmaxf(__ldg(&J.L.observer_altitude), 0.0f), 0.0f);
-                    ++n.e[SKY_EVENT_CHAIN];
-                    thr = 1.0f;
-                    rad = 0.0f;
-                    depth = 0u;
-                    next = kPrimary;
+                    acc_job = job;
+                    acc_cell = cell;
+                    acc_sum = acc_sq = 0.0;
                 }
-                if (next == kPrimary) {  // sky_trace.wgsl:709-717
-                    if (depth >= __ldg(&J.L.watchdog_limit)) {
-                        watchdog = true;
-                        next = kEnd;
-                        continue;
-                    }
-                    const uint32_t max_orders = __ldg(&J.L.max_orders);
-                    g = ray_geo(org, dir);
-                    ++n.e[SKY_EVENT_BOUNDARY];
-                    if ((max_orders != 0u && depth >= max_orders) || !next_boundary(S, g, t_max, boundary)) {
-                        rad = fmaxf(rad, 0.0f);
-                        next = kEnd;
-                        continue;
-                    }
-                    shadow_ray = false;
-                    next = kTrace;
-                    continue;
-                }
-                // kLights: direct_sun_at_scatter (sky_trace.wgsl:566-585) and
-                // ground_radiance (:587-608), one shadow ray at a time
+                band = cell % S.band_count;
+                const uint32_t pixel = cell / S.band_count;
+                const uint32_t width = __ldg(&J.L.width);
+                const uint32_t x = pixel % width, y = pixel / width;
+                rng.init(pixel, __ldg(&J.L.sample_offset) + sample, band, __ldg(&J.L.seed_lo), __ldg(&J.L.seed_hi));
+                dir = camera_dir(J.L, x, y, rng);
+                org = mk(0.0f, S.ground_radius + fmaxf(__ldg(&J.L.observer_altitude), 0.0f), 0.0f);
+                ++n.e[SKY_EVENT_CHAIN];
+                thr = 1.0f;
+                rad = 0.0f;
+                depth = 0u;
+                next = kPrimary;
+            }
+            if (next == kLights) {
+                // direct_sun_at_scatter (sky_trace.wgsl:566-585) and ground_radiance
+                // (:587-608), one shadow ray at a time
                 const uint32_t lights = __ldg(&J.L.direct_light_samples);
                 const float l_sun = __ldg(&S.bands[band].solar_radiance);
-                bool shadow = false;
                 while (ls < lights) {
                     ++ls;
                     const V3 ldir = sample_sun_cone(J.S, rng);
@@ -200,60 +180,74 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                         const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
                         term = l_sun * 1.0f * mixed_phase(S, c, band, dot3(dir, ldir)) / S.light_pdf;
                     }
-                    shadow = true;
-                    break;
-                }
-                if (shadow) {
                     shadow_ray = true;
                     next = kTrace;
-                    continue;
+                    break;
                 }
-                // the continuation (sky_trace.wgsl:728-767)
-                rad += thr * (nee * (1.0f / float(lights)));
-                V3 nd;
-                if (!ground) {
-                    const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
-                    if (kPhase == SKY_PHASE_TABULATED) {
-                        thr *= sample_tabulated(S, c, band, dir, rng, nd);
+                if (next == kLights) {
+                    // the continuation (sky_trace.wgsl:728-767)
+                    rad += thr * (nee * (1.0f / float(lights)));
+                    V3 nd;
+                    bool alive = true;
+                    if (!ground) {
+                        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+                        if (kPhase == SKY_PHASE_TABULATED) {
+                            thr *= sample_tabulated(S, c, band, dir, rng, nd);
+                        } else {
+                            nd = sample_isotropic(rng);
+                            thr *= mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                        }
                     } else {
-                        nd = sample_isotropic(rng);
-                        thr *= mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                        const V3 normal = normalize_or_y(org);
+                        float pdf;
+                        nd = sample_cosine_hemisphere(normal, rng, pdf);
+                        const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+                        if (pdf <= 0.0f || cos_out <= 0.0f) alive = false;
+                        else thr *= S.ground_albedo * kInvPi * cos_out / pdf;
                     }
-                } else {
-                    const V3 normal = normalize_or_y(org);
-                    float pdf;
-                    nd = sample_cosine_hemisphere(normal, rng, pdf);
-                    const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
-                    if (pdf <= 0.0f || cos_out <= 0.0f) {
+                    if (alive && depth >= __ldg(&J.L.rr_start_depth)) {  // russian_roulette (:691-701)
+                        const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
+                        if (rng.next() > q) alive = false;
+                        else thr = thr / q;
+                    }
+                    if (!alive) {
                         rad = fmaxf(rad, 0.0f);
                         next = kEnd;
-                        continue;
+                    } else {
+                        org = madd(org, nd, kRayEpsilonKm);
+                        dir = nd;
+                        if (rad < 0.0f || rad != rad || thr < 0.0f || thr != thr) {
+                            rad = 0.0f;
+                            next = kEnd;
+                        } else {
+                            ++depth;
+                            next = kPrimary;
+                        }
                     }
-                    thr *= S.ground_albedo * kInvPi * cos_out / pdf;
                 }
-                if (depth >= __ldg(&J.L.rr_start_depth)) {  // russian_roulette (sky_trace.wgsl:691-701)
-                    const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
-                    if (rng.next() > q) {
-                        rad = fmaxf(rad, 0.0f);
-                        next = kEnd;
-                        continue;
-                    }
-                    thr = thr / q;
-                }
-                org = madd(org, nd, kRayEpsilonKm);
-                dir = nd;
-                if (rad < 0.0f || rad != rad || thr < 0.0f || thr != thr) {
-                    rad = 0.0f;
+            }
+            if (next == kPrimary) {  // the outgoing ray (sky_trace.wgsl:709-717)
+                const uint32_t max_orders = __ldg(&J.L.max_orders);
+                if (depth >= __ldg(&J.L.watchdog_limit)) {
+                    watchdog = true;
                     next = kEnd;
-                    continue;
+                } else {
+                    g = ray_geo(org, dir);
+                    ++n.e[SKY_EVENT_BOUNDARY];
+                    if ((max_orders != 0u && depth >= max_orders) || !next_boundary(S, g, t_max, boundary)) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kEnd;
+                    } else {
+                        shadow_ray = false;
+                        next = kTrace;
+                    }
                 }
-                ++depth;
-                next = kPrimary;
             }
         }
         const bool tracing = next == kTrace;
         if (!__any_sync(kFull, tracing)) {
-            if (exhausted) break;  // every lane idle and no cell left
+            // every lane idle (or ending a chain, summed next iteration) and no cell left
+            if (exhausted && !__any_sync(kFull, next == kEnd)) break;
             continue;
         }
         if (tracing) {
