@@ -76,6 +76,8 @@ def parse_args():
     p.add_argument("--workload", choices=sorted(WORKLOADS) + [SWEEP_WORKLOAD, ADJOINT_WORKLOAD, FIT_WORKLOAD],
                    default=DEFAULT_WORKLOAD)
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
+    p.add_argument("--tuning", default="",
+                   help="SkyTuning fields set before autotuning, e.g. variant=0,track_slice=3")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-peak", action="store_true", help="skip the SGEMM FP32-peak measurement")
@@ -622,6 +624,9 @@ def main():
     chains = cells * cfg.spp
 
     gs = GpuScene(scene)
+    if args.tuning:
+        gs.set_tuning(**{k: (float(v) if k == "crossing_cost" else int(v))
+                         for k, v in (kv.split("=") for kv in args.tuning.split(","))})
     tuning_log = None
     if not args.no_autotune and cfg.kernel != 1:
         from sky_cuda.autotune import autotune
