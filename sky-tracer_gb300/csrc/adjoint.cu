@@ -549,12 +549,14 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
 // C_after of the factors needs it), pass 1 for the gradient terms; both take
 // the same path.  Random numbers are drawn in adj_chain's order, so the
 // replay follows the primal render's paths.  P = Q (a gradient is taken at
-// the sampling parameters).
+// the sampling parameters).  Without kGrad the kernel is the primal render
+// of P = Q: pass 0 only, each lane keeping the FP64 sums of its current cell
+// and adding them to the cell when it moves on (cells add in no fixed order).
 enum : uint32_t { kRayPrimary = 0u, kRayShadow = 1u, kRayRetrace = 2u };
 enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLights = 3u, kNextEnd = 4u,
                   kNextIdle = 5u };
 
-template <int kPhase>
+template <int kPhase, bool kGrad>
 __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
@@ -562,7 +564,9 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                                                               double* __restrict__ band_grad,
                                                               unsigned long long* __restrict__ counters,
                                                               uint32_t* __restrict__ status, uint32_t cells,
-                                                              uint32_t copies, uint32_t* __restrict__ next_cell) {
+                                                              uint32_t copies, uint32_t* __restrict__ next_cell,
+                                                              double* __restrict__ cell_sum,
+                                                              double* __restrict__ cell_sumsq) {
     extern __shared__ float smem[];
     const DevScene& S = A.S;
     const uint32_t Lc = S.layer_count, B = S.band_count, bins = S.phase_bins;
@@ -570,10 +574,15 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     // layer gradients: one FP32 copy per warp when they fit (only a warp's own
     // lanes contend); band gradients: one copy per block
-    float* sg = layer_grad ? smem + (warp % copies) * nlayer : nullptr;
+    float* sg = kGrad && layer_grad ? smem + (warp % copies) * nlayer : nullptr;
     float* sb = smem + copies * nlayer;
-    for (uint32_t i = threadIdx.x; i < copies * nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
-    __syncthreads();
+    if (kGrad) {
+        for (uint32_t i = threadIdx.x; i < copies * nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
+        __syncthreads();
+    }
+    // primal: FP64 sums of the lane's current cell
+    uint32_t acc_cell = 0xffffffffu;
+    double acc_sum = 0.0, acc_sq = 0.0;
     Counters n;
     n.clear();
     bool watchdog = false;
@@ -607,7 +616,7 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                     uint32_t cn = 0u;
                     if (lane == 0u) {
                         do cn = atomicAdd(next_cell, 1u);
-                        while (cn < cells && __ldg(dloss + cn) == 0.0f);  // no loss: no gradient
+                        while (kGrad && cn < cells && __ldg(dloss + cn) == 0.0f);  // no loss: no gradient
                     }
                     cn = __shfl_sync(0xffffffffu, cn, 0);
                     if (cn >= cells) {
@@ -630,7 +639,12 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
 #pragma unroll 1
             while (next != kNextIdle && next != kNextTrace) {
                 if (next == kNextEnd) {
-                    if (pass == 0u) {
+                    if (!kGrad) {
+                        const double rd = double(resolve(A.P, Lc, band).kS * rad);
+                        acc_sum += rd;
+                        acc_sq += rd * rd;
+                        next = kNextIdle;
+                    } else if (pass == 0u) {
                         total = rad;
                         if (total > 0.0f) {
                             pass = 1u;
@@ -655,10 +669,18 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                     continue;
                 }
                 if (next == kNextStart) {
+                    if (!kGrad && cell != acc_cell) {
+                        if (acc_cell != 0xffffffffu) {
+                            atomicAdd(cell_sum + acc_cell, acc_sum);
+                            if (cell_sumsq) atomicAdd(cell_sumsq + acc_cell, acc_sq);
+                        }
+                        acc_cell = cell;
+                        acc_sum = acc_sq = 0.0;
+                    }
                     band = cell % L.band_count;
                     const uint32_t pixel = cell / L.band_count;
                     const uint32_t x = pixel % L.width, y = pixel / L.width;
-                    wc = __ldg(dloss + cell) * inv_spp;
+                    wc = kGrad ? __ldg(dloss + cell) * inv_spp : 0.0f;
                     rng.init(pixel, L.sample_offset + sample, band, L.seed_lo, L.seed_hi);
                     dir = camera_dir(L, x, y, rng);
                     org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
@@ -744,7 +766,7 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                         fq = vertex_phase(P, bins, mq, mu_c) / mq.s / kIsotropicPdf;
                     }
                     thr *= fq;
-                    if (pass == 1u) vertex_terms(acc, P, bins, hb, mq, mu_c, w * (total - rad));
+                    if (kGrad && pass == 1u) vertex_terms(acc, P, bins, hb, mq, mu_c, w * (total - rad));
                 } else {
                     // the Lambert bounce (sky_trace.wgsl:750-766)
                     const V3 normal = normalize_or_y(org);
@@ -787,7 +809,7 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
         if (tracing) {
             const AdjSet P = resolve(A.P, Lc, band);
             const float w = wc * P.kS;
-            const bool grad = pass == 1u;
+            const bool grad = kGrad && pass == 1u;
             const float gw = ray == kRayPrimary ? (grad ? w * (total - rad) : 0.0f) : (ray == kRayRetrace ? c : 0.0f);
             const uint32_t dim_seg = rng.dim;
             float t_hit = 0.0f, w_eval = 1.0f, tau_bar = 0.0f;
@@ -859,6 +881,13 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
     }
     flush_counters(n, counters, lane);
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
+    if (!kGrad) {
+        if (acc_cell != 0xffffffffu) {
+            atomicAdd(cell_sum + acc_cell, acc_sum);
+            if (cell_sumsq) atomicAdd(cell_sumsq + acc_cell, acc_sq);
+        }
+        return;
+    }
     __syncthreads();
     for (uint32_t i = threadIdx.x; layer_grad && i < nlayer; i += blockDim.x) {
         float v = 0.0f;
@@ -1045,8 +1074,31 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  cudaStream_t stream) {
+                                  uint32_t* next_cell, cudaStream_t stream) {
     const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    cudaError_t e;
+    if (!A.distinct && cells <= 0xffffffffull) {
+        // P = Q: the ray loop, adding into the cell sums
+        if (!accumulate) {
+            if ((e = cudaMemsetAsync(cell_sum, 0, cells * sizeof(double), stream)) != cudaSuccess) return e;
+            if (cell_sumsq && (e = cudaMemsetAsync(cell_sumsq, 0, cells * sizeof(double), stream)) != cudaSuccess)
+                return e;
+        }
+        if ((e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
+        const uint64_t want = (cells * 32u + 255u) / 256u;
+        const uint32_t n = static_cast<uint32_t>(cells);
+        if (L.phase_sampling == SKY_PHASE_TABULATED) {
+            const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED, false>);
+            adjoint_grad_kernel<SKY_PHASE_TABULATED, false><<<grid_blocks(k, 256, 0, want), 256, 0, stream>>>(
+                A, L, nullptr, nullptr, nullptr, counters, status, n, 0u, next_cell, cell_sum, cell_sumsq);
+        } else {
+            const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, false>);
+            adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, false><<<grid_blocks(k, 256, 0, want), 256, 0, stream>>>(
+                A, L, nullptr, nullptr, nullptr, counters, status, n, 0u, next_cell, cell_sum, cell_sumsq);
+        }
+        return cudaGetLastError();
+    }
+    // sampling under Q, evaluation under P: a warp per cell
     const uint64_t blocks = (cells * 32u + 255u) / 256u;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     const dim3 grid(static_cast<uint32_t>(blocks));
@@ -1074,15 +1126,15 @@ cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float
     const uint64_t want = (cells * 32u + 255u) / 256u;
     const uint32_t n = static_cast<uint32_t>(cells);
     if (L.phase_sampling == SKY_PHASE_TABULATED) {
-        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED>);
+        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED, true>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_TABULATED><<<blocks, 256, smem, stream>>>(
-            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell);
+        adjoint_grad_kernel<SKY_PHASE_TABULATED, true><<<blocks, 256, smem, stream>>>(
+            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell, nullptr, nullptr);
     } else {
-        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC>);
+        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, true>);
         const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC><<<blocks, 256, smem, stream>>>(
-            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell);
+        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, true><<<blocks, 256, smem, stream>>>(
+            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell, nullptr, nullptr);
     }
     return cudaGetLastError();
 }

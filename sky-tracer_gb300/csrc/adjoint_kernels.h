@@ -72,10 +72,12 @@ AdjWorkspace adjoint_workspace(void* base, uint32_t B, uint32_t L, uint32_t bins
 cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaStream_t stream);
 
 // Primal render over the parameterised medium: per-cell sums (and squares)
-// of the radiance of P, sampled with Q.
+// of the radiance of P, sampled with Q.  With P = Q it runs the ray loop of
+// the adjoint kernel (next_cell is its work counter); otherwise a warp per
+// cell.
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  cudaStream_t stream);
+                                  uint32_t* next_cell, cudaStream_t stream);
 
 // Path-replay gradient (P == Q): adds dLoss/dparams to layer_grad [3 L + 2]
 // and band_grad [B][4] (may be null) given dLoss/dfilm [pixels][B].

@@ -887,7 +887,7 @@ extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderCo
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
     e = launch_adjoint_primal(A, L, outputs->cell_sum, outputs->cell_sumsq, accumulate, outputs->counters,
-                              outputs->status, stream);
+                              outputs->status, W.next_cell, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
     e = launch_finalize(A.S, pixels, total_spp, outputs->cell_sum, outputs->cell_sumsq, outputs->film,
                         s->has_xyz ? outputs->xyz : nullptr, s->has_xyz ? outputs->xyz_var : nullptr,
