@@ -484,6 +484,41 @@ int sky_cuda_score_combos(const float* bands, uint32_t band_count, uint64_t samp
                           float reference_scale, const uint32_t* combo_bands, const float* combo_xyz,
                           uint32_t combo_count, uint32_t channels, SkyComboScore* results, void* cuda_stream);
 
+/* ---- Mie phase-table bake ---------------------------------------------- */
+
+/* Lognormal size distribution of one aerosol species: r_count radii spaced
+ * geometrically on [r_min_um, r_max_um], weights exp(-ln^2(r/r_mode) /
+ * (2 ln^2 sigma_g)) normalised to 1 (scripts/bake_opac_data.py:20-53, :103-109). */
+typedef struct SkyMieDistribution {
+    double r_mode_um;
+    double sigma_g;      /* geometric standard deviation, > 1 */
+    double r_min_um;
+    double r_max_um;
+    uint32_t r_count;
+    uint32_t _reserved;
+} SkyMieDistribution;
+
+/* Size-averaged optics of one band (weights summing to 1; um^2). */
+typedef struct SkyMieBand {
+    double sigma_sca_um2;  /* sum_r w_r pi r^2 Q_sca(r)                         */
+    double sigma_ext_um2;  /* sum_r w_r pi r^2 Q_ext(r)                         */
+    double g;              /* asymmetry parameter of the averaged phase function */
+} SkyMieBand;
+
+/*
+ * Bake the size-averaged Mie phase function of one species, per band, on the
+ * cube-root mu grid mu_j = 1 - 2 ((j + 0.5) / phase_bins)^3:
+ * phase_out[band * phase_bins + j], normalised to 1 over the sphere, i.e.
+ * size_dist_phase of scripts/bake_opac_data.py:112-121 (its miepython sphere
+ * restated from the published Mie series).  The particle's refractive index
+ * per band is refr_re + i refr_im (refr_im >= 0 absorbs); wavelengths in um.
+ * band_out (may be null) receives the averaged cross sections and g.
+ * Synchronous, on the current device; no scene needed.
+ */
+int sky_cuda_bake_mie_phase(const SkyMieDistribution* dist, const double* wavelength_um, const double* refr_re,
+                            const double* refr_im, uint32_t band_count, uint32_t phase_bins, double* phase_out,
+                            SkyMieBand* band_out);
+
 /*
  * Allocation-free render of up to SKY_NOALLOC_MAX_JOBS jobs of one scene in a
  * single launch of the wavefront tracer.  No counterpart in the reference.

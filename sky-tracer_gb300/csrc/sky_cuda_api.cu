@@ -20,6 +20,7 @@
 
 #include "../../include/sky_cuda.h"
 #include "adjoint_kernels.h"
+#include "mie_kernels.h"
 #include "scene_build.h"
 #include "score_kernels.h"
 #include "trace_kernels.h"
@@ -1077,6 +1078,104 @@ extern "C" int sky_cuda_score_combos(const float* bands, uint32_t band_count, ui
             SkyComboScore& r = results[c0 + c];
             if (r.finite) r.score = r.rmse + 0.25 * r.p95;
         }
+    }
+    return SKY_OK;
+}
+
+// ---- Mie phase-table bake -----------------------------------------------------------
+
+extern "C" int sky_cuda_bake_mie_phase(const SkyMieDistribution* dist, const double* wavelength_um,
+                                       const double* refr_re, const double* refr_im, uint32_t band_count,
+                                       uint32_t phase_bins, double* phase_out, SkyMieBand* band_out) {
+    if (!dist || !wavelength_um || !refr_re || !refr_im || !phase_out)
+        return set_error(SKY_ERR_INVALID_CONFIG, "dist, wavelengths, refractive indices and phase_out are required");
+    if (band_count == 0 || phase_bins == 0) return set_error(SKY_ERR_INVALID_CONFIG, "band_count and phase_bins must be positive");
+    const SkyMieDistribution& D = *dist;
+    if (!(D.r_min_um > 0.0) || !(D.r_max_um >= D.r_min_um) || !(D.r_mode_um > 0.0) || !(D.sigma_g > 1.0) ||
+        D.r_count == 0 || !std::isfinite(D.r_max_um) || !std::isfinite(D.sigma_g))
+        return set_error(SKY_ERR_INVALID_CONFIG, "size distribution needs 0 < r_min <= r_max, r_mode > 0, "
+                                                 "sigma_g > 1 and r_count >= 1");
+    // radii (numpy.geomspace) and lognormal weights (bake_opac_data.py:103-109)
+    std::vector<double> r(D.r_count), w(D.r_count);
+    const double l0 = std::log(D.r_min_um), l1 = std::log(D.r_max_um), ls = std::log(D.sigma_g);
+    double wsum = 0.0;
+    for (uint32_t i = 0; i < D.r_count; ++i) {
+        r[i] = D.r_count == 1 ? D.r_min_um
+               : i == 0       ? D.r_min_um
+               : i + 1 == D.r_count ? D.r_max_um
+                                    : std::exp(l0 + (l1 - l0) * double(i) / double(D.r_count - 1));
+        const double z = std::log(r[i] / D.r_mode_um);
+        w[i] = std::exp(-z * z / (2.0 * ls * ls));
+        wsum += w[i];
+    }
+    if (!(wsum > 0.0)) return set_error(SKY_ERR_INVALID_CONFIG, "the size distribution has no weight on its radii");
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    std::vector<MieItem> items(size_t(band_count) * D.r_count);
+    uint64_t aoff = 0, doff = 0;
+    uint32_t max_terms = 0;
+    for (uint32_t b = 0; b < band_count; ++b) {
+        const double lam = wavelength_um[b], mre = refr_re[b], mim = refr_im[b];
+        if (!(lam > 0.0) || !std::isfinite(lam) || !(mre > 0.0) || !std::isfinite(mre) || !(mim >= 0.0) ||
+            !std::isfinite(mim))
+            return set_error(SKY_ERR_INVALID_CONFIG, "band " + std::to_string(b) +
+                                                         ": wavelength and refractive index must be finite, "
+                                                         "wavelength > 0, n > 0, k >= 0");
+        for (uint32_t i = 0; i < D.r_count; ++i) {
+            MieItem& it = items[size_t(b) * D.r_count + i];
+            it.k = two_pi / lam;
+            it.x = it.k * r[i];
+            it.m_re = mre;
+            it.m_im = mim;
+            it.weight = w[i] / wsum;
+            it.band = b;
+            if (!(it.x <= 12000.0))
+                return set_error(SKY_ERR_INVALID_CONFIG, "size parameter 2 pi r / lambda above 12000");
+            it.terms = mie_terms(it.x);
+            const double mx = it.x * std::sqrt(mre * mre + mim * mim);
+            it.dterms = uint32_t(std::max(double(it.terms), mx)) + 16u;
+            it.aoff = aoff;
+            it.doff = doff;
+            it._pad = 0;
+            aoff += it.terms;
+            doff += uint64_t(it.dterms) + 1u;
+            max_terms = std::max(max_terms, it.terms);
+        }
+    }
+    if (doff * sizeof(double2) + aoff * sizeof(float4) > (uint64_t(16) << 30))
+        return set_error(SKY_ERR_INVALID_CONFIG, "bake too large: more than 16 GB of series scratch");
+    DeviceScratch mem;
+    MieItem* d_items = nullptr;
+    double2* d_scr = nullptr;
+    float4* d_ab = nullptr;
+    double *d_q = nullptr, *d_acc = nullptr;
+    cudaError_t e;
+    if ((e = mem.alloc(&d_items, items.size())) || (e = mem.alloc(&d_scr, doff)) || (e = mem.alloc(&d_ab, aoff)) ||
+        (e = mem.alloc(&d_q, items.size() * 3)) || (e = mem.alloc(&d_acc, size_t(band_count) * phase_bins)))
+        return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "Mie bake scratch allocation", e);
+    clear_stale_error();
+    if ((e = cudaMemcpy(d_items, items.data(), items.size() * sizeof(MieItem), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemset(d_acc, 0, size_t(band_count) * phase_bins * sizeof(double))))
+        return cuda_fail(SKY_ERR_COPY, "Mie bake upload", e);
+    if ((e = launch_mie_bake(d_items, uint32_t(items.size()), max_terms, d_scr, d_ab, d_q, phase_bins, d_acc,
+                             nullptr)))
+        return cuda_fail(SKY_ERR_LAUNCH, "Mie bake kernels", e);
+    std::vector<double> q(items.size() * 3);
+    if ((e = cudaMemcpy(q.data(), d_q, q.size() * sizeof(double), cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(phase_out, d_acc, size_t(band_count) * phase_bins * sizeof(double), cudaMemcpyDeviceToHost)))
+        return cuda_fail(SKY_ERR_COPY, "Mie bake readback", e);
+    const double pi = 0.5 * two_pi;
+    for (uint32_t b = 0; b < band_count; ++b) {
+        double sca = 0.0, ext = 0.0, g = 0.0;
+        for (uint32_t i = 0; i < D.r_count; ++i) {
+            const MieItem& it = items[size_t(b) * D.r_count + i];
+            const double area = pi * r[i] * r[i] * it.weight;
+            sca += area * q[3 * (size_t(b) * D.r_count + i)];
+            ext += area * q[3 * (size_t(b) * D.r_count + i) + 1];
+            g += area * q[3 * (size_t(b) * D.r_count + i)] * q[3 * (size_t(b) * D.r_count + i) + 2];
+        }
+        double* row = phase_out + size_t(b) * phase_bins;
+        for (uint32_t j = 0; j < phase_bins; ++j) row[j] = sca > 0.0 ? row[j] / sca : 0.0;
+        if (band_out) band_out[b] = SkyMieBand{sca, ext, sca > 0.0 ? g / sca : 0.0};
     }
     return SKY_OK;
 }

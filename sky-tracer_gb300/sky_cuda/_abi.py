@@ -62,6 +62,7 @@ assert AEROSOL_DTYPE.itemsize == 32 and OPTICS_DTYPE.itemsize == 8
 _f = ctypes.c_float
 _u32 = ctypes.c_uint32
 _fp = ctypes.POINTER(ctypes.c_float)
+_dp = ctypes.POINTER(ctypes.c_double)
 _vp = ctypes.c_void_p
 
 
@@ -134,6 +135,15 @@ class SkyComboScore(ctypes.Structure):
         ("finite", ctypes.c_uint64)]
 
 
+class SkyMieDistribution(ctypes.Structure):
+    _fields_ = [("r_mode_um", ctypes.c_double), ("sigma_g", ctypes.c_double), ("r_min_um", ctypes.c_double),
+                ("r_max_um", ctypes.c_double), ("r_count", ctypes.c_uint32), ("_reserved", ctypes.c_uint32)]
+
+
+class SkyMieBand(ctypes.Structure):
+    _fields_ = [("sigma_sca_um2", ctypes.c_double), ("sigma_ext_um2", ctypes.c_double), ("g", ctypes.c_double)]
+
+
 ADJOINT_BAND_PARAMS = 4
 ADJOINT_SEGMENT_INTEGRALS = 0
 ADJOINT_NULL_COLLISIONS = 1
@@ -179,6 +189,8 @@ _SIGNATURES = {
                                              ctypes.POINTER(SkyComboScore), _vp]),
     "sky_cuda_render_batch_noalloc": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                                      ctypes.POINTER(SkyDeviceOutputs), ctypes.c_uint32, _vp]),
+    "sky_cuda_bake_mie_phase": (ctypes.c_int, [ctypes.POINTER(SkyMieDistribution), _dp, _dp, _dp, ctypes.c_uint32,
+                                               ctypes.c_uint32, _dp, ctypes.POINTER(SkyMieBand)]),
 }
 NOALLOC_MAX_JOBS = 16
 

@@ -46,7 +46,8 @@ def test_struct_layouts_match_header(tmp_path):
         "SkyRenderStats": _abi.SkyRenderStats, "SkyDeviceOutputs": _abi.SkyDeviceOutputs,
         "SkyTuning": _abi.SkyTuning, "SkyBatchJob": _abi.SkyBatchJob,
         "SkyAdjointParams": _abi.SkyAdjointParams, "SkyAdjointGrads": _abi.SkyAdjointGrads,
-        "SkyComboScore": _abi.SkyComboScore,
+        "SkyComboScore": _abi.SkyComboScore, "SkyMieDistribution": _abi.SkyMieDistribution,
+        "SkyMieBand": _abi.SkyMieBand,
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for name, dt in structs.items():
