@@ -207,11 +207,12 @@ int place_job(DevJob& job, uint64_t pixels, uint32_t bands, uint64_t& cells_so_f
     return SKY_OK;
 }
 
-WaveLaunch wave_launch(const SkyScene* s, const DevJob* dev_jobs, uint32_t n, uint64_t cells, uint32_t max_cells,
-                       uint32_t tracking, uint32_t phase_sampling, uint32_t* counter, unsigned long long* counters,
-                       uint32_t* status) {
+WaveLaunch wave_launch(const SkyScene* s, const DevJob& first, const DevJob* dev_jobs, uint32_t n, uint64_t cells,
+                       uint32_t max_cells, uint32_t tracking, uint32_t phase_sampling, uint32_t* counter,
+                       unsigned long long* counters, uint32_t* status) {
     WaveLaunch w{};
-    w.scene = s->dev;
+    w.scene = first.S;
+    w.launch0 = first.L;
     w.jobs = dev_jobs;
     w.num_jobs = n;
     w.total_cells = uint32_t(cells);
@@ -267,7 +268,7 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     uint32_t max_cells = 0;
     int st = place_job(job, pixels, s->dev.band_count, cells, max_cells);
     if (st) return st;
-    const WaveLaunch w = wave_launch(s, s->jobs, 1, cells, max_cells, c->tracking, c->phase_sampling,
+    const WaveLaunch w = wave_launch(s, job, s->jobs, 1, cells, max_cells, c->tracking, c->phase_sampling,
                                      s->work_counter, o->counters, o->status);
     if ((e = cudaMemcpyAsync(s->jobs, &job, sizeof(job), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
         return cuda_fail(SKY_ERR_COPY, "job upload", e);
@@ -711,9 +712,9 @@ extern "C" int sky_cuda_render_batch(const SkyScene* scene, const SkyBatchJob* j
     cudaError_t e = cudaMemcpyAsync(s->batch_jobs, s->batch_host, size_t(job_count) * sizeof(DevJob),
                                     cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "batch job table upload", e);
-    const WaveLaunch w = wave_launch(s, s->batch_jobs, job_count, cells, max_cells, jobs[0].config.tracking,
-                                     jobs[0].config.phase_sampling, s->batch_counter, jobs[0].outputs.counters,
-                                     jobs[0].outputs.status);
+    const WaveLaunch w = wave_launch(s, s->batch_host[0], s->batch_jobs, job_count, cells, max_cells,
+                                     jobs[0].config.tracking, jobs[0].config.phase_sampling, s->batch_counter,
+                                     jobs[0].outputs.counters, jobs[0].outputs.status);
     e = launch_trace_wave(w, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "batched wavefront launch", e);
     return SKY_OK;
@@ -739,9 +740,9 @@ extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatch
         (e = cudaMalloc(&g->counter, sizeof(uint32_t))) != cudaSuccess) {
         st = cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch graph allocation", e);
     } else if ((st = build_batch_jobs(s, jobs, job_count, g->host, cells, max_cells)) == SKY_OK) {
-        const WaveLaunch w = wave_launch(s, g->jobs, job_count, cells, max_cells, jobs[0].config.tracking,
-                                         jobs[0].config.phase_sampling, g->counter, jobs[0].outputs.counters,
-                                         jobs[0].outputs.status);
+        const WaveLaunch w = wave_launch(s, g->host[0], g->jobs, job_count, cells, max_cells,
+                                         jobs[0].config.tracking, jobs[0].config.phase_sampling, g->counter,
+                                         jobs[0].outputs.counters, jobs[0].outputs.status);
         clear_stale_error();
         if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
@@ -1264,8 +1265,8 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "job table upload", e);
     uint32_t* counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
                                                     offsetof(NoAllocScratch, work_counter));
-    const WaveLaunch w = wave_launch(s, static_cast<const DevJob*>(scratch), job_count, cells, max_cells,
-                                     job_configs[0].tracking, job_configs[0].phase_sampling, counter,
+    const WaveLaunch w = wave_launch(s, image.jobs[0], static_cast<const DevJob*>(scratch), job_count, cells,
+                                     max_cells, job_configs[0].tracking, job_configs[0].phase_sampling, counter,
                                      outputs[0].counters, outputs[0].status);
     e = launch_trace_wave(w, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "wavefront tracing launch", e);

@@ -21,7 +21,9 @@ constexpr uint32_t kWaveThreads = 256;
 constexpr uint32_t kWaveVariants = 3;  // resident blocks per SM: variant 0 -> 3, 1 -> 2, 2 -> 4
 
 struct WaveLaunch {
-    DevScene scene;                // tables and constants of every job (jobs differ in their sun frame only)
+    DevScene scene;                // the first job's scene: its tables and constants are every job's
+                                   // (jobs differ in their sun frame only)
+    DevLaunch launch0;             // the first job's launch constants
     const DevJob* jobs;            // device array, ascending cell_begin
     uint32_t num_jobs;             // at most 65535
     uint32_t total_cells;          // sum of the jobs' cell counts

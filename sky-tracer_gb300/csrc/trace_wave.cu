@@ -62,9 +62,23 @@ __device__ __forceinline__ uint32_t job_of(const DevJob* __restrict__ jobs, uint
     return lo;
 }
 
-template <int kTracking, int kPhase, int kMinBlocks>
+// The launch constants and the sun frame of a lane's job: kernel parameters
+// when the launch holds one job, the job table otherwise.
+template <bool kSingle>
+__device__ __forceinline__ const DevLaunch& job_launch(const DevLaunch& L0, const DevJob* jobs, uint32_t job) {
+    if constexpr (kSingle) return L0;
+    else return jobs[job].L;
+}
+template <bool kSingle>
+__device__ __forceinline__ const DevScene& job_scene(const DevScene& S0, const DevJob* jobs, uint32_t job) {
+    if constexpr (kSingle) return S0;
+    else return jobs[job].S;
+}
+
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
-    wave_kernel(const __grid_constant__ DevScene S, const DevJob* __restrict__ jobs, uint32_t num_jobs,
+    wave_kernel(const __grid_constant__ DevScene S, const __grid_constant__ DevLaunch L0,
+                const DevJob* __restrict__ jobs, uint32_t num_jobs,
                 uint32_t total_cells, uint32_t* __restrict__ work_counter, unsigned long long* __restrict__ counters,
                 uint32_t* __restrict__ status) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -129,7 +143,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         // lights / continuation, outgoing ray), so that each block runs once
         // per iteration for every lane that needs it
         if (next != kIdle && next != kTrace) {
-            const DevJob& J = jobs[job];
+            const DevLaunch& JL = job_launch<kSingle>(L0, jobs, job);
             if (next == kStart) {
                 if (cell != acc_cell || job != acc_job) {
                     if (acc_cell != kNoCell) {
@@ -144,11 +158,11 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 }
                 band = cell % S.band_count;
                 const uint32_t pixel = cell / S.band_count;
-                const uint32_t width = __ldg(&J.L.width);
+                const uint32_t width = JL.width;
                 const uint32_t x = pixel % width, y = pixel / width;
-                rng.init(pixel, __ldg(&J.L.sample_offset) + sample, band, __ldg(&J.L.seed_lo), __ldg(&J.L.seed_hi));
-                dir = camera_dir(J.L, x, y, rng);
-                org = mk(0.0f, S.ground_radius + fmaxf(__ldg(&J.L.observer_altitude), 0.0f), 0.0f);
+                rng.init(pixel, JL.sample_offset + sample, band, JL.seed_lo, JL.seed_hi);
+                dir = camera_dir(JL, x, y, rng);
+                org = mk(0.0f, S.ground_radius + fmaxf(JL.observer_altitude, 0.0f), 0.0f);
                 ++n.e[SKY_EVENT_CHAIN];
                 thr = 1.0f;
                 rad = 0.0f;
@@ -158,11 +172,11 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
             if (next == kLights) {
                 // direct_sun_at_scatter (sky_trace.wgsl:566-585) and ground_radiance
                 // (:587-608), one shadow ray at a time
-                const uint32_t lights = __ldg(&J.L.direct_light_samples);
+                const uint32_t lights = JL.direct_light_samples;
                 const float l_sun = __ldg(&S.bands[band].solar_radiance);
                 while (ls < lights) {
                     ++ls;
-                    const V3 ldir = sample_sun_cone(J.S, rng);
+                    const V3 ldir = sample_sun_cone(job_scene<kSingle>(S, jobs, job), rng);
                     ++n.e[SKY_EVENT_NEE];
                     float cos_sun = 0.0f;
                     if (ground) {
@@ -205,7 +219,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                         if (pdf <= 0.0f || cos_out <= 0.0f) alive = false;
                         else thr *= S.ground_albedo * kInvPi * cos_out / pdf;
                     }
-                    if (alive && depth >= __ldg(&J.L.rr_start_depth)) {  // russian_roulette (:691-701)
+                    if (alive && depth >= JL.rr_start_depth) {  // russian_roulette (:691-701)
                         const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
                         if (rng.next() > q) alive = false;
                         else thr = thr / q;
@@ -227,8 +241,8 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 }
             }
             if (next == kPrimary) {  // the outgoing ray (sky_trace.wgsl:709-717)
-                const uint32_t max_orders = __ldg(&J.L.max_orders);
-                if (depth >= __ldg(&J.L.watchdog_limit)) {
+                const uint32_t max_orders = JL.max_orders;
+                if (depth >= JL.watchdog_limit) {
                     watchdog = true;
                     next = kEnd;
                 } else {
@@ -273,9 +287,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     next = kLights;
                 }
             } else if (boundary == 1u) {
-                const DevJob& J = jobs[job];
-                if (depth == 0u && dot3(dir, mk(__ldg(&J.S.sun[0]), __ldg(&J.S.sun[1]), __ldg(&J.S.sun[2]))) >=
-                                       S.cos_max)
+                if (depth == 0u && dot3(dir, load3(job_scene<kSingle>(S, jobs, job).sun)) >= S.cos_max)
                     rad += thr * __ldg(&S.bands[band].solar_radiance);
                 rad = fmaxf(rad, 0.0f);
                 next = kEnd;
@@ -323,9 +335,9 @@ __global__ void __launch_bounds__(256) wave_prepare_kernel(const DevJob* __restr
     }
 }
 
-template <int kTracking, int kPhase, int kMinBlocks>
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle>
 cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
-    const void* k = reinterpret_cast<const void*>(wave_kernel<kTracking, kPhase, kMinBlocks>);
+    const void* k = reinterpret_cast<const void*>(wave_kernel<kTracking, kPhase, kMinBlocks, kSingle>);
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -336,19 +348,25 @@ cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
     // a warp per cell at most
     const uint64_t want = (uint64_t(w.total_cells) * 32u + kWaveThreads - 1u) / kWaveThreads;
     const uint32_t blocks = uint32_t(std::max<uint64_t>(1u, std::min<uint64_t>(uint64_t(per_sm) * sms, want)));
-    wave_kernel<kTracking, kPhase, kMinBlocks><<<blocks, kWaveThreads, 0, stream>>>(
-        w.scene, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status);
+    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle><<<blocks, kWaveThreads, 0, stream>>>(
+        w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status);
     return cudaGetLastError();
+}
+
+template <int kTracking, int kPhase, bool kSingle>
+cudaError_t launch_wave_single(const WaveLaunch& w, cudaStream_t stream) {
+    switch (w.variant) {
+        case 0: return launch_wave_shape<kTracking, kPhase, 3, kSingle>(w, stream);
+        case 1: return launch_wave_shape<kTracking, kPhase, 2, kSingle>(w, stream);
+        case 2: return launch_wave_shape<kTracking, kPhase, 4, kSingle>(w, stream);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 template <int kTracking, int kPhase>
 cudaError_t launch_wave_mode(const WaveLaunch& w, cudaStream_t stream) {
-    switch (w.variant) {
-        case 0: return launch_wave_shape<kTracking, kPhase, 3>(w, stream);
-        case 1: return launch_wave_shape<kTracking, kPhase, 2>(w, stream);
-        case 2: return launch_wave_shape<kTracking, kPhase, 4>(w, stream);
-        default: return cudaErrorInvalidValue;
-    }
+    return w.num_jobs == 1u ? launch_wave_single<kTracking, kPhase, true>(w, stream)
+                            : launch_wave_single<kTracking, kPhase, false>(w, stream);
 }
 
 }  // namespace
