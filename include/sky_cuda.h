@@ -203,7 +203,7 @@ typedef struct SkyRenderStats {
     double kernel_ms;       /* device time of the tracing kernel(s), CUDA events */
     double total_ms;        /* host wall time of the call                         */
     uint64_t chains;        /* pixel x band x sample paths traced                 */
-    uint64_t events[SKY_EVENT_COUNT];
+    uint64_t events[SKY_EVENT_COUNT];  /* counted only when stats are requested */
     uint32_t watchdog;      /* nonzero when a path reached the watchdog           */
     uint32_t kernel_used;   /* SkyKernel actually launched                         */
 } SkyRenderStats;

@@ -41,6 +41,10 @@ struct WaveLaunch {
 // XYZ variance and linear sRGB.
 cudaError_t launch_trace_wave(const WaveLaunch& w, cudaStream_t stream);
 uint32_t wave_blocks_per_sm(uint32_t variant);
+// The tracing kernel alone, per tracking mode (trace_wave_*.cu).
+cudaError_t launch_wave_segment_restart(const WaveLaunch& w, cudaStream_t stream);
+cudaError_t launch_wave_residual_carry(const WaveLaunch& w, cudaStream_t stream);
+cudaError_t launch_wave_merged_layers(const WaveLaunch& w, cudaStream_t stream);
 
 // Mean film, XYZ, XYZ variance and linear sRGB from the per-cell sums (any
 // output may be null; xyz_var needs cell_sumsq).

@@ -1,0 +1,377 @@
+// trace_wave.cuh — the wavefront tracing kernel (a ray loop with per-lane
+// chain regeneration over a job table) and its launch shapes, included by one
+// translation unit per tracking mode (trace_wave_*.cu) so that its
+// instantiations compile in parallel.  trace_wave.cu holds the launch
+// sequence (prepare, trace, finalize).
+//
+// The plain kernel runs every chain to completion inside one lane, so a warp
+// executes the union of 32 different paths.  Here a chain is a sequence of
+// rays: the camera / continuation ray of each vertex and the sun shadow ray
+// of each NEE sample.  Every iteration of the kernel's loop traces exactly
+// one ray per lane through the one inlined tracker (sample_real_collision /
+// delta_transmittance, sky_trace.wgsl:405-475); the event code (scattering,
+// NEE, ground, Russian roulette, sky_trace.wgsl:566-776) then runs up to the
+// lane's next ray.  A lane whose chain ends takes the next sample of its
+// warp's current (pixel, band) cell, and the warp takes a new cell from a
+// global counter when the cell's samples run out.  So the 32 lanes enter the
+// tracker together on every iteration whatever vertex or chain each is at,
+// no lane waits for the slowest chain of a cell, and nothing waits at a block
+// barrier.
+//
+// Each chain consumes its random stream in the plain kernel's order
+// (trace_path, sky_trace.wgsl:703-776), so both kernels trace the same paths.
+// A lane keeps the FP64 sums of its current cell in registers and adds them
+// to the job's cell sums when it moves to another cell; the cells' sums
+// therefore add in no fixed order (they agree with the plain kernel's to FP64
+// rounding).
+//
+// A launch is three kernels: prepare (zero the sums of jobs that do not
+// accumulate, reset the work counter), trace, and finalize (mean film, XYZ
+// and its variance, linear sRGB of every pixel of every job).
+
+#pragma once
+
+#include <algorithm>
+
+#include "sky_device.cuh"
+#include "trace_kernels.h"
+
+namespace sky {
+namespace wave {
+
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr uint32_t kNoCell = 0xffffffffu;
+// Backstop on the loop iterations of one warp (one ray per lane each); a
+// render needs ~3 rays per chain / lanes in flight.  Beyond it the warp sets
+// status bit 2 and returns.
+constexpr uint64_t kMaxIterations = 1ull << 31;
+
+// What a lane does next.
+enum : uint32_t {
+    kTrace = 0u,    // a ray is set up: trace it in the next tracking step
+    kStart = 1u,    // a new chain: camera ray
+    kPrimary = 2u,  // depth checks and the boundary of the vertex's outgoing ray
+    kLights = 3u,   // the vertex's next NEE sample, else its continuation
+    kEnd = 4u,      // the chain's radiance is final
+    kIdle = 5u      // no chain
+};
+
+// Job of global cell `g`: the last job whose first cell is <= g.
+__device__ __forceinline__ uint32_t job_of(const DevJob* __restrict__ jobs, uint32_t num_jobs, uint32_t g) {
+    uint32_t lo = 0u, hi = num_jobs;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&jobs[mid].cell_begin) <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The launch constants and the sun frame of a lane's job: kernel parameters
+// when the launch holds one job, the job table otherwise.
+template <bool kSingle>
+__device__ __forceinline__ const DevLaunch& job_launch(const DevLaunch& L0, const DevJob* jobs, uint32_t job) {
+    if constexpr (kSingle) return L0;
+    else return jobs[job].L;
+}
+template <bool kSingle>
+__device__ __forceinline__ const DevScene& job_scene(const DevScene& S0, const DevJob* jobs, uint32_t job) {
+    if constexpr (kSingle) return S0;
+    else return jobs[job].S;
+}
+
+// kCount: count events (SkyDeviceOutputs.counters given).  Without it the
+// counters are never read, so their increments compile away (the registers
+// they would hold are worth ~5 % at 64 registers per lane).
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount>
+__global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
+    wave_kernel(const __grid_constant__ DevScene S, const __grid_constant__ DevLaunch L0,
+                const DevJob* __restrict__ jobs, uint32_t num_jobs,
+                uint32_t total_cells, uint32_t* __restrict__ work_counter, unsigned long long* __restrict__ counters,
+                uint32_t* __restrict__ status) {
+    const uint32_t lane = threadIdx.x & 31u;
+    Counters n;
+    n.clear();
+    bool watchdog = false;
+    // the warp's current cell and its next unclaimed sample (warp-uniform)
+    uint32_t claim_job = 0u, claim_cell = 0u, claim_spp = 0u, claim_next = 0u;
+    bool exhausted = false;
+    // the lane's chain
+    uint32_t next = kIdle, job = 0u, cell = 0u, sample = 0u, band = 0u, depth = 0u, ls = 0u, boundary = 0u;
+    bool shadow_ray = false, ground = false;
+    Rng rng;
+    rng.k0 = rng.k1 = rng.k2 = rng.dim = 0u;
+    V3 org = mk(0.0f, 0.0f, 0.0f), dir = org;  // org is the vertex position between rays
+    float thr = 0.0f, rad = 0.0f, nee = 0.0f, alt = 0.0f, term = 0.0f, t_max = 0.0f;
+    RayGeo g{0.0f, 0.0f, 0.0f};
+    // FP64 sums of the lane's current cell
+    uint32_t acc_job = 0u, acc_cell = kNoCell;
+    double acc_sum = 0.0, acc_sq = 0.0;
+
+    for (uint64_t iter = 0;; ++iter) {
+        if (iter >= kMaxIterations) {  // warp-uniform
+            if (lane == 0u) atomicOr(status, 2u);
+            break;
+        }
+        // a chain that ended after its last ray: its radiance joins the cell's sums
+        if (next == kEnd) {
+            const double rd = double(rad);
+            acc_sum += rd;
+            acc_sq += rd * rd;
+            next = kIdle;
+        }
+        // idle lanes take the next samples of the warp's cell
+#pragma unroll 1
+        for (;;) {
+            const uint32_t need = __ballot_sync(kFull, next == kIdle);
+            if (need == 0u || exhausted) break;
+            if (claim_next >= claim_spp) {
+                uint32_t gc = 0u;
+                if (lane == 0u) gc = atomicAdd(work_counter, 1u);
+                gc = __shfl_sync(kFull, gc, 0);
+                if (gc >= total_cells) {
+                    exhausted = true;
+                    break;
+                }
+                claim_job = job_of(jobs, num_jobs, gc);
+                claim_cell = gc - __ldg(&jobs[claim_job].cell_begin);
+                claim_spp = __ldg(&jobs[claim_job].L.spp);
+                claim_next = 0u;
+            }
+            const uint32_t rank = __popc(need & ((1u << lane) - 1u));
+            if (next == kIdle && claim_next + rank < claim_spp) {
+                job = claim_job;
+                cell = claim_cell;
+                sample = claim_next + rank;
+                next = kStart;
+            }
+            claim_next = min(claim_spp, claim_next + uint32_t(__popc(need)));
+        }
+        // event code up to the lane's next ray, one pass in flow order (start,
+        // lights / continuation, outgoing ray), so that each block runs once
+        // per iteration for every lane that needs it
+        if (next != kIdle && next != kTrace) {
+            const DevLaunch& JL = job_launch<kSingle>(L0, jobs, job);
+            if (next == kStart) {
+                if (cell != acc_cell || job != acc_job) {
+                    if (acc_cell != kNoCell) {
+                        const DevJob& A = jobs[acc_job];
+                        atomicAdd(A.cell_sum + acc_cell, acc_sum);
+                        double* sq = A.cell_sumsq;
+                        if (sq) atomicAdd(sq + acc_cell, acc_sq);
+                    }
+                    acc_job = job;
+                    acc_cell = cell;
+                    acc_sum = acc_sq = 0.0;
+                }
+                band = cell % S.band_count;
+                const uint32_t pixel = cell / S.band_count;
+                const uint32_t width = JL.width;
+                const uint32_t x = pixel % width, y = pixel / width;
+                rng.init(pixel, JL.sample_offset + sample, band, JL.seed_lo, JL.seed_hi);
+                dir = camera_dir(JL, x, y, rng);
+                org = mk(0.0f, S.ground_radius + fmaxf(JL.observer_altitude, 0.0f), 0.0f);
+                ++n.e[SKY_EVENT_CHAIN];
+                thr = 1.0f;
+                rad = 0.0f;
+                depth = 0u;
+                next = kPrimary;
+            }
+            if (next == kLights) {
+                // direct_sun_at_scatter (sky_trace.wgsl:566-585) and ground_radiance
+                // (:587-608), one shadow ray at a time
+                const uint32_t lights = JL.direct_light_samples;
+                const float l_sun = __ldg(&S.bands[band].solar_radiance);
+                while (ls < lights) {
+                    ++ls;
+                    const V3 ldir = sample_sun_cone(job_scene<kSingle>(S, jobs, job), rng);
+                    ++n.e[SKY_EVENT_NEE];
+                    float cos_sun = 0.0f;
+                    if (ground) {
+                        cos_sun = fmaxf(dot3(normalize_or_y(org), ldir), 0.0f);
+                        if (!(cos_sun > 0.0f)) continue;
+                    }
+                    g = ray_geo(madd(org, ldir, kRayEpsilonKm), ldir);
+                    uint32_t kind;
+                    ++n.e[SKY_EVENT_BOUNDARY];
+                    if (!(next_boundary(S, g, t_max, kind) && kind == 1u)) continue;
+                    // the sample's term if the shadow ray reaches the sun (transmittance 1)
+                    if (ground) {
+                        term = S.ground_albedo * kInvPi * l_sun * 1.0f * cos_sun / S.light_pdf;
+                    } else {
+                        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+                        term = l_sun * 1.0f * mixed_phase(S, c, band, dot3(dir, ldir)) / S.light_pdf;
+                    }
+                    shadow_ray = true;
+                    next = kTrace;
+                    break;
+                }
+                if (next == kLights) {
+                    // the continuation (sky_trace.wgsl:728-767)
+                    rad += thr * (nee * (1.0f / float(lights)));
+                    V3 nd;
+                    bool alive = true;
+                    if (!ground) {
+                        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+                        if (kPhase == SKY_PHASE_TABULATED) {
+                            thr *= sample_tabulated(S, c, band, dir, rng, nd);
+                        } else {
+                            nd = sample_isotropic(rng);
+                            thr *= mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                        }
+                    } else {
+                        const V3 normal = normalize_or_y(org);
+                        float pdf;
+                        nd = sample_cosine_hemisphere(normal, rng, pdf);
+                        const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+                        if (pdf <= 0.0f || cos_out <= 0.0f) alive = false;
+                        else thr *= S.ground_albedo * kInvPi * cos_out / pdf;
+                    }
+                    if (alive && depth >= JL.rr_start_depth) {  // russian_roulette (:691-701)
+                        const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
+                        if (rng.next() > q) alive = false;
+                        else thr = thr / q;
+                    }
+                    if (!alive) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kEnd;
+                    } else {
+                        org = madd(org, nd, kRayEpsilonKm);
+                        dir = nd;
+                        if (rad < 0.0f || rad != rad || thr < 0.0f || thr != thr) {
+                            rad = 0.0f;
+                            next = kEnd;
+                        } else {
+                            ++depth;
+                            next = kPrimary;
+                        }
+                    }
+                }
+            }
+            if (next == kPrimary) {  // the outgoing ray (sky_trace.wgsl:709-717)
+                const uint32_t max_orders = JL.max_orders;
+                if (depth >= JL.watchdog_limit) {
+                    watchdog = true;
+                    next = kEnd;
+                } else {
+                    g = ray_geo(org, dir);
+                    ++n.e[SKY_EVENT_BOUNDARY];
+                    if ((max_orders != 0u && depth >= max_orders) || !next_boundary(S, g, t_max, boundary)) {
+                        rad = fmaxf(rad, 0.0f);
+                        next = kEnd;
+                    } else {
+                        shadow_ray = false;
+                        next = kTrace;
+                    }
+                }
+            }
+        }
+        const bool tracing = next == kTrace;
+        if (!__any_sync(kFull, tracing)) {
+            // every lane idle (or ending a chain, summed next iteration) and no cell left
+            if (exhausted && !__any_sync(kFull, next == kEnd)) break;
+            continue;
+        }
+        if (tracing) {
+            float t_hit = 0.0f;
+            const bool hit = track_ray<kTracking>(S, g, t_max, band, rng, t_hit, n, watchdog);
+            if (shadow_ray) {
+                if (!hit) nee += term;
+                next = kLights;
+            } else if (hit) {
+                ++n.e[SKY_EVENT_SCATTER];
+                org = madd(org, dir, t_hit);
+                alt = altitude_at(g, t_hit, S.ground_radius);
+                const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+                const bool medium = c.extinction > 0.0f && c.scattering > 0.0f;
+                if (medium) thr *= fminf(fmaxf(c.scattering / c.extinction, 0.0f), 1.0f);
+                if (!medium || thr <= 0.0f) {
+                    rad = fmaxf(rad, 0.0f);
+                    next = kEnd;
+                } else {
+                    ground = false;
+                    ls = 0u;
+                    nee = 0.0f;
+                    next = kLights;
+                }
+            } else if (boundary == 1u) {
+                if (depth == 0u && dot3(dir, load3(job_scene<kSingle>(S, jobs, job).sun)) >= S.cos_max)
+                    rad += thr * __ldg(&S.bands[band].solar_radiance);
+                rad = fmaxf(rad, 0.0f);
+                next = kEnd;
+            } else {
+                ++n.e[SKY_EVENT_GROUND];
+                org = madd(org, dir, t_max);
+                ground = true;
+                ls = 0u;
+                nee = 0.0f;
+                next = kLights;
+            }
+        }
+    }
+    if (acc_cell != kNoCell) {
+        const DevJob& A = jobs[acc_job];
+        atomicAdd(A.cell_sum + acc_cell, acc_sum);
+        double* sq = A.cell_sumsq;
+        if (sq) atomicAdd(sq + acc_cell, acc_sq);
+    }
+    if (kCount) {
+#pragma unroll
+        for (int e = 0; e < SKY_EVENT_COUNT; ++e) {
+            uint32_t v = n.e[e];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+            if (lane == 0u && v) atomicAdd(counters + e, (unsigned long long)v);
+        }
+    }
+    if (__any_sync(kFull, watchdog) && lane == 0u) atomicOr(status, 1u);
+}
+
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount>
+cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
+    const void* k = reinterpret_cast<const void*>(wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount>);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWaveThreads, 0)) != cudaSuccess) return e;
+    per_sm = std::max(per_sm, 1);
+    if (w.max_blocks_per_sm) per_sm = std::min(per_sm, int(w.max_blocks_per_sm));
+    // a warp per cell at most
+    const uint64_t want = (uint64_t(w.total_cells) * 32u + kWaveThreads - 1u) / kWaveThreads;
+    const uint32_t blocks = uint32_t(std::max<uint64_t>(1u, std::min<uint64_t>(uint64_t(per_sm) * sms, want)));
+    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount><<<blocks, kWaveThreads, 0, stream>>>(
+        w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status);
+    return cudaGetLastError();
+}
+
+template <int kTracking, int kPhase, bool kSingle, bool kCount>
+cudaError_t launch_wave_variant(const WaveLaunch& w, cudaStream_t stream) {
+    switch (w.variant) {
+        case 0: return launch_wave_shape<kTracking, kPhase, 3, kSingle, kCount>(w, stream);
+        case 1: return launch_wave_shape<kTracking, kPhase, 2, kSingle, kCount>(w, stream);
+        case 2: return launch_wave_shape<kTracking, kPhase, 4, kSingle, kCount>(w, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int kTracking, int kPhase>
+cudaError_t launch_wave_mode(const WaveLaunch& w, cudaStream_t stream) {
+    if (w.num_jobs == 1u)
+        return w.counters ? launch_wave_variant<kTracking, kPhase, true, true>(w, stream)
+                          : launch_wave_variant<kTracking, kPhase, true, false>(w, stream);
+    return w.counters ? launch_wave_variant<kTracking, kPhase, false, true>(w, stream)
+                      : launch_wave_variant<kTracking, kPhase, false, false>(w, stream);
+}
+
+// The kernels of one tracking mode, both phase samplings.
+template <int kTracking>
+cudaError_t launch_wave_tracking(const WaveLaunch& w, cudaStream_t stream) {
+    if (w.phase_sampling == SKY_PHASE_TABULATED) return launch_wave_mode<kTracking, SKY_PHASE_TABULATED>(w, stream);
+    if (w.phase_sampling == SKY_PHASE_ISOTROPIC) return launch_wave_mode<kTracking, SKY_PHASE_ISOTROPIC>(w, stream);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace wave
+}  // namespace sky

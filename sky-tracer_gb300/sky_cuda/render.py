@@ -250,7 +250,6 @@ def render(scene: Scene, config: RenderConfig) -> Film:
     lib = load_library()
     desc = scene.desc()
     film = np.empty(config.pixels * scene.band_count, dtype=np.float32)
-    stats = SkyRenderStats()
     check(lib.sky_cuda_render_desc(ctypes.byref(desc), ctypes.byref(config.to_c()), _fptr(film), film.size,
-                                   ctypes.byref(stats)), lib)
+                                   None), lib)
     return Film(config.width, config.height, scene.band_count, film)
