@@ -556,7 +556,9 @@ enum : uint32_t { kRayPrimary = 0u, kRayShadow = 1u, kRayRetrace = 2u };
 enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLights = 3u, kNextEnd = 4u,
                   kNextIdle = 5u };
 
-template <int kPhase, bool kGrad>
+// kCount: count events (counters given); without it the counters are never
+// read and their increments compile away.
+template <int kPhase, bool kGrad, bool kCount>
 __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
@@ -879,7 +881,7 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
             }
         }
     }
-    flush_counters(n, counters, lane);
+    if (kCount) flush_counters(n, counters, lane);
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
     if (!kGrad) {
         if (acc_cell != 0xffffffffu) {
@@ -1072,6 +1074,18 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
     return cudaGetLastError();
 }
 
+// One launch of the ray-loop kernel, persistent grid.
+template <int kPhase, bool kGrad, bool kCount>
+cudaError_t launch_ray_loop(const AdjCtx& A, const DevLaunch& L, const float* dloss, double* layer_grad,
+                            double* band_grad, unsigned long long* counters, uint32_t* status, uint32_t cells,
+                            uint32_t copies, uint32_t* next_cell, double* cell_sum, double* cell_sumsq, size_t smem,
+                            uint64_t want, cudaStream_t stream) {
+    const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<kPhase, kGrad, kCount>);
+    adjoint_grad_kernel<kPhase, kGrad, kCount><<<grid_blocks(k, 256, smem, want), 256, smem, stream>>>(
+        A, L, dloss, layer_grad, band_grad, counters, status, cells, copies, next_cell, cell_sum, cell_sumsq);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
                                   uint32_t* next_cell, cudaStream_t stream) {
@@ -1087,16 +1101,21 @@ cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* c
         if ((e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
         const uint64_t want = (cells * 32u + 255u) / 256u;
         const uint32_t n = static_cast<uint32_t>(cells);
-        if (L.phase_sampling == SKY_PHASE_TABULATED) {
-            const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED, false>);
-            adjoint_grad_kernel<SKY_PHASE_TABULATED, false><<<grid_blocks(k, 256, 0, want), 256, 0, stream>>>(
-                A, L, nullptr, nullptr, nullptr, counters, status, n, 0u, next_cell, cell_sum, cell_sumsq);
-        } else {
-            const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, false>);
-            adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, false><<<grid_blocks(k, 256, 0, want), 256, 0, stream>>>(
-                A, L, nullptr, nullptr, nullptr, counters, status, n, 0u, next_cell, cell_sum, cell_sumsq);
-        }
-        return cudaGetLastError();
+        if (L.phase_sampling == SKY_PHASE_TABULATED)
+            e = counters ? launch_ray_loop<SKY_PHASE_TABULATED, false, true>(A, L, nullptr, nullptr, nullptr, counters,
+                                                                               status, n, 0u, next_cell, cell_sum,
+                                                                               cell_sumsq, 0, want, stream)
+                         : launch_ray_loop<SKY_PHASE_TABULATED, false, false>(A, L, nullptr, nullptr, nullptr, counters,
+                                                                                status, n, 0u, next_cell, cell_sum,
+                                                                                cell_sumsq, 0, want, stream);
+        else
+            e = counters ? launch_ray_loop<SKY_PHASE_ISOTROPIC, false, true>(A, L, nullptr, nullptr, nullptr, counters,
+                                                                               status, n, 0u, next_cell, cell_sum,
+                                                                               cell_sumsq, 0, want, stream)
+                         : launch_ray_loop<SKY_PHASE_ISOTROPIC, false, false>(A, L, nullptr, nullptr, nullptr, counters,
+                                                                                status, n, 0u, next_cell, cell_sum,
+                                                                                cell_sumsq, 0, want, stream);
+        return e;
     }
     // sampling under Q, evaluation under P: a warp per cell
     const uint64_t blocks = (cells * 32u + 255u) / 256u;
@@ -1125,18 +1144,19 @@ cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float
     const size_t smem = (copies * nlayer + nband) * sizeof(float);
     const uint64_t want = (cells * 32u + 255u) / 256u;
     const uint32_t n = static_cast<uint32_t>(cells);
-    if (L.phase_sampling == SKY_PHASE_TABULATED) {
-        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_TABULATED, true>);
-        const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_TABULATED, true><<<blocks, 256, smem, stream>>>(
-            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell, nullptr, nullptr);
-    } else {
-        const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, true>);
-        const uint32_t blocks = grid_blocks(k, 256, smem, want);
-        adjoint_grad_kernel<SKY_PHASE_ISOTROPIC, true><<<blocks, 256, smem, stream>>>(
-            A, L, dloss_dfilm, layer_grad, band_grad, counters, status, n, copies, next_cell, nullptr, nullptr);
-    }
-    return cudaGetLastError();
+    if (L.phase_sampling == SKY_PHASE_TABULATED)
+        return counters ? launch_ray_loop<SKY_PHASE_TABULATED, true, true>(A, L, dloss_dfilm, layer_grad, band_grad,
+                                                                            counters, status, n, copies, next_cell,
+                                                                            nullptr, nullptr, smem, want, stream)
+                        : launch_ray_loop<SKY_PHASE_TABULATED, true, false>(A, L, dloss_dfilm, layer_grad, band_grad,
+                                                                             counters, status, n, copies, next_cell,
+                                                                             nullptr, nullptr, smem, want, stream);
+    return counters ? launch_ray_loop<SKY_PHASE_ISOTROPIC, true, true>(A, L, dloss_dfilm, layer_grad, band_grad,
+                                                                        counters, status, n, copies, next_cell,
+                                                                        nullptr, nullptr, smem, want, stream)
+                    : launch_ray_loop<SKY_PHASE_ISOTROPIC, true, false>(A, L, dloss_dfilm, layer_grad, band_grad,
+                                                                         counters, status, n, copies, next_cell,
+                                                                         nullptr, nullptr, smem, want, stream);
 }
 
 }  // namespace sky
