@@ -95,10 +95,11 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     n.clear();
     bool watchdog = false;
     // the warp's current cell and its next unclaimed sample (warp-uniform)
-    uint32_t claim_job = 0u, claim_cell = 0u, claim_spp = 0u, claim_next = 0u;
+    uint32_t claim_job = 0u, claim_spp = 0u, claim_next = 0u;
+    uint32_t claim_band = 0u, claim_x = 0u, claim_y = 0u;  // the cell's band and pixel, divided out once per cell
     bool exhausted = false;
     // the lane's chain
-    uint32_t next = kIdle, job = 0u, cell = 0u, sample = 0u, band = 0u, depth = 0u, ls = 0u, boundary = 0u;
+    uint32_t next = kIdle, job = 0u, sample = 0u, band = 0u, px = 0u, py = 0u, depth = 0u, ls = 0u, boundary = 0u;
     bool shadow_ray = false, ground = false;
     Rng rng;
     rng.k0 = rng.k1 = rng.k2 = rng.dim = 0u;
@@ -135,14 +136,20 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     break;
                 }
                 claim_job = job_of(jobs, num_jobs, gc);
-                claim_cell = gc - __ldg(&jobs[claim_job].cell_begin);
+                const uint32_t c = gc - __ldg(&jobs[claim_job].cell_begin);
+                const uint32_t pixel = c / S.band_count, width = __ldg(&jobs[claim_job].L.width);
+                claim_band = c - pixel * S.band_count;
+                claim_y = pixel / width;
+                claim_x = pixel - claim_y * width;
                 claim_spp = __ldg(&jobs[claim_job].L.spp);
                 claim_next = 0u;
             }
             const uint32_t rank = __popc(need & ((1u << lane) - 1u));
             if (next == kIdle && claim_next + rank < claim_spp) {
                 job = claim_job;
-                cell = claim_cell;
+                band = claim_band;
+                px = claim_x;
+                py = claim_y;
                 sample = claim_next + rank;
                 next = kStart;
             }
@@ -154,6 +161,8 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         if (next != kIdle && next != kTrace) {
             const DevLaunch& JL = job_launch<kSingle>(L0, jobs, job);
             if (next == kStart) {
+                const uint32_t pixel = py * JL.width + px;
+                const uint32_t cell = pixel * S.band_count + band;
                 if (cell != acc_cell || job != acc_job) {
                     if (acc_cell != kNoCell) {
                         const DevJob& A = jobs[acc_job];
@@ -165,12 +174,8 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     acc_cell = cell;
                     acc_sum = acc_sq = 0.0;
                 }
-                band = cell % S.band_count;
-                const uint32_t pixel = cell / S.band_count;
-                const uint32_t width = JL.width;
-                const uint32_t x = pixel % width, y = pixel / width;
                 rng.init(pixel, JL.sample_offset + sample, band, JL.seed_lo, JL.seed_hi);
-                dir = camera_dir(JL, x, y, rng);
+                dir = camera_dir(JL, px, py, rng);
                 org = mk(0.0f, S.ground_radius + fmaxf(JL.observer_altitude, 0.0f), 0.0f);
                 ++n.e[SKY_EVENT_CHAIN];
                 thr = 1.0f;

@@ -258,3 +258,32 @@ def test_autotuner_picks_a_measured_shape(gpu, dome_scene):
         assert gs.get_tuning() == best
         film, _ = gs.render(cfg)
         assert np.all(np.isfinite(film.values))
+
+
+@pytest.mark.parametrize("tracking", [_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_MERGED_LAYERS])
+def test_event_counting_does_not_change_the_render(gpu, dome_scene, tracking):
+    """The wavefront kernel is instantiated with and without event counting
+    (counting only when SkyDeviceOutputs.counters is given): both trace the
+    same chains, so the cell sums agree to FP64 rounding, and the counted run
+    reports one chain event per chain."""
+    import torch
+    cfg = RenderConfig(width=32, height=16, spp=64, phase_sampling=_abi.PHASE_TABULATED, tracking=tracking)
+    with GpuScene(dome_scene) as gs:
+        cells = cfg.pixels * gs.band_count
+        runs = []
+        for count in (False, True):
+            s = torch.zeros(cells, dtype=torch.float64, device="cuda")
+            q = torch.zeros(cells, dtype=torch.float64, device="cuda")
+            st = torch.zeros(1, dtype=torch.int32, device="cuda")
+            ctr = torch.zeros(8, dtype=torch.int64, device="cuda")
+            outs = {"cell_sum": s.data_ptr(), "cell_sumsq": q.data_ptr(), "status": st.data_ptr()}
+            if count:
+                outs["counters"] = ctr.data_ptr()
+            gs.render_device(cfg, outs, torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            assert int(st.item()) == 0
+            runs.append((s.cpu().numpy(), q.cpu().numpy(), ctr.cpu().numpy()))
+    np.testing.assert_allclose(runs[0][0], runs[1][0], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(runs[0][1], runs[1][1], rtol=1e-12, atol=0)
+    assert runs[0][2].sum() == 0
+    assert runs[1][2][6] == cells * cfg.spp and runs[1][2][0] > 0
