@@ -593,9 +593,11 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
     AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     // the warp's cell and its next unclaimed sample (warp-uniform)
     uint32_t claim_cell = 0u, claim_next = L.spp;
+    uint32_t claim_band = 0u, claim_x = 0u, claim_y = 0u;  // divided out once per cell
     bool exhausted = false;
     // the lane's chain
-    uint32_t next = kNextIdle, pass = 0u, cell = 0u, sample = 0u, band = 0u, ray = kRayPrimary, depth = 0u,
+    uint32_t next = kNextIdle, pass = 0u, cell = 0u, sample = 0u, band = 0u, px = 0u, py = 0u, ray = kRayPrimary,
+             depth = 0u,
              ls = 0u, boundary = 0u, dim0 = 0u, dim1 = 0u;
     bool ground = false;
     Rng rng;
@@ -626,11 +628,18 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                         break;
                     }
                     claim_cell = cn;
+                    const uint32_t pixel = cn / L.band_count;
+                    claim_band = cn - pixel * L.band_count;
+                    claim_y = pixel / L.width;
+                    claim_x = pixel - claim_y * L.width;
                     claim_next = 0u;
                 }
                 const uint32_t rank = __popc(need & ((1u << lane) - 1u));
                 if (next == kNextIdle && claim_next + rank < L.spp) {
                     cell = claim_cell;
+                    band = claim_band;
+                    px = claim_x;
+                    py = claim_y;
                     sample = claim_next + rank;
                     pass = 0u;
                     next = kNextStart;
@@ -679,12 +688,10 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                         acc_cell = cell;
                         acc_sum = acc_sq = 0.0;
                     }
-                    band = cell % L.band_count;
-                    const uint32_t pixel = cell / L.band_count;
-                    const uint32_t x = pixel % L.width, y = pixel / L.width;
+                    const uint32_t pixel = py * L.width + px;
                     wc = kGrad ? __ldg(dloss + cell) * inv_spp : 0.0f;
                     rng.init(pixel, L.sample_offset + sample, band, L.seed_lo, L.seed_hi);
-                    dir = camera_dir(L, x, y, rng);
+                    dir = camera_dir(L, px, py, rng);
                     org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);
                     ++n.e[SKY_EVENT_CHAIN];
                     thr = 1.0f;
