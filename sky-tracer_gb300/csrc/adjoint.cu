@@ -200,8 +200,9 @@ __device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_
 
 // Residual-carry delta tracking over Q's tracking grid (track_ray_merged of
 // the plain tracer with the parameterised medium).  w_eval collects the
-// null-collision ratios of P over Q; with gw != 0 and the null-collision
-// estimator every null collision adds gw * d log(mu_bar - sigma_t).
+// null-collision ratios of P over Q; with kNullTerms (the null-collision
+// estimator) and gw != 0 every null collision adds gw * d log(mu_bar - sigma_t).
+template <bool kNullTerms>
 __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
                                           const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
                                           float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
@@ -237,7 +238,7 @@ __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, cons
             }
             const float sn = maj - mq.t;
             if (A.distinct && sn > 0.0f) w_eval *= (maj - adj_med(P, b).t) / sn;
-            if (A.estimator == SKY_ADJOINT_NULL_COLLISIONS && gw != 0.0f && sn > 0.0f)
+            if (kNullTerms && gw != 0.0f && sn > 0.0f)
                 null_terms(acc, Q, b, -gw / sn);
             tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
         } else {
@@ -344,7 +345,7 @@ __device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, co
     if (!(next_boundary(A.S, sg, st, sk) && sk == 1u)) return 0.0f;
     float th, w = 1.0f, tau_bar;
     AdjBase bh;
-    if (adj_track(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
+    if (adj_track<false>(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
     return w;
 }
 
@@ -379,7 +380,8 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
         if (!next_boundary(S, g, t_b, kind)) break;
         float t_hit, w_eval = 1.0f, tau_bar;
         AdjBase hb;
-        const bool hit = adj_track(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, 0.0f, acc, n, watchdog);
+        const bool hit =
+            adj_track<false>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, 0.0f, acc, n, watchdog);
         thr *= w_eval;
         if (hit) {
             ++n.e[SKY_EVENT_SCATTER];
@@ -557,8 +559,10 @@ enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLigh
                   kNextIdle = 5u };
 
 // kCount: count events (counters given); without it the counters are never
-// read and their increments compile away.
-template <int kPhase, bool kGrad, bool kCount>
+// read and their increments compile away.  kSegEst: the segment-integral
+// estimator (else null collisions); each instantiation holds only its own
+// gradient code.
+template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
 __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
@@ -589,7 +593,6 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
     n.clear();
     bool watchdog = false;
     const float inv_spp = 1.0f / float(L.spp), inv_lights = 1.0f / float(L.direct_light_samples);
-    const bool seg_est = A.estimator != SKY_ADJOINT_NULL_COLLISIONS;
     AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     // the warp's cell and its next unclaimed sample (warp-uniform)
     uint32_t claim_cell = 0u, claim_next = L.spp;
@@ -823,8 +826,9 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
             const uint32_t dim_seg = rng.dim;
             float t_hit = 0.0f, w_eval = 1.0f, tau_bar = 0.0f;
             AdjBase hit_b;
-            const bool hit = adj_track(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar, gw, acc, n, watchdog);
-            if (grad && seg_est) {
+            const bool hit = adj_track<!kSegEst>(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar, gw, acc,
+                                                 n, watchdog);
+            if (grad && kSegEst) {
                 // the segment integral of the traced part: a primary segment
                 // from its first random number, an unblocked shadow ray from
                 // the position after its tracking
@@ -874,7 +878,7 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
                     nee += term;
                     if (grad) {
                         if (!ground) vertex_terms(acc, P, bins, hb, adj_med(P, hb), mu, c);
-                        if (!seg_est && c != 0.0f) {  // trace it again for its null collisions
+                        if (!kSegEst && c != 0.0f) {  // trace it again for its null collisions
                             dim1 = rng.dim;
                             rng.dim = dim0;
                             ray = kRayRetrace;
@@ -1082,15 +1086,30 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 }
 
 // One launch of the ray-loop kernel, persistent grid.
+template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
+cudaError_t launch_ray_loop_est(const AdjCtx& A, const DevLaunch& L, const float* dloss, double* layer_grad,
+                            double* band_grad, unsigned long long* counters, uint32_t* status, uint32_t cells,
+                            uint32_t copies, uint32_t* next_cell, double* cell_sum, double* cell_sumsq, size_t smem,
+                            uint64_t want, cudaStream_t stream) {
+    const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst>);
+    adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst><<<grid_blocks(k, 256, smem, want), 256, smem, stream>>>(
+        A, L, dloss, layer_grad, band_grad, counters, status, cells, copies, next_cell, cell_sum, cell_sumsq);
+    return cudaGetLastError();
+}
+
+// The estimator's instantiation (the primal needs no gradient code: segment form).
 template <int kPhase, bool kGrad, bool kCount>
 cudaError_t launch_ray_loop(const AdjCtx& A, const DevLaunch& L, const float* dloss, double* layer_grad,
                             double* band_grad, unsigned long long* counters, uint32_t* status, uint32_t cells,
                             uint32_t copies, uint32_t* next_cell, double* cell_sum, double* cell_sumsq, size_t smem,
                             uint64_t want, cudaStream_t stream) {
-    const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<kPhase, kGrad, kCount>);
-    adjoint_grad_kernel<kPhase, kGrad, kCount><<<grid_blocks(k, 256, smem, want), 256, smem, stream>>>(
-        A, L, dloss, layer_grad, band_grad, counters, status, cells, copies, next_cell, cell_sum, cell_sumsq);
-    return cudaGetLastError();
+    if (kGrad && A.estimator == SKY_ADJOINT_NULL_COLLISIONS)
+        return launch_ray_loop_est<kPhase, kGrad, kCount, false>(A, L, dloss, layer_grad, band_grad, counters, status,
+                                                                 cells, copies, next_cell, cell_sum, cell_sumsq,
+                                                                 smem, want, stream);
+    return launch_ray_loop_est<kPhase, kGrad, kCount, true>(A, L, dloss, layer_grad, band_grad, counters, status,
+                                                            cells, copies, next_cell, cell_sum, cell_sumsq, smem,
+                                                            want, stream);
 }
 
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,

@@ -105,3 +105,23 @@ def test_pilot_budgets_equalise_errors(gpu, dome_scene):
         errs = np.array(sweep.errors())
     assert np.all(spp % 32 == 0) and spp.max() == 2048
     assert errs.max() / errs.min() < 1.6, (spp, p95, errs)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("elevation", [4.0, 35.0])
+def test_single_job_batch_uses_its_own_sun(gpu, dome_scene, elevation):
+    """A one-job batch runs the single-job kernel, which takes the sun frame
+    from the job's own scene parameters: with a sun other than the scene's it
+    still renders what a scene with that sun renders."""
+    import torch
+    base = RenderConfig(width=24, height=12, spp=32, phase_sampling=_abi.PHASE_TABULATED,
+                        tracking=_abi.TRACKING_MERGED_LAYERS, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
+    with GpuScene(dome_scene) as gs:
+        sweep = Sweep(gs, base, [elevation], [32])
+        sweep.launch(torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert int(sweep.status.item()) == 0
+        s = sweep.out[0].cell_sum.cpu().numpy()
+    with GpuScene(dome_scene.with_sun(elevation)) as single:
+        rs, _ = _sums(single, RenderConfig(**{**base.__dict__, "sun_elevation_deg": elevation}))
+    np.testing.assert_allclose(s, rs, rtol=1e-12, atol=0)
