@@ -200,9 +200,10 @@ __device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_
 
 // Residual-carry delta tracking over Q's tracking grid (track_ray_merged of
 // the plain tracer with the parameterised medium).  w_eval collects the
-// null-collision ratios of P over Q; with kNullTerms (the null-collision
+// null-collision ratios of P over Q (kMayDiffer: P and Q may be distinct
+// sets; the ray loop has P = Q); with kNullTerms (the null-collision
 // estimator) and gw != 0 every null collision adds gw * d log(mu_bar - sigma_t).
-template <bool kNullTerms>
+template <bool kNullTerms, bool kMayDiffer = true>
 __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
                                           const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
                                           float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
@@ -237,7 +238,7 @@ __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, cons
                 return true;
             }
             const float sn = maj - mq.t;
-            if (A.distinct && sn > 0.0f) w_eval *= (maj - adj_med(P, b).t) / sn;
+            if (kMayDiffer && A.distinct && sn > 0.0f) w_eval *= (maj - adj_med(P, b).t) / sn;
             if (kNullTerms && gw != 0.0f && sn > 0.0f)
                 null_terms(acc, Q, b, -gw / sn);
             tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
@@ -826,8 +827,8 @@ __global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_const
             const uint32_t dim_seg = rng.dim;
             float t_hit = 0.0f, w_eval = 1.0f, tau_bar = 0.0f;
             AdjBase hit_b;
-            const bool hit = adj_track<!kSegEst>(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar, gw, acc,
-                                                 n, watchdog);
+            const bool hit = adj_track<!kSegEst, false>(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar,
+                                                        gw, acc, n, watchdog);
             if (grad && kSegEst) {
                 // the segment integral of the traced part: a primary segment
                 // from its first random number, an unblocked shadow ray from
