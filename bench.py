@@ -235,8 +235,10 @@ def run_reference(args):
     value = statistics.median(vals)
     cfgw = {"workload": args.workload, "width": w["width"], "height": w["height"], "wavelengths": w["lam"][2],
             "spp": w["spp"], "l2": "compute-bound, tables < 1 MB"}
+    full_chains = w["width"] * w["height"] * w["lam"][2] * w["spp"]
     out = {"impl": "reference", "metric": "spectral path samples/s (chains/s)", "value": value,
            "unit": "chains/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": full_chains / value * 1e3,  # one full render at the sample's rate
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": cfgw,
            "cpu_baseline": {"value": value, "unit": "chains/s", "cores": threads, "kind": "port",
