@@ -562,9 +562,10 @@ enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLigh
 // kCount: count events (counters given); without it the counters are never
 // read and their increments compile away.  kSegEst: the segment-integral
 // estimator (else null collisions); each instantiation holds only its own
-// gradient code.
+// gradient code.  Resident blocks: 4 per SM for the primal (64 registers),
+// 3 for the gradient passes (80 registers; 4 gains nothing there).
 template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
-__global__ void __launch_bounds__(256, 3) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
+__global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
                                                               double* __restrict__ layer_grad,
