@@ -323,10 +323,6 @@ __device__ __forceinline__ float mie_phase_u(const DevScene& S, uint32_t species
     return fmaxf(fmaf(t, p1 - p0, p0), 0.0f);
 }
 
-__device__ __forceinline__ float mie_phase(const DevScene& S, uint32_t species, uint32_t band, float mu) {
-    return mie_phase_u(S, species, band, phase_grid_u(mu));
-}
-
 // mixed_phase_value (sky_trace.wgsl:496-510), at grid position u of mu.
 __device__ __forceinline__ float mixed_phase_u(const DevScene& S, const Coeffs& c, uint32_t band, float mu, float u) {
     if (c.scattering <= 0.0f) return 0.0f;

@@ -40,7 +40,6 @@ struct WaveLaunch {
 // the jobs' cell sums (zeroed first unless a job accumulates), film, XYZ,
 // XYZ variance and linear sRGB.
 cudaError_t launch_trace_wave(const WaveLaunch& w, cudaStream_t stream);
-uint32_t wave_blocks_per_sm(uint32_t variant);
 // The tracing kernel alone, per tracking mode (trace_wave_*.cu).
 cudaError_t launch_wave_segment_restart(const WaveLaunch& w, cudaStream_t stream);
 cudaError_t launch_wave_residual_carry(const WaveLaunch& w, cudaStream_t stream);

@@ -28,10 +28,6 @@ __global__ void __launch_bounds__(256) wave_prepare_kernel(const DevJob* __restr
 
 }  // namespace
 
-uint32_t wave_blocks_per_sm(uint32_t variant) {
-    return variant == 1u ? 2u : (variant == 2u ? 4u : 3u);
-}
-
 cudaError_t launch_trace_wave(const WaveLaunch& w, cudaStream_t stream) {
     if (w.num_jobs == 0u || w.num_jobs > 65535u || w.total_cells == 0u) return cudaErrorInvalidValue;
     const uint32_t xblocks =
