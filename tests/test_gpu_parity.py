@@ -287,3 +287,68 @@ def test_event_counting_does_not_change_the_render(gpu, dome_scene, tracking):
     np.testing.assert_allclose(runs[0][1], runs[1][1], rtol=1e-12, atol=0)
     assert runs[0][2].sum() == 0
     assert runs[1][2][6] == cells * cfg.spp and runs[1][2][0] > 0
+
+
+def _device_buffers(cells: int, pixels: int):
+    import torch
+    return {"s": torch.zeros(cells, dtype=torch.float64, device="cuda"),
+            "q": torch.zeros(cells, dtype=torch.float64, device="cuda"),
+            "film": torch.zeros(cells, dtype=torch.float32, device="cuda"),
+            "xyz": torch.zeros(pixels * 3, dtype=torch.float64, device="cuda"),
+            "st": torch.zeros(1, dtype=torch.int32, device="cuda")}
+
+
+def _outs(b, first=True):
+    o = {"cell_sum": b["s"].data_ptr(), "cell_sumsq": b["q"].data_ptr(), "film": b["film"].data_ptr(),
+         "xyz": b["xyz"].data_ptr()}
+    if first:
+        o["status"] = b["st"].data_ptr()
+    return o
+
+
+def test_one_pixel_odd_spp_matches_plain(gpu, dome_scene):
+    """A 1x1 image at 5 samples: one cell whose samples do not fill a warp."""
+    cfg = RenderConfig(width=1, height=1, spp=5, sample_offset=3, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    with GpuScene(dome_scene) as gs:
+        a, qa, _, sa = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_PLAIN}))
+        b, qb, _, sb = gpu_sums(gs, RenderConfig(**{**cfg.__dict__, "kernel": _abi.KERNEL_WAVEFRONT}))
+    assert sa == 0 and sb == 0
+    np.testing.assert_allclose(b, a, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(qb, qa, rtol=1e-12, atol=0)
+
+
+def test_batch_of_unequal_jobs_matches_separate_renders(gpu, dome_scene):
+    """Jobs of different image sizes, projections and spp in one launch (the
+    cell-to-job lookup and the per-job finalize), one of them accumulating
+    onto sums it already holds, against the same renders made one by one."""
+    import torch
+    stream = torch.cuda.current_stream().cuda_stream
+    cfgs = [RenderConfig(width=24, height=12, spp=16, phase_sampling=_abi.PHASE_TABULATED,
+                         tracking=_abi.TRACKING_MERGED_LAYERS, seed=11),
+            RenderConfig(width=7, height=3, spp=40, phase_sampling=_abi.PHASE_TABULATED,
+                         tracking=_abi.TRACKING_MERGED_LAYERS, output_projection=_abi.PROJECTION_SKY_VIEW_LUT,
+                         seed=12),
+            RenderConfig(width=16, height=16, spp=8, sample_offset=8, flags=FLAG_ACCUMULATE,
+                         phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS, seed=13)]
+    with GpuScene(dome_scene) as gs:
+        B = gs.band_count
+        bufs = [_device_buffers(c.pixels * B, c.pixels) for c in cfgs]
+        # the accumulating job continues a render of samples 0..7 already in its buffers
+        first = RenderConfig(**{**cfgs[2].__dict__, "spp": 8, "sample_offset": 0, "flags": 0})
+        gs.render_device(first, _outs(bufs[2]), stream)
+        gs.render_batch([(c, None, _outs(b, i == 0)) for i, (c, b) in enumerate(zip(cfgs, bufs))], stream)
+        torch.cuda.synchronize()
+        assert int(bufs[0]["st"].item()) == 0
+        want = []
+        for c in cfgs:
+            b = _device_buffers(c.pixels * B, c.pixels)
+            if c.flags:
+                gs.render_device(first, _outs(b), stream)
+            gs.render_device(c, _outs(b), stream)
+            want.append(b)
+        torch.cuda.synchronize()
+    for got, ref in zip(bufs, want):
+        np.testing.assert_allclose(got["s"].cpu().numpy(), ref["s"].cpu().numpy(), rtol=1e-12, atol=0)
+        np.testing.assert_allclose(got["film"].cpu().numpy(), ref["film"].cpu().numpy(), rtol=1e-6, atol=0)
+        np.testing.assert_allclose(got["xyz"].cpu().numpy(), ref["xyz"].cpu().numpy(), rtol=1e-12, atol=1e-300)
