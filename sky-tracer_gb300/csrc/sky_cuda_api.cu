@@ -132,6 +132,8 @@ int validate_config(const SkyScene* scene, const SkyRenderConfig* c) {
         return set_error(SKY_ERR_INVALID_CONFIG, "film is too large for the GPU shader index type");
     if (uint64_t(c->sample_offset) + c->spp > 0xffffffffull)
         return set_error(SKY_ERR_INVALID_CONFIG, "sample indices overflow 32 bits");
+    // the kernels hand out samples in steps of up to 32 with 32-bit counters
+    if (c->spp > 0x7fffffffu) return set_error(SKY_ERR_INVALID_CONFIG, "spp must be below 2^31");
     if (c->output_projection > SKY_PROJECTION_SKY_VIEW_LUT)
         return set_error(SKY_ERR_INVALID_CONFIG, "unknown output projection");
     if (c->phase_sampling > SKY_PHASE_TABULATED)

@@ -212,7 +212,10 @@ def test_watchdog_and_errors(gpu, dome_scene):
         with pytest.raises(SkyCudaError) as e:
             gs.render(RenderConfig(width=0, height=4, spp=4))
         assert e.value.status == _abi.SKY_ERR_INVALID_CONFIG
-        # the scene stays usable after both failures
+        # sample counts that the kernels' 32-bit sample counters could not step through
+        with pytest.raises(SkyCudaError, match="spp must be below"):
+            gs.render(RenderConfig(width=1, height=1, spp=0x80000000))
+        # the scene stays usable after the failures
         film, _ = gs.render(RenderConfig(width=8, height=4, spp=4))
         assert np.all(np.isfinite(film.values))
 
