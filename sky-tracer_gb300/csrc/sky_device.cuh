@@ -441,11 +441,11 @@ __device__ __forceinline__ V3 sample_cosine_hemisphere(V3 axis, Rng& rng, float&
     return dir;
 }
 
-// Tabulated continuation direction (phase.rs:53-75, sampling.rs:182-185):
-// component by sigma_s,i / sigma_s, mu from its inverse CDF, then phi.
-// Returns mixed_phase(mu) / mixture_pdf(mu).
-__device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeffs& c, uint32_t band, V3 axis,
-                                                  Rng& rng, V3& out_dir) {
+// Tabulated continuation (phase.rs:53-75, sampling.rs:182-185): component by
+// sigma_s,i / sigma_s, mu from its inverse CDF, and the draw for phi; returns
+// mixed_phase(mu) / mixture_pdf(mu), which does not depend on phi.
+__device__ __forceinline__ float tabulated_mu(const DevScene& S, const Coeffs& c, uint32_t band, Rng& rng, float& mu,
+                                             float& xi_phi) {
     float target = rng.next() * c.scattering;
     int chosen = -1;
     float acc = c.rayleigh;
@@ -462,9 +462,8 @@ __device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeff
             if (c.sca[i] > 0.0f) chosen = i + 1;
     }
     float xi_mu = rng.next();
-    float mu = chosen == 0 ? invert_rayleigh_cdf(xi_mu) : sample_mie_mu(S, uint32_t(chosen - 1), band, xi_mu);
-    float xi_phi = rng.next();
-    out_dir = direction_from_axis_mu(axis, mu, xi_phi);
+    mu = chosen == 0 ? invert_rayleigh_cdf(xi_mu) : sample_mie_mu(S, uint32_t(chosen - 1), band, xi_mu);
+    xi_phi = rng.next();
     float inv_s = 1.0f / c.scattering;
     const float u = phase_grid_u(mu);  // shared by the pdf and the phase lookups
     float pdf = c.rayleigh * inv_s * rayleigh_phase(mu);
@@ -472,6 +471,15 @@ __device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeff
     for (int i = 0; i < int(kSpecies); ++i)
         if (c.sca[i] > 0.0f) pdf = fmaf(c.sca[i] * inv_s, mie_sampling_pdf_u(S, uint32_t(i), band, u), pdf);
     return mixed_phase_u(S, c, band, mu, u) / pdf;
+}
+
+// The tabulated continuation direction around `axis`; returns the weight.
+__device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeffs& c, uint32_t band, V3 axis,
+                                                  Rng& rng, V3& out_dir) {
+    float mu, xi_phi;
+    const float w = tabulated_mu(S, c, band, rng, mu, xi_phi);
+    out_dir = direction_from_axis_mu(axis, mu, xi_phi);
+    return w;
 }
 
 // ---- cameras (sky_trace.wgsl:610-689) --------------------------------------------------

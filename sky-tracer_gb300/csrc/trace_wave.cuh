@@ -213,25 +213,49 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     break;
                 }
                 if (next == kLights) {
-                    // the continuation (sky_trace.wgsl:728-767)
+                    // the continuation (sky_trace.wgsl:728-767): each branch draws its
+                    // angles, then one shared frame step turns them into the direction
+                    // (orthonormal_basis + direction_from_frame, as direction_from_axis_mu
+                    // and sample_cosine_hemisphere compute it), so that medium and ground
+                    // lanes run that step together
                     rad += thr * (nee * (1.0f / float(lights)));
-                    V3 nd;
-                    bool alive = true;
+                    V3 nd = mk(0.0f, 1.0f, 0.0f), axis = dir;
+                    float cos_t = 1.0f, sin_t = 0.0f, xi_phi = 0.0f, weight = 1.0f;
+                    bool framed = true;
                     if (!ground) {
                         const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
                         if (kPhase == SKY_PHASE_TABULATED) {
-                            thr *= sample_tabulated(S, c, band, dir, rng, nd);
+                            float mu;
+                            weight = tabulated_mu(S, c, band, rng, mu, xi_phi);
+                            cos_t = fminf(fmaxf(mu, -1.0f), 1.0f);
+                            sin_t = sqrtf(fmaxf(1.0f - cos_t * cos_t, 0.0f));
                         } else {
                             nd = sample_isotropic(rng);
-                            thr *= mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                            weight = mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                            framed = false;
                         }
                     } else {
-                        const V3 normal = normalize_or_y(org);
-                        float pdf;
-                        nd = sample_cosine_hemisphere(normal, rng, pdf);
-                        const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+                        axis = normalize_or_y(org);  // the ground normal
+                        const float u = rng.next();
+                        sin_t = sqrtf(u);
+                        xi_phi = rng.next();
+                        cos_t = sqrtf(fmaxf(1.0f - u, 0.0f));
+                    }
+                    V3 n = axis;
+                    if (framed) {
+                        V3 t, bt;
+                        orthonormal_basis(axis, t, bt);
+                        n = normalize_or_y(axis);
+                        nd = direction_from_frame(n, t, bt, cos_t, sin_t, xi_phi);
+                    }
+                    bool alive = true;
+                    if (ground) {
+                        const float pdf = fmaxf(dot3(n, nd), 0.0f) * kInvPi;
+                        const float cos_out = fmaxf(dot3(axis, nd), 0.0f);
                         if (pdf <= 0.0f || cos_out <= 0.0f) alive = false;
                         else thr *= S.ground_albedo * kInvPi * cos_out / pdf;
+                    } else {
+                        thr *= weight;
                     }
                     if (alive && depth >= JL.rr_start_depth) {  // russian_roulette (:691-701)
                         const float q = fminf(fmaxf(thr, 0.05f), 0.95f);
