@@ -760,7 +760,11 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                     continue;
                 }
                 rad += thr * (nee * inv_lights);
-                V3 nd;
+                // each branch draws its angles; one shared frame step turns them into
+                // the direction (as direction_from_axis_mu / sample_cosine_hemisphere)
+                V3 nd = mk(0.0f, 1.0f, 0.0f), axis = dir;
+                float cos_t = 1.0f, sin_t = 0.0f, xi_phi = 0.0f;
+                bool framed = true;
                 if (!ground) {
                     const AdjMed mq = adj_med(P, hb);
                     float mu_c, fq;
@@ -769,13 +773,15 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                         const bool rayleigh = target < mq.R || !(mq.Ms > 0.0f);
                         const float xi_mu = rng.next();
                         mu_c = rayleigh ? invert_rayleigh_cdf(xi_mu) : hg_sample_mu(P, bins, xi_mu);
-                        const float xi_phi = rng.next();
-                        nd = direction_from_axis_mu(dir, mu_c, xi_phi);
+                        xi_phi = rng.next();
+                        cos_t = fminf(fmaxf(mu_c, -1.0f), 1.0f);
+                        sin_t = sqrtf(fmaxf(1.0f - cos_t * cos_t, 0.0f));
                         const float pdf = mq.R * rayleigh_phase(mu_c) +
                                           (mq.Ms > 0.0f ? mq.Ms * hg_sampling_pdf(P, bins, mu_c) : 0.0f);
                         fq = vertex_phase(P, bins, mq, mu_c) / pdf;
                     } else {
                         nd = sample_isotropic(rng);
+                        framed = false;
                         mu_c = dot3(dir, nd);
                         fq = vertex_phase(P, bins, mq, mu_c) / mq.s / kIsotropicPdf;
                     }
@@ -783,10 +789,22 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                     if (kGrad && pass == 1u) vertex_terms(acc, P, bins, hb, mq, mu_c, w * (total - rad));
                 } else {
                     // the Lambert bounce (sky_trace.wgsl:750-766)
-                    const V3 normal = normalize_or_y(org);
-                    float pdf;
-                    nd = sample_cosine_hemisphere(normal, rng, pdf);
-                    const float cos_out = fmaxf(dot3(normal, nd), 0.0f);
+                    axis = normalize_or_y(org);
+                    const float u = rng.next();
+                    sin_t = sqrtf(u);
+                    xi_phi = rng.next();
+                    cos_t = sqrtf(fmaxf(1.0f - u, 0.0f));
+                }
+                V3 fn = axis;
+                if (framed) {
+                    V3 t, bt;
+                    orthonormal_basis(axis, t, bt);
+                    fn = normalize_or_y(axis);
+                    nd = direction_from_frame(fn, t, bt, cos_t, sin_t, xi_phi);
+                }
+                if (ground) {
+                    const float pdf = fmaxf(dot3(fn, nd), 0.0f) * kInvPi;
+                    const float cos_out = fmaxf(dot3(axis, nd), 0.0f);
                     if (pdf <= 0.0f || cos_out <= 0.0f) {
                         rad = fmaxf(rad, 0.0f);
                         next = kNextEnd;
