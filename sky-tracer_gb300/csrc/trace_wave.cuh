@@ -104,7 +104,10 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     Rng rng;
     rng.k0 = rng.k1 = rng.k2 = rng.dim = 0u;
     V3 org = mk(0.0f, 0.0f, 0.0f), dir = org;  // org is the vertex position between rays
-    float thr = 0.0f, rad = 0.0f, nee = 0.0f, alt = 0.0f, term = 0.0f, t_max = 0.0f;
+    // nee_mu: the pending shadow ray's cosine (to the incoming direction at a
+    // medium vertex, to the normal on the ground); its NEE term is evaluated
+    // after the trace, and only when the ray reaches the sun
+    float thr = 0.0f, rad = 0.0f, nee = 0.0f, alt = 0.0f, nee_mu = 0.0f, t_max = 0.0f;
     RayGeo g{0.0f, 0.0f, 0.0f};
     // FP64 sums of the lane's current cell
     uint32_t acc_job = 0u, acc_cell = kNoCell;
@@ -187,7 +190,6 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 // direct_sun_at_scatter (sky_trace.wgsl:566-585) and ground_radiance
                 // (:587-608), one shadow ray at a time
                 const uint32_t lights = JL.direct_light_samples;
-                const float l_sun = __ldg(&S.bands[band].solar_radiance);
                 while (ls < lights) {
                     ++ls;
                     const V3 ldir = sample_sun_cone(job_scene<kSingle>(S, jobs, job), rng);
@@ -201,13 +203,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     uint32_t kind;
                     ++n.e[SKY_EVENT_BOUNDARY];
                     if (!(next_boundary(S, g, t_max, kind) && kind == 1u)) continue;
-                    // the sample's term if the shadow ray reaches the sun (transmittance 1)
-                    if (ground) {
-                        term = S.ground_albedo * kInvPi * l_sun * 1.0f * cos_sun / S.light_pdf;
-                    } else {
-                        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
-                        term = l_sun * 1.0f * mixed_phase(S, c, band, dot3(dir, ldir)) / S.light_pdf;
-                    }
+                    nee_mu = ground ? cos_sun : dot3(dir, ldir);
                     shadow_ray = true;
                     next = kTrace;
                     break;
@@ -305,14 +301,24 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         if (tracing) {
             float t_hit = 0.0f;
             const bool hit = track_ray<kTracking>(S, g, t_max, band, rng, t_hit, n, watchdog);
+            // the medium coefficients at a real collision (albedo) and at the vertex of
+            // an unblocked shadow ray (phase of its NEE term): one call for both kinds
+            const bool lit = shadow_ray && !hit;
+            if (!shadow_ray && hit) {
+                org = madd(org, dir, t_hit);
+                alt = altitude_at(g, t_hit, S.ground_radius);
+            }
+            Coeffs c;
+            if ((!shadow_ray && hit) || (lit && !ground)) c = coefficients_at(S, S.knot_z, S.finder, band, alt);
             if (shadow_ray) {
-                if (!hit) nee += term;
+                if (lit) {  // the sample's term, transmittance 1 (sky_trace.wgsl:566-608)
+                    const float l_sun = __ldg(&S.bands[band].solar_radiance);
+                    nee += ground ? S.ground_albedo * kInvPi * l_sun * 1.0f * nee_mu / S.light_pdf
+                                  : l_sun * 1.0f * mixed_phase(S, c, band, nee_mu) / S.light_pdf;
+                }
                 next = kLights;
             } else if (hit) {
                 ++n.e[SKY_EVENT_SCATTER];
-                org = madd(org, dir, t_hit);
-                alt = altitude_at(g, t_hit, S.ground_radius);
-                const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
                 const bool medium = c.extinction > 0.0f && c.scattering > 0.0f;
                 if (medium) thr *= fminf(fmaxf(c.scattering / c.extinction, 0.0f), 1.0f);
                 if (!medium || thr <= 0.0f) {
