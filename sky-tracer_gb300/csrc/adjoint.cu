@@ -835,7 +835,7 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
         }
         const bool tracing = next == kNextTrace;
         if (!__any_sync(0xffffffffu, tracing)) {
-            if (exhausted) break;  // every lane idle and no cell left
+            if (exhausted && __all_sync(0xffffffffu, next == kNextIdle)) break;  // no cell left, every lane idle
             continue;
         }
         if (tracing) {

@@ -294,8 +294,9 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         }
         const bool tracing = next == kTrace;
         if (!__any_sync(kFull, tracing)) {
-            // every lane idle (or ending a chain, summed next iteration) and no cell left
-            if (exhausted && !__any_sync(kFull, next == kEnd)) break;
+            // no cell left and every lane idle (a lane ending its chain is summed next
+            // iteration)
+            if (exhausted && __all_sync(kFull, next == kIdle)) break;
             continue;
         }
         if (tracing) {
