@@ -286,6 +286,14 @@ def run_sweep(args):
 
     # 32 separate plain launches: per-elevation budgets, and one uniform spp
     singles = [GpuScene(scene.with_sun(float(e))) for e in elevations]
+    # at the plain kernel's own fastest crossing cost, tuned on the middle elevation
+    from sky_cuda.autotune import DEFAULT_SPACE, autotune
+    mid = len(singles) // 2
+    probe = RenderConfig(**{**base.__dict__, "spp": 256, "sun_elevation_deg": float(elevations[mid]),
+                            "kernel": _abi.KERNEL_PLAIN})
+    plain_tuning, _ = autotune(singles[mid], probe, space={"crossing_cost": DEFAULT_SPACE["crossing_cost"]})
+    for g in singles:
+        g.set_tuning(crossing_cost=plain_tuning["crossing_cost"])
     cells = base.pixels * scene.band_count
     bufs = [torch.zeros(cells, dtype=torch.float64, device="cuda") for _ in range(3)]
     xyz = torch.zeros(base.pixels * 3, dtype=torch.float64, device="cuda")
@@ -339,6 +347,8 @@ def run_sweep(args):
             "speedup_time_to_1pct": t1_plain_uniform / t1_batched,
             "speedup_vs_plain_same_budgets": t_plain_budget / t_batched,
             "plain_chains_per_s": chains_batched / t_plain_budget,
+            "plain_crossing_cost": round(float(plain_tuning["crossing_cost"]), 3),
+            "batched_crossing_cost": round(float(gs.get_tuning()["crossing_cost"]), 3),
         },
         "clocks": clocks.summary(),
         "gpu_launches": 3 * args.steps,  # prepare, trace, finalize per replay
@@ -630,10 +640,12 @@ def main():
         gs.set_tuning(**{k: (float(v) if k == "crossing_cost" else int(v))
                          for k, v in (kv.split("=") for kv in args.tuning.split(","))})
     tuning_log = None
-    if not args.no_autotune and cfg.kernel != 1:
-        from sky_cuda.autotune import autotune
+    if not args.no_autotune:
+        from sky_cuda.autotune import DEFAULT_SPACE, autotune
         t0 = time.perf_counter()
-        best, trials = autotune(gs, cfg)
+        # the plain kernel has one shape: only its crossing cost is tuned
+        space = None if cfg.kernel != 1 else {"crossing_cost": DEFAULT_SPACE["crossing_cost"]}
+        best, trials = autotune(gs, cfg, space=space)
         tuning_log = {"chosen": best, "seconds": round(time.perf_counter() - t0, 2),
                       "trials": [[t["variant"], round(t["crossing_cost"], 3), round(ms, 3)]
                                  for t, ms in trials]}

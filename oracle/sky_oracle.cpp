@@ -141,8 +141,9 @@ struct Ctx {
 };
 
 // Grouping of uniform majorant layers for tracking mode 2: contiguous groups
-// minimising sum_groups [0.25 + dz * sum_k (max_group - maj_k)] (the cost of a
-// layer crossing against the expected extra null collisions of a vertical ray).
+// minimising sum_groups [0.1 + dz * sum_k (max_group - maj_k)] (the cost of a
+// layer crossing against the expected extra null collisions of a vertical ray;
+// 0.1 is the CUDA library's default crossing cost).
 std::vector<uint32_t> merge_groups(const float* maj, uint32_t L, float dz) {
     std::vector<double> best(L + 1, 0.0);
     std::vector<uint32_t> from(L + 1, 0);
@@ -153,7 +154,7 @@ std::vector<uint32_t> merge_groups(const float* maj, uint32_t L, float dz) {
             double m = std::max(double(maj[i]), 1e-8);
             mx = std::max(mx, m);
             sum += m;
-            double c = best[i] + 0.25 + (mx * double(j - i) - sum) * double(dz);
+            double c = best[i] + 0.1 + (mx * double(j - i) - sum) * double(dz);
             if (c < best[j]) {
                 best[j] = c;
                 from[j] = i;
