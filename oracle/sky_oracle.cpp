@@ -1151,4 +1151,13 @@ float oracle_cpu_extinction(const SkySceneDesc* s, float altitude, uint32_t band
     return cpu_extinction_total(cpu_coefficients_at(s, altitude, band));
 }
 
+// The merged-layer grouping of tracking mode 2 for one band's majorants: writes
+// the first uniform layer of each group to starts_out[0..L) and returns the
+// number of groups.
+uint32_t oracle_merge_groups(const float* majorants, uint32_t layer_count, float layer_dz, uint32_t* starts_out) {
+    const std::vector<uint32_t> starts = merge_groups(majorants, layer_count, layer_dz);
+    for (size_t i = 0; i < starts.size(); ++i) starts_out[i] = starts[i];
+    return uint32_t(starts.size());
+}
+
 }  // extern "C"

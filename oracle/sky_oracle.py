@@ -52,6 +52,8 @@ def load():
     lib.oracle_bake_majorant_grid.argtypes = [vp, ctypes.c_uint32, fp, fp]
     lib.oracle_cpu_extinction.argtypes = [vp, ctypes.c_float, ctypes.c_uint32]
     lib.oracle_cpu_extinction.restype = ctypes.c_float
+    lib.oracle_merge_groups.argtypes = [fp, ctypes.c_uint32, ctypes.c_float, u32p]
+    lib.oracle_merge_groups.restype = ctypes.c_uint32
     _lib = lib
     return lib
 
@@ -157,6 +159,14 @@ def bake_majorant_grid(scene, layers: int):
     desc = scene.desc()
     lib.oracle_bake_majorant_grid(ctypes.byref(desc), layers, _f(maj), _f(mino))
     return maj.reshape(scene.band_count, layers), mino.reshape(scene.band_count, layers)
+
+
+def merge_groups(majorants, layer_dz: float) -> list[int]:
+    """First uniform layer of each merged group of tracking mode 2."""
+    maj = np.ascontiguousarray(majorants, dtype=np.float32)
+    starts = np.zeros(len(maj), dtype=np.uint32)
+    n = load().oracle_merge_groups(_f(maj), len(maj), layer_dz, starts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    return [int(v) for v in starts[:n]]
 
 
 def cpu_extinction(scene, altitude_km: float, band: int) -> float:

@@ -191,7 +191,8 @@ def test_oracle_vacuum_ground_and_sky(data_dir):
                 assert mean[y, band] == 0.0
 
 
-@pytest.mark.parametrize("tracking", [_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY])
+@pytest.mark.parametrize("tracking", [_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY,
+                                      _abi.TRACKING_MERGED_LAYERS])
 def test_oracle_single_scatter_integral(data_dir, tracking):
     a = SyntheticAtmosphere(ground_albedo=0.0)
     scene = synthetic_scene(wavelengths(440, 640, 3), data_dir, sun_elevation_deg=35.0, atmosphere=a)
@@ -217,10 +218,12 @@ def _small_parity(scene, cfg_a, cfg_b):
     return parity_report(xa, va, xb, vb)
 
 
-def test_oracle_tracking_modes_agree(data_dir):
+@pytest.mark.parametrize("other", [_abi.TRACKING_RESIDUAL_CARRY, _abi.TRACKING_MERGED_LAYERS])
+def test_oracle_tracking_modes_agree(data_dir, other):
     scene = synthetic_scene(wavelengths(400, 700, 4), data_dir, sun_elevation_deg=10.0)
     base = dict(width=8, height=6, spp=256, phase_sampling=_abi.PHASE_TABULATED, max_orders=16)
-    r = _small_parity(scene, RenderConfig(**base, tracking=0), RenderConfig(**base, tracking=1, seed=99))
+    r = _small_parity(scene, RenderConfig(**base, tracking=_abi.TRACKING_SEGMENT_RESTART),
+                      RenderConfig(**base, tracking=other, seed=99))
     assert r["frac_beyond_3se"] <= 0.05 and abs(r["mean_z"]) < 1.0, r
 
 
@@ -230,3 +233,29 @@ def test_oracle_phase_sampling_modes_agree(data_dir):
     r = _small_parity(scene, RenderConfig(**base, phase_sampling=0),
                       RenderConfig(**base, phase_sampling=1, seed=7))
     assert r["frac_beyond_3se"] <= 0.05 and abs(r["mean_z"]) < 1.0, r
+
+
+def _group_cost(maj, starts, dz, crossing_cost=0.1):
+    m = np.maximum(np.asarray(maj, dtype=np.float64), 1e-8)
+    bounds = list(starts) + [len(m)]
+    return sum(crossing_cost + dz * (m[a:b].max() * (b - a) - m[a:b].sum()) for a, b in zip(bounds[:-1], bounds[1:]))
+
+
+def test_merge_groups_is_optimal():
+    """Tracking mode 2's layer grouping is the partition of least cost (a crossing
+    costs 0.1 null collisions, a group costs its majorant excess times dz): checked
+    against every partition of small random grids."""
+    import itertools
+    rng = np.random.default_rng(8)
+    for trial in range(40):
+        L = int(rng.integers(1, 10))
+        dz = float(rng.choice([0.05, 0.5, 1.5625, 4.0]))
+        maj = (rng.lognormal(-3.0, 1.5, size=L) * (rng.random(L) < 0.9)).astype(np.float32)
+        starts = oracle.merge_groups(maj, dz)
+        assert starts[0] == 0 and all(a < b for a, b in zip(starts, starts[1:])) and starts[-1] < L
+        best = min(_group_cost(maj, [0] + [i + 1 for i in range(L - 1) if cut[i]], dz)
+                   for cut in itertools.product((False, True), repeat=L - 1))
+        assert _group_cost(maj, starts, dz) <= best * (1 + 1e-12) + 1e-15, (trial, L, dz, starts)
+    # a uniform grid has no excess to pay for: one group; far-apart majorants in thick layers: none merge
+    assert oracle.merge_groups(np.full(12, 0.02, np.float32), 1.0) == [0]
+    assert oracle.merge_groups(np.array([1.0, 0.001, 1.0, 0.001], np.float32), 10.0) == [0, 1, 2, 3]
