@@ -180,12 +180,10 @@ def measure_fp32_peak(torch, dev):
 
 def time_to_1pct(xyz, var, seconds_per_render):
     """Time to 1 % per-pixel XYZ error: the 95th percentile over pixels of the
-    worst X/Y/Z relative standard error, pixels with Y < 1e-3 p99(Y)
-    excluded, scaled as 1/sqrt(samples)."""
-    y = xyz[:, 1]
-    keep = y >= 1e-3 * np.percentile(y, 99)
-    rel = np.sqrt(np.maximum(var[keep], 0)) / np.maximum(np.abs(xyz[keep]), 1e-30)
-    p95 = float(np.percentile(rel.max(axis=1), 95))
+    worst X/Y/Z relative standard error (pixels with Y < 1e-3 p99(Y)
+    excluded), scaled as 1/sqrt(samples)."""
+    from sky_cuda.sweep import p95_relative_error
+    p95 = p95_relative_error(xyz, var)
     return p95, seconds_per_render * (p95 / 0.01) ** 2
 
 
