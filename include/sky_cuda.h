@@ -168,7 +168,7 @@ typedef struct SkyRenderConfig {
     uint32_t width;
     uint32_t height;
     uint32_t spp;
-    uint32_t direct_light_samples;  /* 0 is treated as 1 (integrator.rs:325) */
+    uint32_t direct_light_samples;  /* 0 is treated as 1 (integrator.rs:325); at most 1024 */
     uint64_t seed;
     float sun_elevation_deg;        /* recorded only; the sun is in the scene */
     float sun_azimuth_deg;

@@ -134,6 +134,9 @@ int validate_config(const SkyScene* scene, const SkyRenderConfig* c) {
         return set_error(SKY_ERR_INVALID_CONFIG, "sample indices overflow 32 bits");
     // the kernels hand out samples in steps of up to 32 with 32-bit counters
     if (c->spp > 0x7fffffffu) return set_error(SKY_ERR_INVALID_CONFIG, "spp must be below 2^31");
+    // each NEE sample is a shadow ray per vertex: an unbounded count would keep a launch running for hours
+    if (c->direct_light_samples > kMaxLightSamples)
+        return set_error(SKY_ERR_INVALID_CONFIG, "direct_light_samples must be at most 1024");
     if (c->output_projection > SKY_PROJECTION_SKY_VIEW_LUT)
         return set_error(SKY_ERR_INVALID_CONFIG, "unknown output projection");
     if (c->phase_sampling > SKY_PHASE_TABULATED)

@@ -29,6 +29,7 @@ constexpr uint32_t kFinderCells = 512;
 constexpr uint32_t kMaxLayers = 1024;
 constexpr uint32_t kDefaultWatchdog = 1024;  // integrator.rs:14
 constexpr uint32_t kDefaultRrDepth = 4;      // sky_trace.wgsl:692
+constexpr uint32_t kMaxLightSamples = 1024;  // NEE samples per vertex accepted by a render config
 constexpr float kRayEpsilonKm = 0.005f;      // sky_trace.wgsl:8
 
 // Per-band constants.

@@ -215,6 +215,9 @@ def test_watchdog_and_errors(gpu, dome_scene):
         # sample counts that the kernels' 32-bit sample counters could not step through
         with pytest.raises(SkyCudaError, match="spp must be below"):
             gs.render(RenderConfig(width=1, height=1, spp=0x80000000))
+        # NEE sample counts that would keep a launch running for hours
+        with pytest.raises(SkyCudaError, match="direct_light_samples"):
+            gs.render(RenderConfig(width=1, height=1, spp=1, direct_light_samples=1025))
         # the scene stays usable after the failures
         film, _ = gs.render(RenderConfig(width=8, height=4, spp=4))
         assert np.all(np.isfinite(film.values))
