@@ -858,6 +858,9 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
 int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& L) {
     int st = validate_config(s, c);
     if (st) return st;
+    // the ray loop's 32-bit cell counter also counts one failed claim per warp
+    if (uint64_t(c->width) * c->height * s->dev.band_count > kMaxLaunchCells)
+        return set_error(SKY_ERR_INVALID_CONFIG, "a launch holds at most 4026531840 (pixel, band) cells");
     if (c->tracking != SKY_TRACKING_RESIDUAL_CARRY && c->tracking != SKY_TRACKING_MERGED_LAYERS)
         return set_error(SKY_ERR_INVALID_CONFIG,
                          "differentiable renders track with SKY_TRACKING_RESIDUAL_CARRY or SKY_TRACKING_MERGED_LAYERS");
