@@ -91,6 +91,29 @@ def test_sky_view_lut_chains_match_oracle(gpu, dome_scene, kernel):
     assert frac >= 0.95
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_several_light_samples_match_oracle(gpu, dome_scene, kernel):
+    """Three sun samples per vertex (direct_sun_at_scatter / ground_radiance
+    loop over direct_light_samples, sky_trace.wgsl:566-608): the wavefront
+    kernel traces them as successive shadow rays of one vertex; chain by chain
+    against the oracle."""
+    agree = total = 0
+    with GpuScene(dome_scene) as gs:
+        for offset in (0, 5):
+            cfg = RenderConfig(width=16, height=8, spp=1, sample_offset=offset, seed=0x5EC7_2026_0430 + offset,
+                               phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS,
+                               max_orders=16, kernel=kernel, direct_light_samples=3)
+            g, _, _, st = gpu_sums(gs, cfg)
+            o, _, _, wd = oracle.render(dome_scene, cfg)
+            assert st == 0 and wd == 0
+            close = np.abs(g - o) <= 2e-3 * np.maximum(np.abs(g), np.abs(o)) + 1e-9
+            agree += int(close.sum())
+            total += close.size
+    frac = agree / total
+    print(f"three light samples, chain agreement kernel={kernel}: {frac:.4f} of {total}")
+    assert frac >= 0.95
+
+
 @pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
 @pytest.mark.parametrize("tracking", [_abi.TRACKING_RESIDUAL_CARRY, _abi.TRACKING_MERGED_LAYERS])
 def test_wavefront_matches_plain_chains(gpu, dome_scene, tracking, phase):
