@@ -54,14 +54,16 @@ def small_scene(data_dir):
     return synthetic_scene(wavelengths(400.0, 700.0, 8), data_dir, sun_elevation_deg=10.0)
 
 
-@pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
-def test_primal_traces_the_plain_chains(gpu, dome_scene, phase):
+@pytest.mark.parametrize("phase,lights", [(_abi.PHASE_ISOTROPIC, 1), (_abi.PHASE_TABULATED, 1),
+                                          (_abi.PHASE_TABULATED, 3)])
+def test_primal_traces_the_plain_chains(gpu, dome_scene, phase, lights):
     """One sample per cell: the adjoint primal (residual carry over the
     device-baked uniform layers) and the plain tracer (residual carry over the
     scene's grid) consume the same random numbers; their chains agree except
-    where float rounding flips a decision."""
+    where float rounding flips a decision (also with three sun samples per
+    vertex)."""
     cfg = RenderConfig(width=32, height=16, spp=1, sample_offset=3, phase_sampling=phase,
-                       tracking=_abi.TRACKING_RESIDUAL_CARRY)
+                       tracking=_abi.TRACKING_RESIDUAL_CARRY, direct_light_samples=lights)
     with GpuScene(dome_scene) as gs:
         want, _ = plain_sums(gs, dataclasses.replace(cfg, kernel=_abi.KERNEL_PLAIN))
         r = AdjointRenderer(gs, cfg)
