@@ -227,6 +227,16 @@ def test_oracle_tracking_modes_agree(data_dir, other):
     assert r["frac_beyond_3se"] <= 0.05 and abs(r["mean_z"]) < 1.0, r
 
 
+def test_oracle_light_sample_counts_agree(data_dir):
+    """direct_light_samples averages that many sun samples per vertex: the
+    expectation does not depend on the count."""
+    scene = synthetic_scene(wavelengths(400, 700, 4), data_dir, sun_elevation_deg=10.0)
+    base = dict(width=8, height=6, spp=256, phase_sampling=_abi.PHASE_TABULATED, max_orders=16,
+                tracking=_abi.TRACKING_MERGED_LAYERS)
+    r = _small_parity(scene, RenderConfig(**base), RenderConfig(**base, direct_light_samples=3, seed=5))
+    assert r["frac_beyond_3se"] <= 0.05 and abs(r["mean_z"]) < 1.0, r
+
+
 def test_oracle_phase_sampling_modes_agree(data_dir):
     scene = synthetic_scene(wavelengths(400, 700, 4), data_dir, sun_elevation_deg=10.0)
     base = dict(width=8, height=6, spp=256, max_orders=16)
