@@ -106,6 +106,14 @@ def make_config(w, args, rank: int):
                         kernel=args.kernel)
 
 
+def apply_tuning(gs, args):
+    """--tuning k=v,...: SkyTuning fields set on a scene the benchmark creates."""
+    if getattr(args, "tuning", None):
+        gs.set_tuning(**{k: (float(v) if k == "crossing_cost" else int(v))
+                         for k, v in (kv.split("=") for kv in args.tuning.split(","))})
+    return gs
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
 
@@ -260,7 +268,7 @@ def run_sweep(args):
                         tracking=args.tracking, rr_start_depth=8, output_projection=_abi.PROJECTION_SKY_VIEW_LUT)
     elevations = elevation_schedule(32, -6.0, 90.0)
     stream = torch.cuda.current_stream().cuda_stream
-    gs = GpuScene(scene)
+    gs = apply_tuning(GpuScene(scene), args)
     budgets, pilot_p95 = plan_budgets(gs, base, elevations, pilot_spp=16)
     sweep = Sweep(gs, RenderConfig(**{**base.__dict__, "seed": 0x5EC7_2026_0430}), elevations, budgets)
     sweep.capture()
@@ -401,7 +409,7 @@ def adjoint_report(args, steps, warmup, checks=True):
     theta_t[3 * L] *= np.float32(1.0 + rng.normal(0.0, 0.02))
     theta_t[3 * L + 1] += np.float32(rng.normal(0.0, 0.02))
     w = torch.as_tensor(np.asarray(scene.band_xyz, np.float64), device=dev)
-    gs = GpuScene(scene)
+    gs = apply_tuning(GpuScene(scene), args)
     r = AdjointRenderer(gs, cfg)
     th0 = t(theta0)
 
@@ -516,7 +524,8 @@ def adjoint_report(args, steps, warmup, checks=True):
     wnp = wcell.reshape(-1)
     plain = {}
     for name, (delta, proj) in dirs.items():
-        gp, gm = GpuScene(moved(name, delta)), GpuScene(moved(name, -delta))
+        gp = apply_tuning(GpuScene(moved(name, delta)), args)
+        gm = apply_tuning(GpuScene(moved(name, -delta)), args)
         fd, adj = [], []
         for k in range(batches):
             c = dataclasses.replace(cfg, spp=bspp, sample_offset=k * bspp)
@@ -633,10 +642,7 @@ def main():
     cells = cfg.pixels * B
     chains = cells * cfg.spp
 
-    gs = GpuScene(scene)
-    if args.tuning:
-        gs.set_tuning(**{k: (float(v) if k == "crossing_cost" else int(v))
-                         for k, v in (kv.split("=") for kv in args.tuning.split(","))})
+    gs = apply_tuning(GpuScene(scene), args)
     tuning_log = None
     if not args.no_autotune:
         from sky_cuda.autotune import DEFAULT_SPACE, autotune
