@@ -308,6 +308,19 @@ def _parse(v: str, path: Path) -> float:
         raise SceneError(f"{path}: cannot parse {v!r}") from e
 
 
+def _parse_index(v: str, path: Path, limit: int, what: str) -> int:
+    """A table index: a non-negative integer (the reference parses usize,
+    data.rs:123, :142-143) below `limit` (where the reference would index out of
+    bounds)."""
+    try:
+        i = int(v)
+    except ValueError as e:
+        raise SceneError(f"{path}: cannot parse {what} {v!r}") from e
+    if not 0 <= i < limit:
+        raise SceneError(f"{path}: {what} {i} out of range [0, {limit})")
+    return i
+
+
 def load_bands(path: Path) -> np.ndarray:
     rows = _csv_rows(path)
     out = np.zeros(len(rows), dtype=[("index", "<i4"), ("center_nm", "<f4"), ("lower_nm", "<f4"),
@@ -354,7 +367,7 @@ def load_aerosol_optics(path: Path, band_count: int) -> np.ndarray:
         if len(r) != 4:
             raise SceneError(f"{path}: expected 4 columns")
         s = _species_index(r[0])
-        b = int(r[1])
+        b = _parse_index(r[1], path, band_count, "band")
         out[b * SPECIES_COUNT + s] = (_parse(r[2], path), _parse(r[3], path))
         seen[b * SPECIES_COUNT + s] = True
     if not seen.all():
@@ -370,7 +383,9 @@ def load_mie_phase(path: Path, band_count: int, bins: int = PHASE_BINS) -> np.nd
     for r in _csv_rows(path):
         if len(r) != 4:
             raise SceneError(f"{path}: expected 4 columns")
-        s, b, k = _species_index(r[0]), int(r[1]), int(r[2])
+        s = _species_index(r[0])
+        b = _parse_index(r[1], path, band_count, "band")
+        k = _parse_index(r[2], path, bins, "bin")
         values[s, b, k] = _parse(r[3], path)
         seen[s, b, k] = True
     if not seen.all():
