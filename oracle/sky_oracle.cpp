@@ -1151,6 +1151,30 @@ float oracle_cpu_extinction(const SkySceneDesc* s, float altitude, uint32_t band
     return cpu_extinction_total(cpu_coefficients_at(s, altitude, band));
 }
 
+// Mean of the binary transmittance estimator (delta_transmittance,
+// sky_trace.wgsl:441-475) along one ray to its boundary (next_boundary; 0 when
+// the ray misses the top shell), over `n` independent random streams, in the
+// given tracking mode.  Returns -1 for an invalid scene.
+double oracle_transmittance(const SkySceneDesc* scene, uint32_t tracking, const float origin[3], const float dir[3],
+                            uint32_t band, uint32_t n) {
+    SkyRenderConfig cfg{};
+    cfg.width = cfg.height = cfg.spp = 1;
+    cfg.tracking = tracking;
+    Ctx c;
+    if (!make_ctx(scene, &cfg, c)) return -1.0;
+    const Ray ray{v3(origin[0], origin[1], origin[2]), normalize_or_y(v3(dir[0], dir[1], dir[2]))};
+    const BoundaryHit h = next_boundary(c, ray);
+    if (!h.hit) return 0.0;
+    Counters cnt;
+    double sum = 0.0;
+    for (uint32_t i = 0; i < n; ++i) {
+        Rng rng{i, 0x9E37u, band, 0u, 0x5EC7u, 0x2026u};
+        bool wd = false;
+        sum += double(delta_transmittance(c, ray, h.t, band, rng, wd, cnt));
+    }
+    return sum / double(n);
+}
+
 // The merged-layer grouping of tracking mode 2 for one band's majorants: writes
 // the first uniform layer of each group to starts_out[0..L) and returns the
 // number of groups.

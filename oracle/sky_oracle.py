@@ -54,6 +54,8 @@ def load():
     lib.oracle_cpu_extinction.restype = ctypes.c_float
     lib.oracle_merge_groups.argtypes = [fp, ctypes.c_uint32, ctypes.c_float, u32p]
     lib.oracle_merge_groups.restype = ctypes.c_uint32
+    lib.oracle_transmittance.argtypes = [vp, ctypes.c_uint32, fp, fp, ctypes.c_uint32, ctypes.c_uint32]
+    lib.oracle_transmittance.restype = ctypes.c_double
     _lib = lib
     return lib
 
@@ -159,6 +161,14 @@ def bake_majorant_grid(scene, layers: int):
     desc = scene.desc()
     lib.oracle_bake_majorant_grid(ctypes.byref(desc), layers, _f(maj), _f(mino))
     return maj.reshape(scene.band_count, layers), mino.reshape(scene.band_count, layers)
+
+
+def transmittance(scene, tracking: int, origin, direction, band: int, n: int) -> float:
+    """Mean of the binary transmittance estimator along one ray to its boundary."""
+    desc = scene.desc()
+    o = np.ascontiguousarray(origin, dtype=np.float32)
+    d = np.ascontiguousarray(direction, dtype=np.float32)
+    return float(load().oracle_transmittance(ctypes.byref(desc), tracking, _f(o), _f(d), band, n))
 
 
 def merge_groups(majorants, layer_dz: float) -> list[int]:

@@ -269,3 +269,26 @@ def test_merge_groups_is_optimal():
     # a uniform grid has no excess to pay for: one group; far-apart majorants in thick layers: none merge
     assert oracle.merge_groups(np.full(12, 0.02, np.float32), 1.0) == [0]
     assert oracle.merge_groups(np.array([1.0, 0.001, 1.0, 0.001], np.float32), 10.0) == [0, 1, 2, 3]
+
+
+@pytest.mark.parametrize("tracking", [_abi.TRACKING_SEGMENT_RESTART, _abi.TRACKING_RESIDUAL_CARRY,
+                                      _abi.TRACKING_MERGED_LAYERS])
+def test_oracle_transmittance_known_answer(ref_scene, tracking):
+    """The binary transmittance estimator (delta_transmittance,
+    sky_trace.wgsl:441-475) averages to exp(-optical depth) along rays through
+    the repository's medium, in every tracking mode: a vertical ray and a 5-degree
+    ray from 100 m, in the bluest and the reddest band."""
+    rg, rt, top = ref_scene.ground_radius_km, ref_scene.atmosphere_radius_km, ref_scene.top_altitude_km
+    z, _, _, ext = analytic.knot_tables(ref_scene)
+    o = np.array([0.0, rg + 0.1, 0.0])
+    n = 40000
+    for elev in (90.0, 5.0):
+        d = np.array([math.cos(math.radians(elev)), math.sin(math.radians(elev)), 0.0])
+        t_exit, _ = analytic._sphere_exit(o, d, rt)
+        t = np.linspace(0.0, float(t_exit), 40001)
+        alt = np.linalg.norm(o[None, :] + t[:, None] * d[None, :], axis=1) - rg
+        for band in (0, ref_scene.band_count - 1):
+            want = math.exp(-np.trapezoid(analytic._interp_alt(z, ext[band], alt, top), t))
+            got = oracle.transmittance(ref_scene, tracking, o, d, band, n)
+            se = math.sqrt(max(want * (1.0 - want), 1e-12) / n)
+            assert abs(got - want) <= 4.0 * se + 1e-3, (elev, band, got, want, se)
