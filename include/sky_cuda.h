@@ -183,7 +183,16 @@ typedef struct SkyRenderConfig {
     uint32_t kernel;                /* SkyKernel                               */
     uint32_t flags;                 /* SKY_FLAG_*                              */
     uint32_t tracking;              /* SkyTracking                             */
-    uint32_t _reserved[2];
+    /* Pixel-row slab: render only rows [row_begin, row_begin + row_count) of
+     * the width x height image (row_count 0 = every row; row_begin must then
+     * be 0).  Every output holds the slab only (width * row_count pixels,
+     * pixel-major from row row_begin).  Pixels keep their whole-image index
+     * in the random-number counter and the camera, so slabs rendered
+     * separately (on several GPUs) and concatenated equal the whole render.
+     * The reference splits its dispatch the same way, over (x, y, band)
+     * workgroups (integrator.rs:252-283). */
+    uint32_t row_begin;
+    uint32_t row_count;
 } SkyRenderConfig;
 
 /* Event counters, indexed by these values (the per-event work weights of
@@ -248,7 +257,11 @@ typedef struct SkyTuning {
     uint32_t _unused[2];         /* zero                                                         */
     float crossing_cost;         /* merged tracking grid: cost of a layer crossing relative to a
                                     null collision; <= 0 leaves the grid as it is              */
-    uint32_t _reserved[3];
+    uint32_t iteration_limit;    /* backstop of the wavefront kernel: loop iterations (one ray
+                                    per lane each) a warp may run before it stops and reports
+                                    SKY_ERR_WATCHDOG; 0 = 2^31.  A render needs about
+                                    3 x chains / (32 x resident warps) iterations per warp.    */
+    uint32_t _reserved[2];
 } SkyTuning;
 
 /* ---- Entry points ------------------------------------------------------ */
@@ -259,6 +272,34 @@ const char* sky_cuda_version(void);
 /* Copy the last error message of the calling thread into `buf` (always NUL
  * terminated); returns the status that produced it. */
 int sky_cuda_last_error(char* buf, size_t buf_len);
+
+/*
+ * Device allocations (cudaMalloc) the library has made in this process, on
+ * every device.  Diagnostic; no counterpart in the reference.  Every device
+ * allocation of the library goes through one routine, which counts it; when
+ * the environment variable SKY_CUDA_FAIL_DEVICE_ALLOC is set to a nonzero
+ * value that routine fails instead, as if the device were out of memory
+ * (the call returns SKY_ERR_OUT_OF_MEMORY), so that a host can test its
+ * handling of the reference's allocation failures without exhausting a GPU.
+ */
+uint64_t sky_cuda_device_allocations(void);
+
+/*
+ * Diagnostic: the tracer's own FP32 ray-shell geometry for caller rays.  The
+ * reference intersects a ray with a sphere in f32 as b^2 - c with
+ * c = (|o| - R)(|o| + R) (sky_trace.wgsl:211-221); the tracer evaluates the
+ * same roots as t = -b -+ sqrt((R - p)(R + p)) from the impact parameter
+ * p = |o x d|, and the altitude at t as sqrt(t (t + 2b) + |o|^2) - ground.
+ * For ray i (origins / directions: device float [ray_count][3], unit
+ * directions) and shell j (radii: device float [radius_count], km):
+ *   t_out  [(i * radius_count + j) * 2 + {0, 1}]  near and far crossing
+ *   alt_out[(i * radius_count + j) * 2 + {0, 1}]  altitude the tracker
+ *                                                 computes at that crossing
+ * NaN where the ray misses the shell.  Asynchronous on `cuda_stream`.
+ */
+int sky_cuda_probe_shell_geometry(const float* origins, const float* directions, uint32_t ray_count,
+                                  const float* radii, uint32_t radius_count, float ground_radius_km, float* t_out,
+                                  float* alt_out, void* cuda_stream);
 
 /* Validate a scene (integrator.rs:130-163, :401-407) and upload its tables to
  * the current CUDA device.  Replaces the buffer creation of
@@ -529,20 +570,27 @@ int sky_cuda_bake_mie_phase(const SkyMieDistribution* dist, const double* wavele
  * scene once at start-up, owns every output buffer, and renders through this
  * call, which calls no cudaMalloc, cudaFree or allocating library routine.
  *
- * job_configs[i] / outputs[i] describe job i exactly as in
- * sky_cuda_render_device(); every job must use the same tracking mode and
- * phase sampling.  outputs[0].status is required and receives the watchdog
- * bits of the whole batch (OR-ed in; the caller clears it); outputs[0].counters
- * receives the batch's event counts.  More than SKY_NOALLOC_MAX_JOBS jobs are
- * rejected with SKY_ERR_INVALID_CONFIG.
+ * job_configs[i] / outputs[i] describe job i as in sky_cuda_render_device(),
+ * except that this call always runs the wavefront kernel: a job whose
+ * `kernel` is SKY_KERNEL_PLAIN is rejected with SKY_ERR_INVALID_CONFIG.
+ * Every job must use the same tracking mode and phase sampling.
+ * outputs[0].status is required and receives the watchdog bits of the whole
+ * batch (OR-ed in; the caller clears it); outputs[0].counters receives the
+ * batch's event counts.  More than SKY_NOALLOC_MAX_JOBS jobs are rejected
+ * with SKY_ERR_INVALID_CONFIG.
  *
  * The kernel's job table and work counter live in one fixed scratch area of
  * the library (SKY_NOALLOC_SCRATCH_BYTES of device memory on every GPU that
- * loads it, held until the process exits).  The first call on a device looks
- * up that area's address (set-up once per device), so make it before any
- * stream capture.  All calls share the area and it keeps the last call's
- * contents: calls that overlap on the GPU (different streams without
- * ordering, or different host threads) race on it, so order them.
+ * loads it, held until the process exits).  The job table reaches that area
+ * through the argument of a small kernel launched on `cuda_stream`, not
+ * through a host-to-device copy, so the call neither waits for earlier work
+ * on the stream nor reads host memory once it has returned.  Each call looks
+ * up the area's address in the current CUDA context; the first call in a
+ * process may make the CUDA runtime load the library's device code (lazy
+ * module loading), so make it before any stream capture.  All calls share
+ * the area and it keeps the last call's contents: calls that overlap on the
+ * GPU (different streams without ordering, or different host threads) race
+ * on it, so order them.
  */
 #define SKY_NOALLOC_MAX_JOBS 16u
 #define SKY_NOALLOC_SCRATCH_BYTES 16384u

@@ -203,11 +203,13 @@ __device__ __forceinline__ void vertex_terms(AdjAcc& a, const AdjSet& X, uint32_
 // null-collision ratios of P over Q (kMayDiffer: P and Q may be distinct
 // sets; the ray loop has P = Q); with kNullTerms (the null-collision
 // estimator) and gw != 0 every null collision adds gw * d log(mu_bar - sigma_t).
+// At the 100000-segment guard a shadow ray (shadow = true) ends blocked and
+// any other ray without a collision, as in track_ray.
 template <bool kNullTerms, bool kMayDiffer = true>
 __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, const AdjSet& Q, uint32_t band,
                                           const RayGeo& g, float t_max, Rng& rng, float& t_hit, AdjBase& hit,
                                           float& w_eval, float& tau_bar, float gw, AdjAcc& acc, Counters& n,
-                                          bool& watchdog) {
+                                          bool& watchdog, bool shadow) {
     const DevScene& S = A.S;
     const uint32_t L = S.layer_count;
     MergedGrid G;
@@ -247,7 +249,7 @@ __device__ __forceinline__ bool adj_track(const AdjCtx& A, const AdjSet& P, cons
             if (dir == 0) return false;
             if (++guard > 100000u) {
                 watchdog = true;
-                return false;
+                return shadow;
             }
             tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
             t = t_seg;
@@ -346,7 +348,7 @@ __device__ __forceinline__ float adj_shadow(const AdjCtx& A, const AdjSet& P, co
     if (!(next_boundary(A.S, sg, st, sk) && sk == 1u)) return 0.0f;
     float th, w = 1.0f, tau_bar;
     AdjBase bh;
-    if (adj_track<false>(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog)) return 0.0f;
+    if (adj_track<false>(A, P, Q, band, sg, st, rng, th, bh, w, tau_bar, 0.0f, acc, n, watchdog, true)) return 0.0f;
     return w;
 }
 
@@ -382,7 +384,7 @@ __device__ __forceinline__ float adj_chain(const AdjCtx& A, const AdjSet& P, con
         float t_hit, w_eval = 1.0f, tau_bar;
         AdjBase hb;
         const bool hit =
-            adj_track<false>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, 0.0f, acc, n, watchdog);
+            adj_track<false>(A, P, Q, band, g, t_b, rng, t_hit, hb, w_eval, tau_bar, 0.0f, acc, n, watchdog, false);
         thr *= w_eval;
         if (hit) {
             ++n.e[SKY_EVENT_SCATTER];
@@ -508,8 +510,8 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
     const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
     const uint32_t band = uint32_t(cell % L.band_count);
-    const uint64_t pixel = cell / L.band_count;
-    const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
+    const uint64_t pixel = cell / L.band_count;  // pixel of the slab; y is the image row
+    const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width) + L.row_begin;
     const AdjSet P = resolve(A.P, A.S.layer_count, band);
     const AdjSet Q = A.distinct ? resolve(A.Q, A.S.layer_count, band) : P;
     Counters n;
@@ -635,8 +637,9 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                     claim_cell = cn;
                     const uint32_t pixel = cn / L.band_count;
                     claim_band = cn - pixel * L.band_count;
-                    claim_y = pixel / L.width;
-                    claim_x = pixel - claim_y * L.width;
+                    const uint32_t row = pixel / L.width;  // row within the slab
+                    claim_x = pixel - row * L.width;
+                    claim_y = row + L.row_begin;
                     claim_next = 0u;
                 }
                 const uint32_t rank = __popc(need & ((1u << lane) - 1u));
@@ -847,7 +850,7 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
             float t_hit = 0.0f, w_eval = 1.0f, tau_bar = 0.0f;
             AdjBase hit_b;
             const bool hit = adj_track<!kSegEst, false>(A, P, P, band, g, t_max, rng, t_hit, hit_b, w_eval, tau_bar,
-                                                        gw, acc, n, watchdog);
+                                                        gw, acc, n, watchdog, ray != kRayPrimary);
             if (grad && kSegEst) {
                 // the segment integral of the traced part: a primary segment
                 // from its first random number, an unblocked shadow ray from
@@ -1135,7 +1138,7 @@ cudaError_t launch_ray_loop(const AdjCtx& A, const DevLaunch& L, const float* dl
 cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                   bool accumulate, unsigned long long* counters, uint32_t* status,
                                   uint32_t* next_cell, cudaStream_t stream) {
-    const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;  // the slab's cells
     cudaError_t e;
     if (!A.distinct && cells <= 0xffffffffull) {
         // P = Q: the ray loop, adding into the cell sums
@@ -1180,7 +1183,7 @@ cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* c
 cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
                                 double* band_grad, unsigned long long* counters, uint32_t* status,
                                 uint32_t* next_cell, cudaStream_t stream) {
-    const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;  // the slab's cells
     if (cells > 0xffffffffull) return cudaErrorInvalidConfiguration;  // the cell counter is 32-bit
     cudaError_t e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;

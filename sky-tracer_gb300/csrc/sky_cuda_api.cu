@@ -11,7 +11,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cstddef>
-#include <mutex>
+#include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -82,6 +83,33 @@ int cuda_fail(int status, const char* what, cudaError_t e) {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Every device allocation of the library: counted (sky_cuda_device_allocations)
+// and, while SKY_CUDA_FAIL_DEVICE_ALLOC is set to a nonzero value, failed as
+// out of memory without touching the device.
+std::atomic<uint64_t> g_device_allocations{0};
+
+bool allocation_failure_injected() {
+    const char* v = std::getenv("SKY_CUDA_FAIL_DEVICE_ALLOC");
+    return v && *v && std::strcmp(v, "0") != 0;
+}
+
+template <class T>
+cudaError_t dev_malloc(T** ptr, size_t bytes) {
+    if (allocation_failure_injected()) {
+        *ptr = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) g_device_allocations.fetch_add(1, std::memory_order_relaxed);
+    *ptr = static_cast<T*>(p);
+    return e;
+}
+
+// Pixels of the rows a config renders (its slab, or the whole image).
+uint32_t slab_rows(const SkyRenderConfig* c) { return c->row_count ? c->row_count : c->height; }
+uint64_t slab_pixels(const SkyRenderConfig* c) { return uint64_t(c->width) * slab_rows(c); }
+
 void free_workspace(SkyScene* s) {
     cudaFree(s->ws_sum);
     cudaFree(s->ws_sumsq);
@@ -100,22 +128,37 @@ void free_workspace(SkyScene* s) {
     s->ws_cells = s->ws_pixels = 0;
 }
 
+// Grow the render workspace to `pixels`.  The new buffers are allocated
+// before the old ones are freed, so a failed allocation leaves the scene with
+// its old workspace: renders that fit it still run without allocating.
 int ensure_workspace(SkyScene* s, uint64_t pixels) {
     uint64_t cells = pixels * s->dev.band_count;
     if (cells <= s->ws_cells && pixels <= s->ws_pixels && s->ws_sum) return SKY_OK;
-    free_workspace(s);
+    SkyScene grown;
+    grown.dev = s->dev;
     cudaError_t e = cudaSuccess;
-    if ((e = cudaMalloc(&s->ws_sum, cells * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_sumsq, cells * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_film, cells * sizeof(float))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_xyz, pixels * 3 * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_xyz_var, pixels * 3 * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_rgb, pixels * 3 * sizeof(float))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_counters, SKY_EVENT_COUNT * sizeof(unsigned long long))) != cudaSuccess ||
-        (e = cudaMalloc(&s->ws_status, sizeof(uint32_t))) != cudaSuccess) {
-        free_workspace(s);
+    if ((e = dev_malloc(&grown.ws_sum, cells * sizeof(double))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_sumsq, cells * sizeof(double))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_film, cells * sizeof(float))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_xyz, pixels * 3 * sizeof(double))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_xyz_var, pixels * 3 * sizeof(double))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_rgb, pixels * 3 * sizeof(float))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_counters, SKY_EVENT_COUNT * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = dev_malloc(&grown.ws_status, sizeof(uint32_t))) != cudaSuccess) {
+        free_workspace(&grown);
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "workspace allocation", e);
     }
+    // the old buffers may still be read by work queued on the scene's stream
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    free_workspace(s);
+    s->ws_sum = grown.ws_sum;
+    s->ws_sumsq = grown.ws_sumsq;
+    s->ws_film = grown.ws_film;
+    s->ws_xyz = grown.ws_xyz;
+    s->ws_xyz_var = grown.ws_xyz_var;
+    s->ws_rgb = grown.ws_rgb;
+    s->ws_counters = grown.ws_counters;
+    s->ws_status = grown.ws_status;
     s->ws_cells = cells;
     s->ws_pixels = pixels;
     return SKY_OK;
@@ -127,6 +170,11 @@ int validate_config(const SkyScene* scene, const SkyRenderConfig* c) {
     if (!c) return set_error(SKY_ERR_INVALID_CONFIG, "render config is null");
     if (c->width == 0 || c->height == 0 || c->spp == 0)
         return set_error(SKY_ERR_INVALID_CONFIG, "width, height, and spp must be greater than zero");
+    if (c->row_count == 0 && c->row_begin != 0)
+        return set_error(SKY_ERR_INVALID_CONFIG, "row_begin needs a nonzero row_count");
+    if (uint64_t(c->row_begin) + c->row_count > c->height)
+        return set_error(SKY_ERR_INVALID_CONFIG, "rows [row_begin, row_begin + row_count) exceed the image height");
+    // the reference's own limit is on the whole image (integrator.rs:143-147)
     uint64_t cells = uint64_t(c->width) * c->height * scene->dev.band_count;
     if (cells > 0xffffffffull)
         return set_error(SKY_ERR_INVALID_CONFIG, "film is too large for the GPU shader index type");
@@ -157,6 +205,8 @@ DevLaunch make_launch(const SkyScene* s, const SkyRenderConfig* c) {
     DevLaunch L{};
     L.width = c->width;
     L.height = c->height;
+    L.row_begin = c->row_begin;
+    L.rows = slab_rows(c);
     L.spp = c->spp;
     L.sample_offset = c->sample_offset;
     L.band_count = s->dev.band_count;
@@ -229,6 +279,7 @@ WaveLaunch wave_launch(const SkyScene* s, const DevJob& first, const DevJob* dev
     w.work_counter = counter;
     w.counters = counters;
     w.status = status;
+    w.iteration_limit = s->tuning.iteration_limit;
     return w;
 }
 
@@ -241,7 +292,7 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
                   bool timed) {
     clear_stale_error();
     DevLaunch L = make_launch(s, c);
-    const uint64_t pixels = uint64_t(c->width) * c->height;
+    const uint64_t pixels = slab_pixels(c);
     cudaError_t e;
     const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
     const uint32_t total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
@@ -290,12 +341,12 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
     auto t0 = std::chrono::steady_clock::now();
     int st = validate_config(s, c);
     if (st) return st;
-    const uint64_t pixels = uint64_t(c->width) * c->height;
+    const uint64_t pixels = slab_pixels(c);
     const uint64_t cells = pixels * s->dev.band_count;
     if (film_out && film_len < cells)
-        return set_error(SKY_ERR_INVALID_CONFIG, "film buffer is smaller than width*height*bands");
+        return set_error(SKY_ERR_INVALID_CONFIG, "film buffer is smaller than width*rows*bands");
     if ((xyz_out || xyz_var_out || rgb_out) && pixel_count < pixels)
-        return set_error(SKY_ERR_INVALID_CONFIG, "xyz / rgb buffer is smaller than width*height");
+        return set_error(SKY_ERR_INVALID_CONFIG, "xyz / rgb buffer is smaller than width*rows");
     if ((xyz_out || xyz_var_out || rgb_out) && !s->has_xyz)
         return set_error(SKY_ERR_INVALID_CONFIG, "scene has no band_xyz_weights");
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
@@ -337,6 +388,7 @@ int render_host(SkyScene* s, const SkyRenderConfig* c, float* film_out, size_t f
         stats->kernel_used = c->kernel == SKY_KERNEL_PLAIN ? SKY_KERNEL_PLAIN : SKY_KERNEL_WAVEFRONT;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
+    if (status & 2u) return set_error(SKY_ERR_WATCHDOG, "the tracing kernel reached its iteration limit");
     if (status) return set_error(SKY_ERR_WATCHDOG, "GPU path watchdog was reached");
     return SKY_OK;
 }
@@ -361,7 +413,7 @@ int upload_tracking_grid(SkyScene* s, const HostTables& h) {
     std::memcpy(host.data() + o_tc, h.trk_count.data(), h.trk_count.size() * sizeof(uint32_t));
     std::memcpy(host.data() + o_to, h.trk_off.data(), h.trk_off.size() * sizeof(uint32_t));
     void* blob = nullptr;
-    cudaError_t e = cudaMalloc(&blob, off);
+    cudaError_t e = dev_malloc(&blob, off);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "tracking grid allocation", e);
     if ((e = cudaMemcpy(blob, host.data(), off, cudaMemcpyHostToDevice)) != cudaSuccess) {
         cudaFree(blob);
@@ -442,6 +494,23 @@ int sky_cuda_scene_get_tuning(const SkyScene* s, SkyTuning* t) {
 
 const char* sky_cuda_version(void) { return "sky_cuda 0.1.0 (abi 1, sm_103a)"; }
 
+uint64_t sky_cuda_device_allocations(void) { return g_device_allocations.load(std::memory_order_relaxed); }
+
+int sky_cuda_probe_shell_geometry(const float* origins, const float* directions, uint32_t ray_count,
+                                  const float* radii, uint32_t radius_count, float ground_radius_km, float* t_out,
+                                  float* alt_out, void* cuda_stream) {
+    if (!origins || !directions || !radii || !t_out || !alt_out)
+        return set_error(SKY_ERR_INVALID_CONFIG, "every buffer of the shell probe is required");
+    if (ray_count == 0 || radius_count == 0 || uint64_t(ray_count) * radius_count > (uint64_t(1) << 36))
+        return set_error(SKY_ERR_INVALID_CONFIG, "ray_count * radius_count must be in [1, 2^36]");
+    if (!std::isfinite(ground_radius_km)) return set_error(SKY_ERR_INVALID_CONFIG, "ground radius must be finite");
+    clear_stale_error();
+    const cudaError_t e = launch_shell_probe(origins, directions, ray_count, radii, radius_count, ground_radius_km,
+                                             t_out, alt_out, static_cast<cudaStream_t>(cuda_stream));
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "shell probe launch", e);
+    return SKY_OK;
+}
+
 int sky_cuda_last_error(char* buf, size_t buf_len) {
     if (buf && buf_len) {
         std::snprintf(buf, buf_len, "%s", g_error.c_str());
@@ -496,7 +565,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     put(o_pp, h.phase_bin_pdf.data(), h.phase_bin_pdf.size() * sizeof(float));
     put(o_pg, h.phase_guide.data(), h.phase_guide.size() * sizeof(uint16_t));
 
-    if ((e = cudaMalloc(&s->blob, off)) != cudaSuccess) {
+    if ((e = dev_malloc(&s->blob, off)) != cudaSuccess) {
         delete s;
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "scene table allocation", e);
     }
@@ -541,8 +610,8 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
             s->adjoint_unsupported = "differentiable renders need a scene whose only aerosol is species 0; species " +
                                      std::to_string(sp) + " has mass and optics";
     }
-    if ((e = cudaMalloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
-        (e = cudaMalloc(&s->work_counter, sizeof(uint32_t))) != cudaSuccess) {
+    if ((e = dev_malloc(&s->jobs, sizeof(DevJob))) != cudaSuccess ||
+        (e = dev_malloc(&s->work_counter, sizeof(uint32_t))) != cudaSuccess) {
         sky_cuda_scene_destroy(s);
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "job table allocation", e);
     }
@@ -675,7 +744,7 @@ int build_batch_jobs(SkyScene* s, const SkyBatchJob* jobs, uint32_t n, DevJob* o
         job.rgb = s->has_xyz ? jobs[i].outputs.rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
-        if ((st = place_job(job, uint64_t(c->width) * c->height, s->dev.band_count, cells, max_cells))) return st;
+        if ((st = place_job(job, slab_pixels(c), s->dev.band_count, cells, max_cells))) return st;
     }
     return SKY_OK;
 }
@@ -691,9 +760,9 @@ int ensure_batch_capacity(SkyScene* s, uint32_t n) {
     s->batch_counter = nullptr;
     s->batch_capacity = 0;
     cudaError_t e;
-    if ((e = cudaMalloc(&s->batch_jobs, size_t(n) * sizeof(DevJob))) != cudaSuccess ||
+    if ((e = dev_malloc(&s->batch_jobs, size_t(n) * sizeof(DevJob))) != cudaSuccess ||
         (e = cudaMallocHost(&s->batch_host, size_t(n) * sizeof(DevJob))) != cudaSuccess ||
-        (e = cudaMalloc(&s->batch_counter, sizeof(uint32_t))) != cudaSuccess)
+        (e = dev_malloc(&s->batch_counter, sizeof(uint32_t))) != cudaSuccess)
         return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch job table allocation", e);
     s->batch_capacity = n;
     return SKY_OK;
@@ -742,8 +811,8 @@ extern "C" int sky_cuda_batch_graph_create(const SkyScene* scene, const SkyBatch
     int st = SKY_OK;
     cudaStream_t cap = nullptr;
     if ((e = cudaMallocHost(&g->host, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
-        (e = cudaMalloc(&g->jobs, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
-        (e = cudaMalloc(&g->counter, sizeof(uint32_t))) != cudaSuccess) {
+        (e = dev_malloc(&g->jobs, size_t(std::max(job_count, 1u)) * sizeof(DevJob))) != cudaSuccess ||
+        (e = dev_malloc(&g->counter, sizeof(uint32_t))) != cudaSuccess) {
         st = cuda_fail(SKY_ERR_OUT_OF_MEMORY, "batch graph allocation", e);
     } else if ((st = build_batch_jobs(s, jobs, job_count, g->host, cells, max_cells)) == SKY_OK) {
         const WaveLaunch w = wave_launch(s, g->host[0], g->jobs, job_count, cells, max_cells,
@@ -809,7 +878,7 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
     const uint32_t B = s->dev.band_count, L = s->dev.layer_count, bins = s->dev.phase_bins;
     if (!s->adj_ws) {
-        cudaError_t e = cudaMalloc(&s->adj_ws, adjoint_workspace_bytes(B, L, bins));
+        cudaError_t e = dev_malloc(&s->adj_ws, adjoint_workspace_bytes(B, L, bins));
         if (e != cudaSuccess) {
             s->adj_ws = nullptr;
             return cuda_fail(SKY_ERR_OUT_OF_MEMORY, "differentiable-render workspace allocation", e);
@@ -859,7 +928,7 @@ int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& 
     int st = validate_config(s, c);
     if (st) return st;
     // the ray loop's 32-bit cell counter also counts one failed claim per warp
-    if (uint64_t(c->width) * c->height * s->dev.band_count > kMaxLaunchCells)
+    if (slab_pixels(c) * s->dev.band_count > kMaxLaunchCells)
         return set_error(SKY_ERR_INVALID_CONFIG, "a launch holds at most 4026531840 (pixel, band) cells");
     if (c->tracking != SKY_TRACKING_RESIDUAL_CARRY && c->tracking != SKY_TRACKING_MERGED_LAYERS)
         return set_error(SKY_ERR_INVALID_CONFIG,
@@ -893,7 +962,7 @@ extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderCo
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
     const bool accumulate = (config->flags & SKY_FLAG_ACCUMULATE) != 0;
     const uint32_t total_spp = accumulate ? config->sample_offset + config->spp : config->spp;
-    const uint64_t pixels = uint64_t(config->width) * config->height;
+    const uint64_t pixels = slab_pixels(config);
     clear_stale_error();
     cudaError_t e = launch_adjoint_prepare(A, W, stream);
     if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
@@ -973,7 +1042,7 @@ struct DeviceScratch {  // frees what it allocated when the call returns
     template <class T>
     cudaError_t alloc(T** out, size_t count) {
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+        cudaError_t e = dev_malloc(&p, std::max<size_t>(count, 1) * sizeof(T));
         if (e == cudaSuccess) ptrs.push_back(p);
         *out = static_cast<T*>(p);
         return e;
@@ -1200,28 +1269,27 @@ struct NoAllocScratch {
 };
 static_assert(sizeof(NoAllocScratch) <= SKY_NOALLOC_SCRATCH_BYTES, "scratch area too small");
 
+// The job rows of one call, handed to the install kernel by value: kernel
+// arguments may hold up to 32764 bytes on this architecture, so the rows
+// travel with the launch itself and no host buffer is read after the call.
+struct NoAllocTable {
+    DevJob jobs[SKY_NOALLOC_MAX_JOBS];
+    uint32_t words;  // 32-bit words of the rows in use
+};
+static_assert(sizeof(NoAllocTable) <= 32000, "job table exceeds the kernel-argument limit");
+static_assert(sizeof(DevJob) % 4 == 0, "job rows are copied as 32-bit words");
+
 // The job table and work counter of sky_cuda_render_batch_noalloc().  Host
-// code may not use this name as a device address: it is resolved per device
-// with cudaGetSymbolAddress() below.
+// code may not use this name as a device address: it is resolved with
+// cudaGetSymbolAddress() below.  Device code names it directly.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SKY_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_address[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch area on `device` (which must be current).
-int noalloc_scratch(int device, void** out) {
-    if (device < 0 || device >= kNoAllocMaxDevices)
-        return set_error(SKY_ERR_DEVICE_INIT, "device ordinal beyond the allocation-free scratch table");
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_address[device]) {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(SKY_ERR_DEVICE_INIT, "locating the allocation-free scratch area", e);
-        g_noalloc_address[device] = ptr;
-    }
-    *out = g_noalloc_address[device];
-    return SKY_OK;
+// Copy the call's job rows from the kernel argument into the scratch area,
+// ordered on the caller's stream before the tracing kernels that read them.
+__global__ void __launch_bounds__(256) noalloc_install_kernel(const __grid_constant__ NoAllocTable table) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(table.jobs);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(reinterpret_cast<NoAllocScratch*>(g_noalloc_scratch)->jobs);
+    for (uint32_t i = threadIdx.x; i < table.words; i += blockDim.x) dst[i] = src[i];
 }
 
 }  // namespace
@@ -1237,20 +1305,22 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
                                                      std::to_string(SKY_NOALLOC_MAX_JOBS) + ")");
     if (!outputs[0].status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[0].status is required");
     SkyScene* s = const_cast<SkyScene*>(scene);
-    NoAllocScratch image;
-    std::memset(&image, 0, sizeof(image));
+    NoAllocTable table;
+    std::memset(&table, 0, sizeof(table));
     uint64_t cells = 0;
     uint32_t max_cells = 0;
     for (uint32_t i = 0; i < job_count; ++i) {
         const SkyRenderConfig* c = &job_configs[i];
         int st = validate_config(s, c);
         if (st) return st;
+        if (c->kernel == SKY_KERNEL_PLAIN)
+            return set_error(SKY_ERR_INVALID_CONFIG,
+                             "the allocation-free render runs the wavefront kernel only; SKY_KERNEL_PLAIN was asked for");
         if (c->tracking != job_configs[0].tracking || c->phase_sampling != job_configs[0].phase_sampling)
             return set_error(SKY_ERR_INVALID_CONFIG, "all jobs of a batch need the same tracking and phase sampling");
         if (!outputs[i].cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs[i].cell_sum is required");
         const bool accumulate = (c->flags & SKY_FLAG_ACCUMULATE) != 0;
-        const uint64_t pixels = uint64_t(c->width) * c->height;
-        DevJob& job = image.jobs[i];
+        DevJob& job = table.jobs[i];
         job.S = s->dev;
         job.L = make_launch(s, c);
         job.cell_sum = outputs[i].cell_sum;
@@ -1261,20 +1331,23 @@ extern "C" int sky_cuda_render_batch_noalloc(const SkyScene* scene, const SkyRen
         job.rgb = s->has_xyz ? outputs[i].rgb : nullptr;
         job.accumulate = accumulate ? 1u : 0u;
         job.total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
-        if ((st = place_job(job, pixels, s->dev.band_count, cells, max_cells))) return st;
+        if ((st = place_job(job, slab_pixels(c), s->dev.band_count, cells, max_cells))) return st;
     }
+    table.words = uint32_t(job_count * sizeof(DevJob) / 4u);
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");
+    // The area's address in the current context, looked up on every call (a
+    // cached address would outlive a context reset).
     void* scratch = nullptr;
-    int st = noalloc_scratch(s->device, &scratch);
-    if (st) return st;
+    cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(SKY_ERR_DEVICE_INIT, "locating the allocation-free scratch area", e);
     cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
     clear_stale_error();
-    // the job table (the launch resets the work counter itself)
-    cudaError_t e = cudaMemcpyAsync(scratch, &image, sizeof(image), cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_COPY, "job table upload", e);
+    noalloc_install_kernel<<<1, 256, 0, stream>>>(table);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "job table install launch", e);
     uint32_t* counter = reinterpret_cast<uint32_t*>(static_cast<unsigned char*>(scratch) +
                                                     offsetof(NoAllocScratch, work_counter));
-    const WaveLaunch w = wave_launch(s, image.jobs[0], static_cast<const DevJob*>(scratch), job_count, cells,
+    // the launch resets the work counter itself
+    const WaveLaunch w = wave_launch(s, table.jobs[0], static_cast<const DevJob*>(scratch), job_count, cells,
                                      max_cells, job_configs[0].tracking, job_configs[0].phase_sampling, counter,
                                      outputs[0].counters, outputs[0].status);
     e = launch_trace_wave(w, stream);

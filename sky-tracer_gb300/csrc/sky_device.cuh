@@ -541,9 +541,14 @@ __device__ __forceinline__ V3 camera_dir(const DevLaunch& L, uint32_t x, uint32_
 // delta_transmittance, sky_trace.wgsl:405-475).  Returns true at a real
 // collision (t_hit set).  kTracking selects the reference's per-segment
 // restart or the residual carry (same distribution, fewer draws).
+// A ray that crosses more than 100000 segments sets the watchdog and ends as
+// the reference ends it: a camera or continuation ray (shadow = false)
+// without a collision (sky_trace.wgsl:412-415), a shadow ray (shadow = true)
+// as blocked, transmittance 0 (:448-451).
 // Residual-carry delta tracking over the band's merged tracking grid.
 __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo& g, float t_max, uint32_t band,
-                                                 Rng& rng, float& t_hit, Counters& n, bool& watchdog) {
+                                                 Rng& rng, float& t_hit, Counters& n, bool& watchdog,
+                                                 bool shadow) {
     const MergedGrid G = merged_grid(S, band);
     const float2* sig_row = S.sigma_t + band * S.knot_count;
     float t = 0.0f;
@@ -569,7 +574,7 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo
             if (dir == 0) return false;
             if (++guard > 100000u) {
                 watchdog = true;
-                return false;
+                return shadow;
             }
             tau = fmaxf(tau - (t_seg - t) * maj, 0.0f);
             t = t_seg;
@@ -583,8 +588,9 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo
 
 template <int kTracking>
 __device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, float t_max, uint32_t band, Rng& rng,
-                                          float& t_hit, Counters& n, bool& watchdog) {
-    if (kTracking == SKY_TRACKING_MERGED_LAYERS) return track_ray_merged(S, g, t_max, band, rng, t_hit, n, watchdog);
+                                          float& t_hit, Counters& n, bool& watchdog, bool shadow) {
+    if (kTracking == SKY_TRACKING_MERGED_LAYERS)
+        return track_ray_merged(S, g, t_max, band, rng, t_hit, n, watchdog, shadow);
     const float* maj_row = S.majorants + band * S.layer_count;
     const float2* sig_row = S.sigma_t + band * S.knot_count;
     float t = 0.0f;
@@ -595,7 +601,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, fl
         if (t >= t_max) return false;
         if (guard > 100000u) {
             watchdog = true;
-            return false;
+            return shadow;
         }
         ++guard;
         uint32_t layer;

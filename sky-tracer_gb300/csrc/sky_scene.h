@@ -101,6 +101,8 @@ struct DevScene {
 // Per-launch constants.
 struct DevLaunch {
     uint32_t width, height, spp, sample_offset;
+    uint32_t row_begin;       // first image row of the rendered slab
+    uint32_t rows;            // rows of the slab (height when the whole image is rendered)
     uint32_t band_count;
     uint32_t direct_light_samples;
     uint32_t projection;

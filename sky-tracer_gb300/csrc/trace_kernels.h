@@ -34,6 +34,7 @@ struct WaveLaunch {
     uint32_t* work_counter;        // reset by the launch itself
     unsigned long long* counters;  // may be null
     uint32_t* status;
+    uint64_t iteration_limit;      // loop iterations per warp before status bit 2 (SkyTuning.iteration_limit)
 };
 
 // Prepare, trace and finalize every job of `w` (three kernels on `stream`):
@@ -55,6 +56,12 @@ cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_s
 // concatenated pixels; jobs without film / XYZ / RGB outputs are skipped).
 cudaError_t launch_finalize_jobs(const DevScene& S, const DevJob* jobs, uint32_t num_jobs, uint32_t total_cells,
                                  cudaStream_t stream);
+
+// The tracer's FP32 shell crossings and altitudes for caller rays (probe.cu):
+// t_out / alt_out [ray][shell][near, far], NaN where a ray misses a shell.
+cudaError_t launch_shell_probe(const float* origins, const float* directions, uint32_t rays, const float* radii,
+                               uint32_t shells, float ground_radius, float* t_out, float* alt_out,
+                               cudaStream_t stream);
 
 // XYZ -> white-balanced linear sRGB of a scene (kernel argument copy).
 struct RgbMatrix {

@@ -27,7 +27,7 @@ __device__ __forceinline__ float shadow_transmittance(const DevScene& S, V3 pos,
     ++n.e[SKY_EVENT_BOUNDARY];
     if (!next_boundary(S, sg, t_b, kind) || kind != 1u) return -1.0f;  // no sun visible: no contribution
     float t_hit;
-    return track_ray<kTracking>(S, sg, t_b, band, rng, t_hit, n, watchdog) ? 0.0f : 1.0f;
+    return track_ray<kTracking>(S, sg, t_b, band, rng, t_hit, n, watchdog, true) ? 0.0f : 1.0f;
 }
 
 // trace_path (sky_trace.wgsl:703-776) for one chain.
@@ -55,7 +55,7 @@ __device__ float trace_chain(const DevScene& S, const DevLaunch& L, uint32_t x, 
         ++n.e[SKY_EVENT_BOUNDARY];
         if (!next_boundary(S, g, t_b, kind)) break;
         float t_hit;
-        if (track_ray<kTracking>(S, g, t_b, band, rng, t_hit, n, watchdog)) {
+        if (track_ray<kTracking>(S, g, t_b, band, rng, t_hit, n, watchdog, false)) {
             ++n.e[SKY_EVENT_SCATTER];
             V3 pos = madd(org, dir, t_hit);
             Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, altitude_at(g, t_hit, S.ground_radius));
@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch 
     const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
     const uint32_t band = uint32_t(cell % L.band_count);
-    const uint64_t pixel = cell / L.band_count;
-    const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width);
+    const uint64_t pixel = cell / L.band_count;  // pixel of the slab; y is the image row
+    const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width) + L.row_begin;
     Counters n;
     n.clear();
     bool watchdog = false;
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch 
 cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                unsigned long long* counters, uint32_t* status, bool accumulate,
                                cudaStream_t stream) {
-    const uint64_t cells = uint64_t(L.width) * L.height * L.band_count;
+    const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;
     const uint32_t block = 256;
     const uint64_t blocks = (cells * 32u + block - 1) / block;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;

@@ -42,9 +42,9 @@ namespace wave {
 
 constexpr uint32_t kFull = 0xffffffffu;
 constexpr uint32_t kNoCell = 0xffffffffu;
-// Backstop on the loop iterations of one warp (one ray per lane each); a
-// render needs ~3 rays per chain / lanes in flight.  Beyond it the warp sets
-// status bit 2 and returns.
+// Default backstop on the loop iterations of one warp (one ray per lane
+// each; SkyTuning.iteration_limit overrides it); a render needs ~3 rays per
+// chain / lanes in flight.  Beyond it the warp sets status bit 2 and returns.
 constexpr uint64_t kMaxIterations = 1ull << 31;
 
 // What a lane does next.
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     wave_kernel(const __grid_constant__ DevScene S, const __grid_constant__ DevLaunch L0,
                 const DevJob* __restrict__ jobs, uint32_t num_jobs,
                 uint32_t total_cells, uint32_t* __restrict__ work_counter, unsigned long long* __restrict__ counters,
-                uint32_t* __restrict__ status) {
+                uint32_t* __restrict__ status, uint64_t iteration_limit) {
     const uint32_t lane = threadIdx.x & 31u;
     Counters n;
     n.clear();
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     double acc_sum = 0.0, acc_sq = 0.0;
 
     for (uint64_t iter = 0;; ++iter) {
-        if (iter >= kMaxIterations) {  // warp-uniform
+        if (iter >= iteration_limit) {  // warp-uniform
             if (lane == 0u) atomicOr(status, 2u);
             break;
         }
@@ -142,8 +142,9 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 const uint32_t c = gc - __ldg(&jobs[claim_job].cell_begin);
                 const uint32_t pixel = c / S.band_count, width = __ldg(&jobs[claim_job].L.width);
                 claim_band = c - pixel * S.band_count;
-                claim_y = pixel / width;
-                claim_x = pixel - claim_y * width;
+                const uint32_t row = pixel / width;  // row within the job's slab
+                claim_x = pixel - row * width;
+                claim_y = row + __ldg(&jobs[claim_job].L.row_begin);
                 claim_spp = __ldg(&jobs[claim_job].L.spp);
                 claim_next = 0u;
             }
@@ -164,8 +165,9 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         if (next != kIdle && next != kTrace) {
             const DevLaunch& JL = job_launch<kSingle>(L0, jobs, job);
             if (next == kStart) {
+                // the image pixel drives the random stream, the slab pixel indexes the sums
                 const uint32_t pixel = py * JL.width + px;
-                const uint32_t cell = pixel * S.band_count + band;
+                const uint32_t cell = ((py - JL.row_begin) * JL.width + px) * S.band_count + band;
                 if (cell != acc_cell || job != acc_job) {
                     if (acc_cell != kNoCell) {
                         const DevJob& A = jobs[acc_job];
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         }
         if (tracing) {
             float t_hit = 0.0f;
-            const bool hit = track_ray<kTracking>(S, g, t_max, band, rng, t_hit, n, watchdog);
+            const bool hit = track_ray<kTracking>(S, g, t_max, band, rng, t_hit, n, watchdog, shadow_ray);
             // the medium coefficients at a real collision (albedo) and at the vertex of
             // an unblocked shadow ray (phase of its NEE term): one call for both kinds
             const bool lit = shadow_ray && !hit;
@@ -378,7 +380,8 @@ cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
     const uint64_t want = (uint64_t(w.total_cells) * 32u + kWaveThreads - 1u) / kWaveThreads;
     const uint32_t blocks = uint32_t(std::max<uint64_t>(1u, std::min<uint64_t>(uint64_t(per_sm) * sms, want)));
     wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount><<<blocks, kWaveThreads, 0, stream>>>(
-        w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status);
+        w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status,
+        w.iteration_limit ? w.iteration_limit : kMaxIterations);
     return cudaGetLastError();
 }
 

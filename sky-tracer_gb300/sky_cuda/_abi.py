@@ -86,7 +86,7 @@ class SkyRenderConfig(ctypes.Structure):
         ("output_projection", _u32),
         ("sample_offset", _u32), ("phase_sampling", _u32), ("rr_start_depth", _u32),
         ("max_orders", _u32), ("watchdog_limit", _u32), ("kernel", _u32), ("flags", _u32),
-        ("tracking", _u32), ("_reserved", _u32 * 2),
+        ("tracking", _u32), ("row_begin", _u32), ("row_count", _u32),
     ]
 
 
@@ -107,7 +107,7 @@ class SkyDeviceOutputs(ctypes.Structure):
 class SkyTuning(ctypes.Structure):
     _fields_ = [
         ("variant", _u32), ("max_blocks_per_sm", _u32), ("_unused", _u32 * 2),
-        ("crossing_cost", _f), ("_reserved", _u32 * 3),
+        ("crossing_cost", _f), ("iteration_limit", _u32), ("_reserved", _u32 * 2),
     ]
 
 
@@ -156,6 +156,9 @@ assert ctypes.sizeof(SkyRenderStats) == 96
 _SIGNATURES = {
     "sky_cuda_version": (ctypes.c_char_p, []),
     "sky_cuda_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    "sky_cuda_device_allocations": (ctypes.c_uint64, []),
+    "sky_cuda_probe_shell_geometry": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_float,
+                                                     _vp, _vp, _vp]),
     "sky_cuda_scene_create": (ctypes.c_int, [ctypes.POINTER(SkySceneDesc), ctypes.POINTER(_vp)]),
     "sky_cuda_scene_destroy": (None, [_vp]),
     "sky_cuda_scene_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(SkyTuning)]),

@@ -58,6 +58,28 @@ def param_names(layers: int) -> list[str]:
     return names + ["mie_albedo", "mie_g"]
 
 
+def fd_check_parameters(grad, layers: int, count: int = 16, seed: int = 4, floor: float = 1e-4) -> list[int]:
+    """Indices of `count` parameters for a finite-difference check of a
+    gradient: the Mie albedo and g always, the others drawn with `seed`
+    evenly from the Rayleigh, Mie and ozone layer scales whose gradient is
+    at least `floor` times the largest (a layer without the species, such as
+    ozone outside its tent, has a zero gradient and checks nothing)."""
+    g = np.abs(np.asarray(grad, dtype=np.float64))
+    top = float(g.max()) if g.size else 0.0
+    rng = np.random.default_rng(seed)
+    picked = [PARAMS_PER_LAYER * layers, PARAMS_PER_LAYER * layers + 1]
+    pools = [[PARAMS_PER_LAYER * l + k for l in range(layers) if g[PARAMS_PER_LAYER * l + k] >= floor * top]
+             for k in range(PARAMS_PER_LAYER)]
+    want = count - len(picked)
+    for k, pool in enumerate(pools):
+        n = min(len(pool), want // PARAMS_PER_LAYER + (1 if k < want % PARAMS_PER_LAYER else 0))
+        picked += [int(i) for i in rng.choice(pool, n, replace=False)] if n else []
+    spare = [i for pool in pools for i in pool if i not in picked]
+    if len(picked) < count and spare:
+        picked += [int(i) for i in rng.choice(spare, min(count - len(picked), len(spare)), replace=False)]
+    return sorted(picked)
+
+
 def _ptr(t) -> int | None:
     return None if t is None else t.data_ptr()
 
@@ -191,7 +213,7 @@ def _autograd_function():
             ctx.has_band = band is not None
             ctx.save_for_backward(layer_c, band_c if band_c is not None else layer_c)
             cfg = renderer.config
-            return out["film"].reshape(cfg.height, cfg.width, renderer.bands)
+            return out["film"].reshape(cfg.rows, cfg.width, renderer.bands)
 
         @staticmethod
         def backward(ctx, grad_film):

@@ -161,6 +161,12 @@ class PrimaryFitConfig:
     # sky-view LUT columns nearest the sun's azimuth, which hold the sun disc:
     # its rare hits would dominate every squared error, so they are left out
     sun_columns: int = 2
+    # primaries closer than this are pushed apart by a penalty added to the loss:
+    # the reference searches combinations of distinct bands of its 10-nm grid
+    # (sky-wavelength-optimizer/src/main.rs:1121-1137), and an XYZ loss alone
+    # is met by two pairs of coincident bands on smooth sky spectra
+    min_spacing_nm: float = 10.0
+    spacing_weight: float = 1e-3
 
     @property
     def elevations(self) -> np.ndarray:
@@ -229,6 +235,17 @@ def _loss(xyz_hat, target, keep):
     return (keep * (xyz_hat - target) ** 2).sum() / (keep * target ** 2).sum()
 
 
+def spacing_penalty(lam, cfg: PrimaryFitConfig):
+    """spacing_weight * sum over pairs of (max(0, min_spacing - |lambda_k - lambda_l|) / min_spacing)^2."""
+    import torch
+    if cfg.min_spacing_nm <= 0.0 or cfg.spacing_weight <= 0.0:
+        return lam.sum() * 0.0
+    d = (lam[:, None] - lam[None, :]).abs()
+    iu = torch.triu_indices(len(lam), len(lam), offset=1, device=lam.device)
+    gap = torch.relu(cfg.min_spacing_nm - d[iu[0], iu[1]]) / cfg.min_spacing_nm
+    return cfg.spacing_weight * (gap * gap).sum()
+
+
 def _initial_matrix(films, target, keep):
     """Least-squares K x 3 matrix of the initial primaries."""
     import torch
@@ -261,6 +278,10 @@ def evaluate(cfg: PrimaryFitConfig, lam_nm, matrix, target, target_var=None, spp
     out["relative_rms_error"] = float(math.sqrt(float(d2 / t2)))
     out["relative_rms_error_debiased"] = float(math.sqrt(max(float((d2 - noise) / t2), 0.0)))
     out["relative_rms_noise"] = float(math.sqrt(float(noise / t2)))
+    # the smallest relative RMS error the debiased figure resolves (one standard deviation
+    # of the noise-subtracted squared error, for a reconstruction without error)
+    noise_el = keep * (var @ (m * m)) + (keep * target_var if target_var is not None else 0.0)
+    out["relative_rms_resolution"] = float(math.sqrt(math.sqrt(2.0 * float((noise_el ** 2).sum())) / float(t2)))
     return out
 
 
@@ -294,7 +315,7 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
         k = model.multipliers(lam)
         films = torch.stack([render_film(r, layer, k, sun=s, decorrelate=True).reshape(-1, scene.band_count)
                              for s in suns])
-        loss = _loss(films.double() @ matrix, target, keep)
+        loss = _loss(films.double() @ matrix, target, keep) + spacing_penalty(lam, cfg)
         loss.backward()
         opt.step()
         with torch.no_grad():
@@ -343,6 +364,11 @@ def fit_finite_differences(cfg: PrimaryFitConfig, target, iterations=None, log_e
                     js.append(float(_loss(f @ matrix, target, keep)))
                 grad[kk] = (js[0] - js[1]) / (2 * h)
         lam.grad = torch.as_tensor(grad, dtype=torch.float64, device="cuda")
+        lam_p = lam.detach().clone().requires_grad_(True)
+        pen = spacing_penalty(lam_p, cfg)
+        pen.backward()
+        lam.grad += lam_p.grad
+        loss = loss.detach() + pen.detach()
         opt.step()
         with torch.no_grad():
             lam.clamp_(380.0, 780.0)

@@ -48,6 +48,9 @@ class RenderConfig:
     kernel: int = _abi.KERNEL_AUTO
     flags: int = 0
     tracking: int = _abi.TRACKING_SEGMENT_RESTART
+    # pixel-row slab [row_begin, row_begin + row_count); 0 rows = the whole image
+    row_begin: int = 0
+    row_count: int = 0
 
     def to_c(self) -> SkyRenderConfig:
         c = SkyRenderConfig()
@@ -58,8 +61,14 @@ class RenderConfig:
         return c
 
     @property
+    def rows(self) -> int:
+        """Image rows this config renders (its slab, or every row)."""
+        return self.row_count or self.height
+
+    @property
     def pixels(self) -> int:
-        return self.width * self.height
+        """Pixels of the outputs: the slab's (width * rows)."""
+        return self.width * self.rows
 
 
 @dataclass
@@ -138,7 +147,7 @@ class GpuScene:
         t = SkyTuning()
         check(self.lib.sky_cuda_scene_get_tuning(self.handle, ctypes.byref(t)), self.lib)
         return {"variant": t.variant, "max_blocks_per_sm": t.max_blocks_per_sm,
-                "crossing_cost": float(t.crossing_cost)}
+                "crossing_cost": float(t.crossing_cost), "iteration_limit": t.iteration_limit}
 
     def set_tuning(self, **kw) -> None:
         """Set launch-shape fields of SkyTuning (unnamed fields keep their value)."""
@@ -154,7 +163,7 @@ class GpuScene:
         stats = SkyRenderStats()
         check(self.lib.sky_cuda_render(self.handle, ctypes.byref(config.to_c()), _fptr(film), film.size,
                                        ctypes.byref(stats)), self.lib)
-        return Film(config.width, config.height, self.band_count, film), RenderStats.from_c(stats)
+        return Film(config.width, config.rows, self.band_count, film), RenderStats.from_c(stats)
 
     def render_xyz(self, config: RenderConfig, with_film: bool = True):
         """Film, per-pixel XYZ [pixels, 3] (FP64) and its variance, and stats."""
@@ -166,7 +175,7 @@ class GpuScene:
                                            _fptr(film) if film is not None else None,
                                            film.size if film is not None else 0, _dptr(xyz), _dptr(var),
                                            config.pixels, ctypes.byref(stats)), self.lib)
-        f = Film(config.width, config.height, self.band_count, film) if film is not None else None
+        f = Film(config.width, config.rows, self.band_count, film) if film is not None else None
         return f, xyz, var, RenderStats.from_c(stats)
 
     def render_rgb(self, config: RenderConfig, with_film: bool = True):
@@ -179,7 +188,7 @@ class GpuScene:
                                            _fptr(film) if film is not None else None,
                                            film.size if film is not None else 0, _fptr(rgb), config.pixels,
                                            ctypes.byref(stats)), self.lib)
-        f = Film(config.width, config.height, self.band_count, film) if film is not None else None
+        f = Film(config.width, config.rows, self.band_count, film) if film is not None else None
         return f, rgb, RenderStats.from_c(stats)
 
     def render_batch(self, jobs, stream: int = 0) -> None:
@@ -252,4 +261,4 @@ def render(scene: Scene, config: RenderConfig) -> Film:
     film = np.empty(config.pixels * scene.band_count, dtype=np.float32)
     check(lib.sky_cuda_render_desc(ctypes.byref(desc), ctypes.byref(config.to_c()), _fptr(film), film.size,
                                    None), lib)
-    return Film(config.width, config.height, scene.band_count, film)
+    return Film(config.width, config.rows, scene.band_count, film)

@@ -52,7 +52,16 @@ def parity_report(xyz_a, var_a, xyz_b, var_b, bright_fraction=1e-3):
     rel = np.abs(xyz_a[keep] - xyz_b[keep]) / np.maximum(np.abs(xyz_b[keep]), 1e-30)
     mean_rel = float(np.abs(xyz_a[keep] - xyz_b[keep]).sum() / np.abs(xyz_b[keep]).sum())
     bias, bias_se = relative_bias(xyz_a, var_a, xyz_b, var_b)
+    # per pixel: mean over regular bright pixels and X, Y, Z of |a - b| / |b|,
+    # and the value pure noise would give (E|N(0, s)| = 0.8 s per component)
+    reg = keep & regular_pixels(xyz_a, var_a) & regular_pixels(xyz_b, var_b)
+    rel_pp = np.abs(xyz_a[reg] - xyz_b[reg]) / np.maximum(np.abs(xyz_b[reg]), 1e-30)
+    noise_pp = np.sqrt(2.0 / np.pi) * np.sqrt(np.maximum(var_a[reg] + var_b[reg], 0.0)) / \
+        np.maximum(np.abs(xyz_b[reg]), 1e-30)
     return {
+        "mean_rel_err_per_pixel": float(rel_pp.mean()) if rel_pp.size else 0.0,
+        "noise_rel_err_per_pixel": float(noise_pp.mean()) if noise_pp.size else 0.0,
+        "regular_pixels": int(reg.sum()),
         "bias_xyz": [float(v) for v in bias],
         "bias_se_xyz": [float(v) for v in bias_se],
         "pixels": int(keep.sum()),

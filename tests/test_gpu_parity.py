@@ -151,20 +151,24 @@ def test_statistical_parity_dome(gpu, dome_scene, tracking, phase):
         assert abs(b) < 0.005 + 3 * se
 
 
-def test_high_spp_mean_relative_error(gpu, data_dir):
-    """Matched high sample counts: mean relative XYZ error under 0.5 %."""
-    scene = synthetic_scene(wavelengths(400, 700, 8), data_dir, sun_elevation_deg=10.0)
-    cfg = RenderConfig(width=64, height=32, spp=4096, phase_sampling=_abi.PHASE_TABULATED,
+def test_high_spp_mean_relative_error(gpu, dome_scene):
+    """The CPU-runnable scene and settings (32 bands, sun 10 deg, at most 16
+    orders) on an 8x4 view at matched high sample counts (GPU 2^20, oracle
+    2^16 per pixel and band): per-pixel mean relative XYZ error under 0.5 %,
+    and the image-summed bias under 0.5 %."""
+    cfg = RenderConfig(width=8, height=4, spp=1 << 20, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS, max_orders=16)
-    with GpuScene(scene) as gs:
+    cfg_o = RenderConfig(**{**cfg.__dict__, "spp": 1 << 16, "seed": 4242})
+    with GpuScene(dome_scene) as gs:
         gs_, gq, _, _ = gpu_sums(gs, cfg)
-    os_, oq, _, _ = oracle.render(scene, RenderConfig(**{**cfg.__dict__, "seed": 4242}))
-    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, scene.band_xyz)
-    xo, vo = xyz_from_sums(os_, oq, cfg.spp, scene.band_xyz)
+    os_, oq, _, _ = oracle.render(dome_scene, cfg_o)
+    xg, vg = xyz_from_sums(gs_, gq, cfg.spp, dome_scene.band_xyz)
+    xo, vo = xyz_from_sums(os_, oq, cfg_o.spp, dome_scene.band_xyz)
     r = parity_report(xg, vg, xo, vo)
     print("high-spp parity", r)
-    assert r["frac_beyond_3se"] <= 0.02
-    # mean relative error of the image under 0.5 % (sun-disc pixels excluded)
+    assert r["frac_beyond_3se"] <= 0.05
+    assert r["noise_rel_err_per_pixel"] < 0.003
+    assert r["mean_rel_err_per_pixel"] < 0.005
     assert max(abs(b) for b in r["bias_xyz"]) < 0.005
 
 

@@ -1,9 +1,18 @@
-"""World-size-2 gloo ranks on CPU: sharding of sweep jobs across ranks, the
-max-over-ranks timing reduction and the gather of per-rank results."""
+"""World-size-2 gloo ranks on CPU: one render split into pixel-row slabs
+(SkyRenderConfig.row_begin / row_count), gathered to rank 0 and joined there,
+equals the whole render; a sweep splits into contiguous blocks of whole
+elevations; the max-over-ranks timing reduction.
+
+The renderer of each rank is a stand-in that needs no GPU: a fake renderer
+whose value is a function of the image pixel, and the oracle (test
+infrastructure) rendering the slab's rows.  Both index pixels the way the
+tracer does (image pixel in the random stream, slab pixel in the output), so
+a wrong slab offset shows up as a mismatch."""
 
 import os
 import socket
 
+import numpy as np
 import pytest
 
 
@@ -13,24 +22,64 @@ def _free_port():
         return s.getsockname()[1]
 
 
+def fake_slab(cfg, bands):
+    """[slab pixels, bands]: a hash of (image pixel, band), like a render whose
+    random stream is keyed by the image pixel."""
+    rows = cfg.row_count or cfg.height
+    y = np.arange(cfg.row_begin, cfg.row_begin + rows)[:, None]
+    x = np.arange(cfg.width)[None, :]
+    pixel = (y * cfg.width + x).reshape(-1, 1).astype(np.uint64)
+    band = np.arange(bands, dtype=np.uint64)[None, :]
+    h = (pixel * np.uint64(2654435761) + band * np.uint64(40503) + np.uint64(cfg.seed)) % np.uint64(1000003)
+    return h.astype(np.float64)
+
+
+def oracle_slab(scene, cfg):
+    """The oracle's per-cell sums of the slab's rows ([slab pixels, bands])."""
+    import sky_oracle
+    from dataclasses import replace
+    whole = replace(cfg, row_begin=0, row_count=0)
+    s, _, _, _ = sky_oracle.render(scene, whole, row_begin=cfg.row_begin, row_step=1, threads=1)
+    rows = cfg.row_count or cfg.height
+    return s[cfg.row_begin * cfg.width:(cfg.row_begin + rows) * cfg.width]
+
+
+def _scene_and_config():
+    from sky_cuda import RenderConfig, synthetic_scene, wavelengths
+    from sky_cuda import _abi
+    data = os.path.join(os.path.dirname(__file__), "golden", "data")
+    scene = synthetic_scene(wavelengths(380.0, 780.0, 4), data, sun_elevation_deg=10.0)
+    cfg = RenderConfig(width=6, height=5, spp=4, seed=21, max_orders=4, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    return scene, cfg
+
+
 def _worker(rank, world, port, q):
     import sys
-    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "sky-tracer_gb300"))
+    here = os.path.dirname(os.path.abspath(__file__))
+    for p in (os.path.join(here, "..", "sky-tracer_gb300"), os.path.join(here, "..", "oracle"), here):
+        sys.path.insert(0, p)
     import torch.distributed as dist
-    from sky_cuda.parallel import gather_to_rank0, max_over_ranks, shard
+    from sky_cuda.parallel import elevation_shard, gather_to_rank0, max_over_ranks, render_split
     from sky_cuda.sweep import elevation_schedule
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
-    mine = shard(list(elevation_schedule(32)), rank, world)
+    scene, cfg = _scene_and_config()
+    fake = render_split(lambda c: fake_slab(c, 3), cfg, rank, world, 3)
+    orc = render_split(lambda c: oracle_slab(scene, c), cfg, rank, world, scene.band_count)
+    elev = elevation_schedule(32)
+    mine = [float(elev[i]) for i in elevation_shard(len(elev), rank, world)]
+    sweep = gather_to_rank0(mine)
     t = max_over_ranks(1.0 + rank)
-    got = gather_to_rank0(mine)
     if rank == 0:
-        q.put((t, got))
+        q.put((t, fake, orc, sweep))
     dist.barrier()
     dist.destroy_process_group()
 
 
-def test_two_rank_sharding_and_timing():
+def test_two_rank_row_split_equals_whole_render():
+    import sky_oracle
     import torch.multiprocessing as mp
+    sky_oracle.load()  # built before the ranks start
     ctx = mp.get_context("spawn")
     q = ctx.SimpleQueue()
     port = _free_port()
@@ -38,18 +87,34 @@ def test_two_rank_sharding_and_timing():
     for p in procs:
         p.start()
     for p in procs:
-        p.join(timeout=120)
+        p.join(timeout=180)
         assert p.exitcode == 0
-    t, got = q.get()
+    t, fake, orc, sweep = q.get()
     assert t == 2.0
+    scene, cfg = _scene_and_config()
+    np.testing.assert_array_equal(fake, fake_slab(cfg, 3))
+    whole, _, _, _ = sky_oracle.render(scene, cfg, threads=1)
+    np.testing.assert_array_equal(orc, whole)
+    assert orc.shape == (cfg.pixels, scene.band_count) and np.any(orc > 0)
+    # whole elevations, contiguous blocks in rank order, covering the sweep once
     from sky_cuda.sweep import elevation_schedule
-    flat = sorted(x for part in got for x in part)
-    assert flat == sorted(elevation_schedule(32))
-    assert not set(got[0]) & set(got[1])
+    assert [e for part in sweep for e in part] == [float(e) for e in elevation_schedule(32)]
 
 
-def test_shard_rejects_bad_ranks():
-    from sky_cuda.parallel import shard
-    assert shard(range(5), 1, 2) == [1, 3]
+def test_row_slabs_partition_the_image():
+    from sky_cuda import RenderConfig
+    from sky_cuda.parallel import elevation_shard, row_slabs, slab_config
+    for height, world in [(256, 8), (256, 3), (5, 5), (7, 2), (1, 1)]:
+        slabs = row_slabs(height, world)
+        assert len(slabs) == world and slabs[0][0] == 0
+        assert all(b1 == b0 + n0 for (b0, n0), (b1, _) in zip(slabs, slabs[1:]))
+        assert sum(n for _, n in slabs) == height and max(n for _, n in slabs) - min(n for _, n in slabs) <= 1
     with pytest.raises(ValueError):
-        shard(range(5), 2, 2)
+        row_slabs(3, 4)
+    cfg = slab_config(RenderConfig(width=4, height=10, spp=1), 2, 3)
+    assert (cfg.row_begin, cfg.row_count, cfg.pixels) == (7, 3, 12)
+    with pytest.raises(ValueError):
+        slab_config(cfg, 0, 2)  # already a slab
+    assert [list(elevation_shard(5, r, 2)) for r in range(2)] == [[0, 1, 2], [3, 4]]
+    with pytest.raises(ValueError):
+        elevation_shard(5, 2, 2)

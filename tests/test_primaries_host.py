@@ -56,3 +56,20 @@ def test_oklab_score_of_identity_is_zero():
     assert s["rmse"] == 0.0 and s["score"] == 0.0
     s = oklab_score(xyz * 1.1, xyz)
     assert s["rmse"] > 0 and s["score"] == pytest.approx(s["rmse"] + 0.25 * s["p95"])
+
+
+def test_spacing_penalty_pushes_close_primaries_apart():
+    from sky_cuda.primaries import PrimaryFitConfig, spacing_penalty
+    cfg = PrimaryFitConfig()
+    far = torch.tensor([450.0, 520.0, 570.0, 630.0], dtype=torch.float64)
+    assert float(spacing_penalty(far, cfg)) == 0.0
+    # two pairs 1 nm apart (what the unconstrained fit converged to): each pair costs (9/10)^2
+    lam = torch.tensor([479.0, 480.0, 579.0, 580.0], dtype=torch.float64, requires_grad=True)
+    pen = spacing_penalty(lam, cfg)
+    assert float(pen) == pytest.approx(cfg.spacing_weight * 2 * 0.81)
+    pen.backward()
+    g = lam.grad.numpy()
+    # descending the penalty separates each pair
+    assert g[0] > 0 > g[1] and g[2] > 0 > g[3]
+    off = PrimaryFitConfig(min_spacing_nm=0.0)
+    assert float(spacing_penalty(lam.detach(), off)) == 0.0

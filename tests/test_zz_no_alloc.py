@@ -8,7 +8,10 @@ persistent tracer while keeping the kernel's job table and work counter in a
 fixed scratch area of the library instead of in allocated memory.  These
 tests check it against the ordinary device-output entry point,
 sky_cuda_render_device(), on two calls in a row (the scratch area is reused
-by every call), and that an oversized batch is refused.
+by every call); that the second, warmed call allocates nothing (the
+library's own count of device allocations and the GPU's free memory are
+unchanged across it); and that an oversized batch and a request for the
+plain kernel are refused.
 """
 
 import ctypes
@@ -70,17 +73,22 @@ def test_noalloc_batch_matches_render_device(gpu, dome_scene):
             reference.append({k: v.cpu().numpy() for k, v in bufs.items()})
 
         c_configs = (_abi.SkyRenderConfig * len(configs))(*[c.to_c() for c in configs])
-        for _ in range(2):  # the shared scratch area must serve consecutive calls
+        for call in range(2):  # the shared scratch area must serve consecutive calls
             bufs = [_buffers(torch, c, bands) for c in configs]
             status = torch.zeros(1, dtype=torch.int32, device="cuda")
             counters = torch.zeros(8, dtype=torch.int64, device="cuda")
             outs = (_abi.SkyDeviceOutputs * len(configs))(
                 *[_outputs_struct(b, status if i == 0 else None, counters if i == 0 else None)
                   for i, b in enumerate(bufs)])
+            torch.cuda.synchronize()
+            allocs, free = lib.sky_cuda_device_allocations(), torch.cuda.mem_get_info()[0]
             st = lib.sky_cuda_render_batch_noalloc(gs.handle, c_configs, outs, len(configs),
                                                    ctypes.c_void_p(stream))
             _abi.check(st, lib)
             torch.cuda.synchronize()
+            if call == 1:  # warmed: the device code is loaded, nothing may be allocated
+                assert lib.sky_cuda_device_allocations() == allocs
+                assert torch.cuda.mem_get_info()[0] == free
             assert int(status.item()) == 0
             chains = sum(c.pixels * bands * c.spp for c in configs)
             assert int(counters[6].item()) == chains
@@ -103,6 +111,11 @@ def test_noalloc_rejects_oversized_batch(gpu, dome_scene):
         st = lib.sky_cuda_render_batch_noalloc(gs.handle, c_configs, outs, n, None)
         assert st == _abi.SKY_ERR_INVALID_CONFIG
         assert "SKY_NOALLOC_MAX_JOBS" in _abi.last_error(lib)
+        # the call runs the wavefront kernel only: a job asking for the plain kernel is refused
+        plain = (_abi.SkyRenderConfig * 1)(RenderConfig(width=4, height=4, spp=4, kernel=_abi.KERNEL_PLAIN,
+                                                        tracking=_abi.TRACKING_MERGED_LAYERS).to_c())
+        st = lib.sky_cuda_render_batch_noalloc(gs.handle, plain, outs, 1, None)
+        assert st == _abi.SKY_ERR_INVALID_CONFIG and "wavefront kernel only" in _abi.last_error(lib)
         # the scene still renders through the allocation-free path afterwards
         st = lib.sky_cuda_render_batch_noalloc(gs.handle, c_configs, outs, 1, None)
         _abi.check(st, lib)
