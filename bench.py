@@ -83,7 +83,7 @@ def parse_args():
                    default=DEFAULT_WORKLOAD)
     p.add_argument("--kernel", type=int, default=0, help="SkyKernel (0 auto, 1 plain, 2 wavefront)")
     p.add_argument("--tuning", default="",
-                   help="SkyTuning fields set before autotuning, e.g. variant=0,track_slice=3")
+                   help="SkyTuning fields set before autotuning, e.g. variant=0,crossing_cost=0.25")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-peak", action="store_true", help="skip the SGEMM FP32-peak measurement")
@@ -691,7 +691,7 @@ def fit_report(args, iterations):
                      "relative_rms_error_debiased": ev["relative_rms_error_debiased"],
                      "relative_rms_resolution": ev["relative_rms_resolution"],
                      "relative_rms_noise": ev["relative_rms_noise"],
-                     "wall_s": fit["seconds"], "iterations": fit["iterations"],
+                     "wall_s": fit["seconds"], "setup_s": fit["setup_seconds"], "iterations": fit["iterations"],
                      "loss_first": fit["loss"][0] if fit["loss"] else None,
                      "loss_last": fit["loss"][-1] if fit["loss"] else None}
     return {"workload": FIT_WORKLOAD, "iterations": iterations, "target_render_s": t_target,

@@ -5,10 +5,12 @@
 //   * the pcg4d counter RNG is bit-exact with sky_trace.wgsl:156-189; the
 //     three chain-constant lanes of the counter are hashed once per chain;
 //   * a ray is described by its impact parameter p = |o x d| and b = o.d, so
-//     the shell quadratic  t = -b +- sqrt(R^2 - p^2)  is evaluated as
-//     sqrt((R - p)(R + p)) without the cancellation of b^2 - c at Earth
-//     radius, one square root per shell instead of the two full sphere
-//     intersections of sky_trace.wgsl:211-221;
+//     the majorant-layer crossings of the tracker, t = -b +- sqrt(R^2 - p^2),
+//     are evaluated as sqrt((R - p)(R + p)), one square root per shell
+//     instead of the two full sphere intersections of sky_trace.wgsl:211-221
+//     (an error there only moves where a majorant changes); the ground and
+//     top-of-atmosphere boundary keeps the reference's b^2 - c form, whose
+//     roots stay consistent with the origin's altitude;
 //   * the medium is read from the union-knot tables of sky_scene.h (one
 //     lookup + one FMA instead of two linear profile scans).
 #pragma once
@@ -126,17 +128,35 @@ __device__ __forceinline__ float half_chord(float radius, float p) {
     return disc >= 0.0f ? sqrtf(disc) : -1.0f;
 }
 
+// Both roots -b -+ sqrt(b^2 - c) of the sphere of `radius` with
+// c = (|o| - R)(|o| + R), the form of intersect_sphere (sky_trace.wgsl:211-221).
+// Here the sign of c is the sign of the origin's computed altitude above the
+// sphere, so a ray that leaves the ground upwards (b > 0, c > 0) has two
+// negative roots and cannot re-enter it.  The impact-parameter form's far root
+// sqrt((R - p)(R + p)) - b carries the FP32 rounding of p amplified by
+// cot(elevation) (6 m at 5 degrees, more than the 5 m ray epsilon), which made
+// some shadow rays leaving the ground towards a low sun hit it again.
+// The rounding is fixed by intrinsics (no contraction left to the compiler),
+// so that every kernel that inlines it takes the same decisions on grazing rays.
+__device__ __forceinline__ bool sphere_roots(const RayGeo& g, float r0, float radius, float& t0, float& t1) {
+    const float c = __fmul_rn(__fsub_rn(r0, radius), __fadd_rn(r0, radius));
+    const float disc = __fmaf_rn(g.b, g.b, -c);
+    if (disc < 0.0f) return false;
+    const float s = sqrtf(disc);
+    t0 = -g.b - s;
+    t1 = -g.b + s;
+    return true;
+}
+
 // next_boundary (sky_trace.wgsl:233-250): ground (kind 0) or top exit (kind 1).
 __device__ __forceinline__ bool next_boundary(const DevScene& S, const RayGeo& g, float& t_out, uint32_t& kind) {
-    float q_top = half_chord(S.atmosphere_radius, g.p);
-    if (q_top < 0.0f) return false;
-    float t_exit = fmaxf(q_top - g.b, kRayEpsilonKm);
-    float t_ground = -1.0f;
-    float q_g = half_chord(S.ground_radius, g.p);
-    if (q_g >= 0.0f) {
-        float t0 = -q_g - g.b, t1 = q_g - g.b;
+    const float r0 = sqrtf(g.r0sq);
+    float a0, a1;
+    if (!sphere_roots(g, r0, S.atmosphere_radius, a0, a1)) return false;
+    float t_exit = fmaxf(a1, kRayEpsilonKm);
+    float t_ground = -1.0f, t0, t1;
+    if (sphere_roots(g, r0, S.ground_radius, t0, t1))
         t_ground = t0 > kRayEpsilonKm ? t0 : (t1 > kRayEpsilonKm ? t1 : -1.0f);
-    }
     if (t_ground > kRayEpsilonKm && t_ground < t_exit) {
         t_out = t_ground;
         kind = 0u;

@@ -1,0 +1,154 @@
+//! Declarations of include/sky_cuda.h used by this crate.  Every struct is
+//! `#[repr(C)]` with the header's field order; the table rows have the byte
+//! layout of the reference's GPU structs (integrator.rs:77-112).
+
+use std::os::raw::{c_char, c_int, c_void};
+
+pub const SKY_OK: c_int = 0;
+pub const SKY_ERR_INVALID_CONFIG: c_int = 1;
+pub const SKY_ERR_NO_DEVICE: c_int = 2;
+pub const SKY_ERR_DEVICE_INIT: c_int = 3;
+pub const SKY_ERR_COPY: c_int = 4;
+pub const SKY_ERR_SYNC: c_int = 5;
+pub const SKY_ERR_WATCHDOG: c_int = 6;
+pub const SKY_ERR_OUT_OF_MEMORY: c_int = 7;
+pub const SKY_ERR_LAUNCH: c_int = 8;
+pub const SKY_ERR_IO: c_int = 9;
+
+/// = GpuBand (integrator.rs:79-86), 24 bytes.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyBand {
+    pub center_nm: f32,
+    pub lower_nm: f32,
+    pub upper_nm: f32,
+    pub ozone_cross_section_cm2: f32,
+    pub solar_radiance_w_m2_sr: f32,
+    pub rayleigh_cross_section_m2: f32,
+}
+
+/// = GpuAtmospherePoint (integrator.rs:90-95), 16 bytes.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyAtmospherePoint {
+    pub altitude_km: f32,
+    pub temperature_k: f32,
+    pub air_cm3: f32,
+    pub ozone_cm3: f32,
+}
+
+/// = GpuAerosolPoint (integrator.rs:99-105), 32 bytes.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyAerosolPoint {
+    pub altitude_km: f32,
+    pub mass_g_m3: [f32; 4],
+    pub _pad: [f32; 3],
+}
+
+/// = GpuAerosolOptics (integrator.rs:109-112), 8 bytes.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyAerosolOptics {
+    pub scattering_km_inv_per_g_m3: f32,
+    pub absorption_km_inv_per_g_m3: f32,
+}
+
+#[repr(C)]
+pub struct SkySceneDesc {
+    pub band_count: u32,
+    pub atmosphere_len: u32,
+    pub aerosol_len: u32,
+    pub majorant_layers: u32,
+    pub phase_bins: u32,
+    pub _reserved0: u32,
+    pub ground_radius_km: f32,
+    pub atmosphere_radius_km: f32,
+    pub top_altitude_km: f32,
+    pub sun_direction: [f32; 3],
+    pub sun_angular_radius_rad: f32,
+    pub sun_solid_angle_sr: f32,
+    pub ground_albedo: f32,
+    pub _reserved1: f32,
+    pub bands: *const SkyBand,
+    pub atmosphere: *const SkyAtmospherePoint,
+    pub aerosol: *const SkyAerosolPoint,
+    pub aerosol_optics: *const SkyAerosolOptics,
+    pub majorants_km_inv: *const f32,
+    pub phase_values: *const f32,
+    pub band_xyz_weights: *const f32,
+}
+
+/// = RenderConfig (config.rs:2-12) followed by the extensions; all-zero
+/// extensions render what the reference shader renders.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyRenderConfig {
+    pub width: u32,
+    pub height: u32,
+    pub spp: u32,
+    pub direct_light_samples: u32,
+    pub seed: u64,
+    pub sun_elevation_deg: f32,
+    pub sun_azimuth_deg: f32,
+    pub observer_altitude_km: f32,
+    pub output_projection: u32,
+    pub sample_offset: u32,
+    pub phase_sampling: u32,
+    pub rr_start_depth: u32,
+    pub max_orders: u32,
+    pub watchdog_limit: u32,
+    pub kernel: u32,
+    pub flags: u32,
+    pub tracking: u32,
+    pub row_begin: u32,
+    pub row_count: u32,
+}
+
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct SkyRenderStats {
+    pub kernel_ms: f64,
+    pub total_ms: f64,
+    pub chains: u64,
+    pub events: [u64; 8],
+    pub watchdog: u32,
+    pub kernel_used: u32,
+}
+
+/// Opaque scene handle (device tables owned by the library).
+#[repr(C)]
+pub struct SkyScene {
+    _opaque: [u8; 0],
+}
+
+unsafe extern "C" {
+    pub fn sky_cuda_version() -> *const c_char;
+    pub fn sky_cuda_last_error(buf: *mut c_char, buf_len: usize) -> c_int;
+    pub fn sky_cuda_scene_create(desc: *const SkySceneDesc, out_scene: *mut *mut SkyScene) -> c_int;
+    pub fn sky_cuda_scene_destroy(scene: *mut SkyScene);
+    pub fn sky_cuda_render(scene: *const SkyScene, config: *const SkyRenderConfig, film_out: *mut f32,
+                           film_len: usize, stats: *mut SkyRenderStats) -> c_int;
+    pub fn sky_cuda_render_desc(desc: *const SkySceneDesc, config: *const SkyRenderConfig, film_out: *mut f32,
+                                film_len: usize, stats: *mut SkyRenderStats) -> c_int;
+    pub fn sky_cuda_render_device(scene: *const SkyScene, config: *const SkyRenderConfig,
+                                  outputs: *const c_void, cuda_stream: *mut c_void) -> c_int;
+}
+
+#[cfg(test)]
+mod layout {
+    use super::*;
+    use std::mem::size_of;
+
+    #[test]
+    fn rows_have_the_reference_gpu_layouts() {
+        // integrator.rs:479-510 checks the same sizes for GpuBand and friends
+        assert_eq!(size_of::<SkyBand>(), 24);
+        assert_eq!(size_of::<SkyAtmospherePoint>(), 16);
+        assert_eq!(size_of::<SkyAerosolPoint>(), 32);
+        assert_eq!(size_of::<SkyAerosolOptics>(), 8);
+        assert_eq!(size_of::<SkySceneDesc>(), 120);
+        assert_eq!(size_of::<SkyRenderConfig>(), 80);
+        assert_eq!(size_of::<SkyRenderStats>(), 96);
+    }
+}

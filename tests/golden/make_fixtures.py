@@ -1,9 +1,9 @@
 """Regenerate the committed fixtures under tests/golden/ from the reference.
 
-Run in a container where the reference checkout is mounted (it is absent on
-GPU machines, which use the committed copies):
+Run where a checkout of the reference is available (GPU machines have none
+and use the committed copies), giving the checkout's root directory:
 
-    python tests/golden/make_fixtures.py /root/reference
+    python tests/golden/make_fixtures.py PATH_TO_REFERENCE_CHECKOUT
 
 It copies the reference's data tables (crates/sky-core/src/data.rs reads
 bands.csv, atmosphere_profile.csv, aerosol_profile.csv, aerosol_optics.csv;
@@ -38,4 +38,6 @@ def main(reference: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py PATH_TO_REFERENCE_CHECKOUT")
+    main(sys.argv[1])

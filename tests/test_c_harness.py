@@ -1,0 +1,84 @@
+"""The sky-cuda Rust crate's calls, made from C (tests/c_abi_harness.c).
+
+No Rust toolchain exists on these machines (cargo and rustc are absent here
+and on the GPU machine), so the crate's FFI sequence is exercised by a C program
+that makes the same calls with the same structs: sky_cuda_render_desc (the
+crate's `render`), sky_cuda_scene_create / sky_cuda_render /
+sky_cuda_scene_destroy (its `GpuScene`), and the error path through
+sky_cuda_last_error (its RenderError mapping).  On the CPU the harness is
+compiled and linked against libsky_cuda.so; on the GPU it renders the
+reference's own data/ scene and its film must equal the Python one-shot
+render of the same scene and config.
+"""
+
+import os
+import struct
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from sky_cuda import RenderConfig, render
+
+ROOT = Path(__file__).resolve().parents[1]
+HARNESS = ROOT / "tests" / "c_abi_harness.c"
+LIB_DIR = ROOT / "sky-tracer_gb300" / "_build"
+
+
+def build_harness(out_dir: Path) -> Path:
+    exe = out_dir / "c_abi_harness"
+    cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(HARNESS),
+           "-L", str(LIB_DIR), "-lsky_cuda", f"-Wl,-rpath,{LIB_DIR}", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    return exe
+
+
+def write_scene(scene, path: Path) -> None:
+    """The harness's scene file: counts, scalars, then the table rows."""
+    with open(path, "wb") as f:
+        f.write(b"SKYT")
+        f.write(struct.pack("<5I", scene.band_count, len(scene.atmosphere), len(scene.aerosol), scene.layer_count,
+                            scene.phase_bins))
+        f.write(struct.pack("<11f", scene.ground_radius_km, scene.atmosphere_radius_km, scene.top_altitude_km,
+                            *scene.sun_direction, scene.sun_angular_radius_rad, scene.sun_solid_angle_sr,
+                            scene.ground_albedo, 0.0, 0.0))
+        for table in (scene.bands, scene.atmosphere, scene.aerosol, scene.aerosol_optics,
+                      np.ascontiguousarray(scene.majorants, dtype=np.float32),
+                      np.ascontiguousarray(scene.phase_values, dtype=np.float32)):
+            f.write(np.ascontiguousarray(table).tobytes())
+
+
+def test_harness_compiles_and_links_against_the_library(lib_built, tmp_path):
+    exe = build_harness(tmp_path)
+    assert exe.exists()
+    # the dynamic symbols the harness binds resolve in the library
+    res = subprocess.run(["nm", "-D", "--undefined-only", str(exe)], capture_output=True, text=True)
+    for sym in ("sky_cuda_render_desc", "sky_cuda_scene_create", "sky_cuda_render", "sky_cuda_last_error",
+                "sky_cuda_scene_destroy", "sky_cuda_version"):
+        assert sym in res.stdout
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("projection", [0, 1])
+def test_harness_film_equals_the_python_render(gpu, ref_scene, tmp_path, projection):
+    exe = build_harness(tmp_path)
+    scene_file, film_file = tmp_path / "scene.bin", tmp_path / "film.bin"
+    write_scene(ref_scene, scene_file)
+    cfg = RenderConfig(width=24, height=12, spp=8, seed=0x5EC7_2026_0430, output_projection=projection)
+    res = subprocess.run([str(exe), str(scene_file), "24", "12", "8", str(cfg.seed), str(projection),
+                          str(film_file)], capture_output=True, text=True, timeout=300,
+                         env={**os.environ, "LD_LIBRARY_PATH": str(LIB_DIR)})
+    assert res.returncode == 0, res.stdout + res.stderr
+    film_c = np.fromfile(film_file, dtype=np.float32)
+    film_py = render(ref_scene, cfg).values
+    assert film_c.shape == film_py.shape == (24 * 12 * ref_scene.band_count,)
+    # the same one-shot call on the same inputs: equal up to the order of the FP64 cell sums
+    np.testing.assert_allclose(film_c, film_py, rtol=1e-6, atol=0)
+    assert np.all(np.isfinite(film_c)) and np.all(film_c >= 0) and np.any(film_c > 0)
+
+
+if __name__ == "__main__":
+    sys.exit(pytest.main([__file__, "-q"]))
