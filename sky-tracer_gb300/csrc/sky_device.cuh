@@ -254,6 +254,21 @@ __device__ __forceinline__ float merged_crossing(const MergedGrid& G, const RayG
 
 // ---- medium ---------------------------------------------------------------------------
 
+// The band-independent knot tables and the per-band constants that the
+// medium functions read, wherever they are held: the scene's global copies,
+// or the copies a kernel staged in its block's shared memory.
+struct Medium {
+    const float* knot_z;            // [K]
+    const uint16_t* finder;         // [kFinderCells]
+    const DevProfileKnot* profile;  // [K]
+    const DevBand* bands;           // [B]
+    const SkyAerosolOptics* optics; // [B][species]
+};
+
+__device__ __forceinline__ Medium global_medium(const DevScene& S) {
+    return Medium{S.knot_z, S.finder, S.profile, S.bands, S.optics};
+}
+
 // Knot interval containing `alt` (alt in [0, top]).
 __device__ __forceinline__ uint32_t knot_interval(const DevScene& S, const float* knot_z, const uint16_t* finder,
                                                   float alt) {
@@ -283,8 +298,7 @@ struct Coeffs {  // MediumCoefficients (sky_trace.wgsl:101-106)
 
 // coefficients_at (sky_trace.wgsl:356-386) from the band-independent knot
 // profile and the per-band cross sections.
-__device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
-                                                  uint32_t band, float alt) {
+__device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const Medium& M, uint32_t band, float alt) {
     Coeffs c;
     c.rayleigh = 0.0f;
 #pragma unroll
@@ -293,10 +307,10 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float
     c.scattering = 0.0f;
     c.extinction = 0.0f;
     if (!(alt >= 0.0f && alt <= S.top_altitude)) return c;
-    uint32_t k = knot_interval(S, knot_z, finder, alt);
-    float dz = alt - knot_z[k];
-    const DevProfileKnot& P = S.profile[k];
-    const DevBand& B = S.bands[band];
+    uint32_t k = knot_interval(S, M.knot_z, M.finder, alt);
+    float dz = alt - M.knot_z[k];
+    const DevProfileKnot& P = M.profile[k];
+    const DevBand& B = M.bands[band];
     float air = fmaf(dz, P.air_slope, P.air);
     float ozone = fmaf(dz, P.ozone_slope, P.ozone);
     c.rayleigh = fmaxf(air * B.rayleigh_xs, 0.0f);
@@ -305,7 +319,7 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float
 #pragma unroll
     for (int i = 0; i < int(kSpecies); ++i) {
         float mass = fmaxf(fmaf(dz, P.mass_slope[i], P.mass[i]), 0.0f);
-        SkyAerosolOptics o = S.optics[band * kSpecies + i];
+        SkyAerosolOptics o = M.optics[band * kSpecies + i];
         c.sca[i] = fmaxf(mass * o.scattering_km_inv_per_g_m3, 0.0f);
         absorption += fmaxf(mass * o.absorption_km_inv_per_g_m3, 0.0f);
         scattering += c.sca[i];
@@ -314,6 +328,12 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float
     c.scattering = scattering;
     c.extinction = scattering + absorption;
     return c;
+}
+
+// The same from the scene's global tables.
+__device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
+                                                  uint32_t band, float alt) {
+    return coefficients_at(S, Medium{knot_z, finder, S.profile, S.bands, S.optics}, band, alt);
 }
 
 // ---- phase functions ----------------------------------------------------------------
@@ -566,8 +586,8 @@ __device__ __forceinline__ V3 camera_dir(const DevLaunch& L, uint32_t x, uint32_
 // without a collision (sky_trace.wgsl:412-415), a shadow ray (shadow = true)
 // as blocked, transmittance 0 (:448-451).
 // Residual-carry delta tracking over the band's merged tracking grid.
-__device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo& g, float t_max, uint32_t band,
-                                                 Rng& rng, float& t_hit, Counters& n, bool& watchdog,
+__device__ __forceinline__ bool track_ray_merged(const DevScene& S, const Medium& M, const RayGeo& g, float t_max,
+                                                 uint32_t band, Rng& rng, float& t_hit, Counters& n, bool& watchdog,
                                                  bool shadow) {
     const MergedGrid G = merged_grid(S, band);
     const float2* sig_row = S.sigma_t + band * S.knot_count;
@@ -584,7 +604,7 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo
         if (t + dt < t_seg) {
             t = t + dt;
             ++n.e[SKY_EVENT_TRACK_STEP];
-            float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
+            float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
             if (rng.next() * maj < sig) {
                 t_hit = t;
                 return true;
@@ -607,10 +627,11 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const RayGeo
 }
 
 template <int kTracking>
-__device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, float t_max, uint32_t band, Rng& rng,
-                                          float& t_hit, Counters& n, bool& watchdog, bool shadow) {
+__device__ __forceinline__ bool track_ray(const DevScene& S, const Medium& M, const RayGeo& g, float t_max,
+                                          uint32_t band, Rng& rng, float& t_hit, Counters& n, bool& watchdog,
+                                          bool shadow) {
     if (kTracking == SKY_TRACKING_MERGED_LAYERS)
-        return track_ray_merged(S, g, t_max, band, rng, t_hit, n, watchdog, shadow);
+        return track_ray_merged(S, M, g, t_max, band, rng, t_hit, n, watchdog, shadow);
     const float* maj_row = S.majorants + band * S.layer_count;
     const float2* sig_row = S.sigma_t + band * S.knot_count;
     float t = 0.0f;
@@ -643,7 +664,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, fl
                 need_draw = true;
                 ++n.e[SKY_EVENT_TRACK_STEP];
                 float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, alt);
+                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, alt);
                 if (rng.next() * maj < sig) {
                     t_hit = t;
                     return true;
@@ -657,7 +678,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const RayGeo& g, fl
                 if (t >= seg_end) break;
                 ++n.e[SKY_EVENT_TRACK_STEP];
                 float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, S.knot_z, S.finder, sig_row, 0u, alt);
+                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, alt);
                 if (rng.next() * maj < sig) {
                     t_hit = t;
                     return true;

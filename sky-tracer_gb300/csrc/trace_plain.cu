@@ -27,7 +27,7 @@ __device__ __forceinline__ float shadow_transmittance(const DevScene& S, V3 pos,
     ++n.e[SKY_EVENT_BOUNDARY];
     if (!next_boundary(S, sg, t_b, kind) || kind != 1u) return -1.0f;  // no sun visible: no contribution
     float t_hit;
-    return track_ray<kTracking>(S, sg, t_b, band, rng, t_hit, n, watchdog, true) ? 0.0f : 1.0f;
+    return track_ray<kTracking>(S, global_medium(S), sg, t_b, band, rng, t_hit, n, watchdog, true) ? 0.0f : 1.0f;
 }
 
 // trace_path (sky_trace.wgsl:703-776) for one chain.
@@ -55,7 +55,7 @@ __device__ float trace_chain(const DevScene& S, const DevLaunch& L, uint32_t x, 
         ++n.e[SKY_EVENT_BOUNDARY];
         if (!next_boundary(S, g, t_b, kind)) break;
         float t_hit;
-        if (track_ray<kTracking>(S, g, t_b, band, rng, t_hit, n, watchdog, false)) {
+        if (track_ray<kTracking>(S, global_medium(S), g, t_b, band, rng, t_hit, n, watchdog, false)) {
             ++n.e[SKY_EVENT_SCATTER];
             V3 pos = madd(org, dir, t_hit);
             Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, altitude_at(g, t_hit, S.ground_radius));

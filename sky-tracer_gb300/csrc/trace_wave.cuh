@@ -81,6 +81,40 @@ __device__ __forceinline__ const DevScene& job_scene(const DevScene& S0, const D
     else return jobs[job].S;
 }
 
+// Bytes of shared memory that stage_medium() fills: the band-independent knot
+// profile (48 B per knot), the per-band constants (32 B per band) and aerosol
+// optics (32 B per band), the union knots and the knot finder.
+__host__ __device__ inline size_t staged_medium_bytes(uint32_t knots, uint32_t bands) {
+    return size_t(knots) * sizeof(DevProfileKnot) + size_t(bands) * sizeof(DevBand) +
+           size_t(bands) * kSpecies * sizeof(SkyAerosolOptics) + size_t(knots) * sizeof(float) +
+           size_t(kFinderCells) * sizeof(uint16_t);
+}
+
+// Copy the medium tables every collision and NEE evaluation reads into the
+// block's shared memory (once per block, before the loop), and return the
+// view of them.  The per-band extinction rows and the phase tables stay in
+// global memory, read through the L1 cache.
+__device__ __forceinline__ Medium stage_medium(const DevScene& S, unsigned char* smem) {
+    DevProfileKnot* profile = reinterpret_cast<DevProfileKnot*>(smem);
+    DevBand* bands = reinterpret_cast<DevBand*>(profile + S.knot_count);
+    SkyAerosolOptics* optics = reinterpret_cast<SkyAerosolOptics*>(bands + S.band_count);
+    float* knot_z = reinterpret_cast<float*>(optics + S.band_count * kSpecies);
+    uint16_t* finder = reinterpret_cast<uint16_t*>(knot_z + S.knot_count);
+    // 4-byte words throughout (every table is a multiple of 4 bytes; the finder's 512 halves are 256 words)
+    auto copy = [](void* dst, const void* src, size_t bytes) {
+        uint32_t* d = static_cast<uint32_t*>(dst);
+        const uint32_t* s = static_cast<const uint32_t*>(src);
+        for (size_t i = threadIdx.x; i < bytes / 4u; i += blockDim.x) d[i] = __ldg(s + i);
+    };
+    copy(profile, S.profile, size_t(S.knot_count) * sizeof(DevProfileKnot));
+    copy(bands, S.bands, size_t(S.band_count) * sizeof(DevBand));
+    copy(optics, S.optics, size_t(S.band_count) * kSpecies * sizeof(SkyAerosolOptics));
+    copy(knot_z, S.knot_z, size_t(S.knot_count) * sizeof(float));
+    copy(finder, S.finder, size_t(kFinderCells) * sizeof(uint16_t));
+    __syncthreads();
+    return Medium{knot_z, finder, profile, bands, optics};
+}
+
 // kCount: count events (SkyDeviceOutputs.counters given).  Without it the
 // counters are never read, so their increments compile away (the registers
 // they would hold are worth ~5 % at 64 registers per lane).
@@ -90,6 +124,8 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 const DevJob* __restrict__ jobs, uint32_t num_jobs,
                 uint32_t total_cells, uint32_t* __restrict__ work_counter, unsigned long long* __restrict__ counters,
                 uint32_t* __restrict__ status, uint64_t iteration_limit) {
+    extern __shared__ __align__(16) unsigned char medium_smem[];
+    const Medium M = stage_medium(S, medium_smem);
     const uint32_t lane = threadIdx.x & 31u;
     Counters n;
     n.clear();
@@ -221,7 +257,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     float cos_t = 1.0f, sin_t = 0.0f, xi_phi = 0.0f, weight = 1.0f;
                     bool framed = true;
                     if (!ground) {
-                        const Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+                        const Coeffs c = coefficients_at(S, M, band, alt);
                         if (kPhase == SKY_PHASE_TABULATED) {
                             float mu;
                             weight = tabulated_mu(S, c, band, rng, mu, xi_phi);
@@ -303,7 +339,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         }
         if (tracing) {
             float t_hit = 0.0f;
-            const bool hit = track_ray<kTracking>(S, g, t_max, band, rng, t_hit, n, watchdog, shadow_ray);
+            const bool hit = track_ray<kTracking>(S, M, g, t_max, band, rng, t_hit, n, watchdog, shadow_ray);
             // the medium coefficients at a real collision (albedo) and at the vertex of
             // an unblocked shadow ray (phase of its NEE term): one call for both kinds
             const bool lit = shadow_ray && !hit;
@@ -312,10 +348,10 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 alt = altitude_at(g, t_hit, S.ground_radius);
             }
             Coeffs c;
-            if ((!shadow_ray && hit) || (lit && !ground)) c = coefficients_at(S, S.knot_z, S.finder, band, alt);
+            if ((!shadow_ray && hit) || (lit && !ground)) c = coefficients_at(S, M, band, alt);
             if (shadow_ray) {
                 if (lit) {  // the sample's term, transmittance 1 (sky_trace.wgsl:566-608)
-                    const float l_sun = __ldg(&S.bands[band].solar_radiance);
+                    const float l_sun = M.bands[band].solar_radiance;
                     nee += ground ? S.ground_albedo * kInvPi * l_sun * 1.0f * nee_mu / S.light_pdf
                                   : l_sun * 1.0f * mixed_phase(S, c, band, nee_mu) / S.light_pdf;
                 }
@@ -335,7 +371,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 }
             } else if (boundary == 1u) {
                 if (depth == 0u && dot3(dir, load3(job_scene<kSingle>(S, jobs, job).sun)) >= S.cos_max)
-                    rad += thr * __ldg(&S.bands[band].solar_radiance);
+                    rad += thr * M.bands[band].solar_radiance;
                 rad = fmaxf(rad, 0.0f);
                 next = kEnd;
             } else {
@@ -373,13 +409,19 @@ cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
     cudaError_t e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWaveThreads, 0)) != cudaSuccess) return e;
+    // the staged medium tables: 10 KB for 81 bands over 68 knots; the largest scenes the library
+    // accepts (1024 knots, 256 bands) need 71 KB, beyond the 48 KB a launch gets without opting in
+    const size_t smem = staged_medium_bytes(w.scene.knot_count, w.scene.band_count);
+    if (smem > 48u * 1024u &&
+        (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
+        return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWaveThreads, smem)) != cudaSuccess) return e;
     per_sm = std::max(per_sm, 1);
     if (w.max_blocks_per_sm) per_sm = std::min(per_sm, int(w.max_blocks_per_sm));
     // a warp per cell at most
     const uint64_t want = (uint64_t(w.total_cells) * 32u + kWaveThreads - 1u) / kWaveThreads;
     const uint32_t blocks = uint32_t(std::max<uint64_t>(1u, std::min<uint64_t>(uint64_t(per_sm) * sms, want)));
-    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount><<<blocks, kWaveThreads, 0, stream>>>(
+    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount><<<blocks, kWaveThreads, smem, stream>>>(
         w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status,
         w.iteration_limit ? w.iteration_limit : kMaxIterations);
     return cudaGetLastError();

@@ -93,3 +93,31 @@ def test_production_settings_mean_relative_error_at_high_spp(gpu, production_sce
     assert r["noise_rel_err_per_pixel"] < 0.003
     assert r["mean_rel_err_per_pixel"] < 0.005
     assert r["frac_beyond_3se"] <= 0.05
+
+
+@pytest.mark.parametrize("elevation", [-2.0, 0.5, 3.0])
+def test_twilight_sky_view_lut_parity(gpu, ref_scene, elevation):
+    """The reference's own scene (data/ tables, 41 bands) as its elevation bake
+    renders it (sky-view LUT, scripts/bake_skyview_elevations.ps1), at the low
+    sun elevations where shadow rays graze the ground: a 16x8 LUT at 2^17
+    (GPU) and 2^14 (oracle) samples, merged-layer tracking and tabulated phase
+    sampling on both, independent seeds."""
+    scene = ref_scene.with_sun(elevation)
+    base = dict(width=16, height=8, sun_elevation_deg=elevation, output_projection=_abi.PROJECTION_SKY_VIEW_LUT,
+                phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS)
+    cfg_g = RenderConfig(spp=1 << 17, seed=0x5EC7_2026_0430, **base)
+    cfg_o = RenderConfig(spp=1 << 14, seed=0x2BAD5EED, **base)
+    with GpuScene(scene) as gs:
+        gs_, gq = _gpu_sums(gs, cfg_g)
+    os_, oq, _, wd = oracle.render(scene, cfg_o)
+    assert wd == 0
+    w = scene.band_xyz
+    xg, vg = xyz_from_sums(gs_, gq, cfg_g.spp, w)
+    xo, vo = xyz_from_sums(os_, oq, cfg_o.spp, w)
+    r = parity_report(xg, vg, xo, vo)
+    print(f"twilight {elevation} deg", r)
+    assert r["pixels"] >= 64
+    assert r["frac_beyond_3se"] <= 0.03
+    assert abs(r["mean_z"]) < 0.35
+    for b, se in zip(r["bias_xyz"], r["bias_se_xyz"]):
+        assert abs(b) < 0.005 + 3 * se
