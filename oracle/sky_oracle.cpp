@@ -277,17 +277,39 @@ inline float next_majorant_segment_end(const Ctx& c, const Ray& ray, float t,
     return next_t;
 }
 
-// Tracking mode 2: next_majorant_segment_end over the merged grid, with the
-// reference's candidate rule (both roots of both shells beyond t + epsilon).
+// Altitude of ray_at(ray, t) evaluated in double precision.  The reference's
+// f32 probe (next_majorant_segment_end, sky_trace.wgsl:284-294) resolves
+// altitude to ~0.5 m at Earth radius, while a ray descending at less than
+// ~6 degrees drops less than that in RAY_EPSILON_KM: at a downward shell
+// crossing the f32 probe still reads the upper layer, and the segment then
+// runs past the tangent point under the upper layer's majorant (optical depth
+// skipped; see tests/test_oracle.py::test_transmittance_on_descending_rays).
+// Tracking modes 0 and 1 keep the reference's probe, defect included, since
+// they restate the reference; mode 2, an extension, probes exactly.
+inline double altitude_exact(const Ctx& c, const Ray& ray, float t) {
+    const double x = double(ray.origin.x) + double(ray.dir.x) * double(t);
+    const double y = double(ray.origin.y) + double(ray.dir.y) * double(t);
+    const double z = double(ray.origin.z) + double(ray.dir.z) * double(t);
+    return std::sqrt(x * x + y * y + z * z) - double(c.ground_radius_km);
+}
+inline uint32_t layer_for_altitude_exact(const Ctx& c, double altitude) {
+    const double top = std::max(double(c.top_altitude_km), 0.000001);
+    const double clamped = std::min(std::max(altitude, 0.0), top - 0.000001);
+    return std::min(uint32_t(std::floor(clamped / top * double(c.majorant_layers))), c.majorant_layers - 1u);
+}
+
+// Tracking mode 2: the next segment end over the merged grid with the
+// reference's candidate rule (both roots of both shells of the current merged
+// layer beyond t + epsilon), the layer taken from an exact probe at t + epsilon.
 inline float merged_segment_end(const Ctx& c, const Ray& ray, uint32_t band, float t, float t_max, float& majorant) {
     float probe_t = std::min(t + RAY_EPSILON_KM, t_max);
-    uint32_t k = layer_for_altitude(c, altitude_km(c, ray_at(ray, probe_t)));
+    uint32_t k = layer_for_altitude_exact(c, altitude_exact(c, ray, probe_t));
     uint32_t g = c.merged_of[band][k];
     float next_t = t_max;
     next_t = boundary_candidate(c, ray, t, next_t, c.merged_lo[band][g]);
     next_t = boundary_candidate(c, ray, t, next_t, c.merged_lo[band][g + 1]);
     float probe2 = std::min(t + RAY_EPSILON_KM, next_t);
-    uint32_t k2 = layer_for_altitude(c, altitude_km(c, ray_at(ray, probe2)));
+    uint32_t k2 = layer_for_altitude_exact(c, altitude_exact(c, ray, probe2));
     majorant = c.merged_maj[band][c.merged_of[band][k2]];
     return next_t;
 }

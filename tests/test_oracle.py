@@ -292,3 +292,34 @@ def test_oracle_transmittance_known_answer(ref_scene, tracking):
             got = oracle.transmittance(ref_scene, tracking, o, d, band, n)
             se = math.sqrt(max(want * (1.0 - want), 1e-12) / n)
             assert abs(got - want) <= 4.0 * se + 1e-3, (elev, band, got, want, se)
+
+
+def test_transmittance_on_descending_rays(ref_scene):
+    """Rays that descend through shells to a tangent point, as shadow rays do
+    at twilight.  Merged-layer tracking (mode 2) averages to exp(-optical
+    depth) on all of them.  The reference's segment rule (modes 0 and 1,
+    next_majorant_segment_end, sky_trace.wgsl:284-294) takes the next layer
+    from the f32 altitude 5 m along the ray; a ray descending at a few degrees
+    drops less than that altitude's resolution in 5 m, so at a downward shell
+    crossing the probe still reads the upper layer and the segment runs past
+    the tangent point under the upper layer's majorant: optical depth is
+    skipped and the transmittance comes out too high.  The oracle keeps that
+    behaviour in modes 0 and 1, since they restate the reference."""
+    rg, rt, top = ref_scene.ground_radius_km, ref_scene.atmosphere_radius_km, ref_scene.top_altitude_km
+    z, _, _, ext = analytic.knot_tables(ref_scene)
+    n = 20000
+    band = ref_scene.band_count - 1
+    skipped = 0
+    for h0, elev in ((10.0, -0.5), (10.0, -2.0), (20.0, -1.0), (20.0, -4.0), (40.0, -2.0), (40.0, -4.0)):
+        o = np.array([0.0, rg + h0, 0.0])
+        d = np.array([math.cos(math.radians(elev)), math.sin(math.radians(elev)), 0.0])
+        t_exit, _ = analytic._sphere_exit(o, d, rt)
+        t = np.linspace(0.0, float(t_exit), 80001)
+        alt = np.linalg.norm(o[None, :] + t[:, None] * d[None, :], axis=1) - rg
+        want = math.exp(-np.trapezoid(analytic._interp_alt(z, ext[band], alt, top), t))
+        se = math.sqrt(max(want * (1.0 - want), 1e-12) / n)
+        got = oracle.transmittance(ref_scene, _abi.TRACKING_MERGED_LAYERS, o, d, band, n)
+        assert abs(got - want) <= 4.0 * se + 1e-3, (h0, elev, got, want)
+        ref = oracle.transmittance(ref_scene, _abi.TRACKING_SEGMENT_RESTART, o, d, band, n)
+        skipped += ref > want + 10.0 * se
+    assert skipped >= 3  # the reference rule skips optical depth on the steeper of these rays
