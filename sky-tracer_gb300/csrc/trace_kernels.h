@@ -34,7 +34,7 @@ struct WaveLaunch {
     uint32_t* work_counter;        // reset by the launch itself
     unsigned long long* counters;  // may be null
     uint32_t* status;
-    uint64_t iteration_limit;      // loop iterations per warp before status bit 2 (SkyTuning.iteration_limit)
+    uint32_t iteration_limit;      // loop iterations per warp before status bit 2 (SkyTuning.iteration_limit)
 };
 
 // Prepare, trace and finalize every job of `w` (three kernels on `stream`):
@@ -52,7 +52,7 @@ cudaError_t launch_finalize(const DevScene& S, uint64_t pixels, uint32_t total_s
                             const double* cell_sumsq, float* film, double* xyz, double* xyz_var, float* rgb,
                             cudaStream_t stream);
 
-// The same for every job of a job table (one warp per pixel of the jobs'
+// The same for every job of a job table (four lanes per pixel of the jobs'
 // concatenated pixels; jobs without film / XYZ / RGB outputs are skipped).
 cudaError_t launch_finalize_jobs(const DevScene& S, const DevJob* jobs, uint32_t num_jobs, uint32_t total_cells,
                                  cudaStream_t stream);
@@ -71,18 +71,6 @@ __host__ __device__ inline RgbMatrix rgb_matrix(const DevScene& S) {
     RgbMatrix r;
     for (int i = 0; i < 9; ++i) r.m[i] = S.rgb_from_xyz[i];
     return r;
-}
-
-// rgb = M xyz in FP64, stored as float; black when any component is not
-// finite (Rgb::finite_or_black, math.rs:137-143).
-__device__ __forceinline__ void store_rgb(const RgbMatrix& M, const double xyz[3], float* out) {
-    float f[3];
-    bool finite = true;
-    for (int r = 0; r < 3; ++r) {
-        f[r] = float(double(M.m[r * 3]) * xyz[0] + double(M.m[r * 3 + 1]) * xyz[1] + double(M.m[r * 3 + 2]) * xyz[2]);
-        finite = finite && isfinite(f[r]);
-    }
-    for (int r = 0; r < 3; ++r) out[r] = finite ? f[r] : 0.0f;
 }
 
 }  // namespace sky

@@ -45,7 +45,7 @@ constexpr uint32_t kNoCell = 0xffffffffu;
 // Default backstop on the loop iterations of one warp (one ray per lane
 // each; SkyTuning.iteration_limit overrides it); a render needs ~3 rays per
 // chain / lanes in flight.  Beyond it the warp sets status bit 2 and returns.
-constexpr uint64_t kMaxIterations = 1ull << 31;
+constexpr uint32_t kMaxIterations = 1u << 31;
 
 // What a lane does next.
 enum : uint32_t {
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     wave_kernel(const __grid_constant__ DevScene S, const __grid_constant__ DevLaunch L0,
                 const DevJob* __restrict__ jobs, uint32_t num_jobs,
                 uint32_t total_cells, uint32_t* __restrict__ work_counter, unsigned long long* __restrict__ counters,
-                uint32_t* __restrict__ status, uint64_t iteration_limit) {
+                uint32_t* __restrict__ status, uint32_t iteration_limit) {
     extern __shared__ __align__(16) unsigned char medium_smem[];
     const Medium M = stage_medium(S, medium_smem);
     const uint32_t lane = threadIdx.x & 31u;
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     uint32_t acc_job = 0u, acc_cell = kNoCell;
     double acc_sum = 0.0, acc_sq = 0.0;
 
-    for (uint64_t iter = 0;; ++iter) {
+    for (uint32_t iter = 0u;; ++iter) {
         if (iter >= iteration_limit) {  // warp-uniform
             if (lane == 0u) atomicOr(status, 2u);
             break;
