@@ -92,7 +92,7 @@ def parse_args():
     p.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     p.add_argument("--no-adjoint", action="store_true", help="leave the differentiable-render block out")
     p.add_argument("--fit-iterations", type=int, default=200, help="Adam steps of each primary fit")
-    p.add_argument("--fit-summary-iterations", type=int, default=20,
+    p.add_argument("--fit-summary-iterations", type=int, default=60,
                    help="Adam steps of the cut-down fit in the default line (0 leaves the fit block out)")
     p.add_argument("--no-sweep", action="store_true", help="leave the elevation-sweep block out")
     p.add_argument("--no-adjoint-checks", action="store_true",
@@ -696,7 +696,7 @@ def fit_report(args, iterations):
                      "loss_last": fit["loss"][-1] if fit["loss"] else None}
     return {"workload": FIT_WORKLOAD, "iterations": iterations, "target_render_s": t_target,
             "elevations": len(cfg.elevations), "fit_spp": cfg.fit_spp, "target_spp": cfg.target_spp,
-            "min_spacing_nm": cfg.min_spacing_nm, "acceptance": "Oklab score (lower is better)",
+            "min_spacing_nm": cfg.min_spacing_nm, "loss": cfg.loss, "acceptance": "Oklab score (lower is better)",
             "fit": res, "speedup_wall_adjoint_vs_fd": fd["seconds"] / adj["seconds"] if adj["seconds"] else None,
             "adjoint_ms_per_iteration": adj["seconds"] / max(iterations, 1) * 1e3}
 

@@ -85,15 +85,19 @@ class BandModel:
 # ---- scoring: sky-wavelength-optimizer/src/main.rs:1121-1156 -------------------------------
 
 
+_OKLAB_M1 = [[0.8189330101, 0.3618667424, -0.1288597137],
+             [0.0329845436, 0.9293118715, 0.0361456387],
+             [0.0482003018, 0.2643662691, 0.6338517070]]
+_OKLAB_M2 = [[0.2104542553, 0.7936177850, -0.0040720468],
+             [1.9779984951, -2.4285922050, 0.4505937099],
+             [0.0259040371, 0.7827717662, -0.8086757660]]
+
+
 def xyz_to_oklab(xyz):
     """Oklab of XYZ (Ottosson's published matrices), signed cube root."""
     import torch
-    m1 = torch.tensor([[0.8189330101, 0.3618667424, -0.1288597137],
-                       [0.0329845436, 0.9293118715, 0.0361456387],
-                       [0.0482003018, 0.2643662691, 0.6338517070]], dtype=xyz.dtype, device=xyz.device)
-    m2 = torch.tensor([[0.2104542553, 0.7936177850, -0.0040720468],
-                       [1.9779984951, -2.4285922050, 0.4505937099],
-                       [0.0259040371, 0.7827717662, -0.8086757660]], dtype=xyz.dtype, device=xyz.device)
+    m1 = torch.tensor(_OKLAB_M1, dtype=xyz.dtype, device=xyz.device)
+    m2 = torch.tensor(_OKLAB_M2, dtype=xyz.dtype, device=xyz.device)
     lms = xyz @ m1.T
     lms = torch.sign(lms) * lms.abs().pow(1.0 / 3.0)
     return lms @ m2.T
@@ -171,6 +175,15 @@ class PrimaryFitConfig:
     # is met by two pairs of coincident bands on smooth sky spectra
     min_spacing_nm: float = 10.0
     spacing_weight: float = 1e-3
+    # what the fit minimises: "oklab", the mean squared Oklab distance of the
+    # reconstruction (the rmse term of the reference optimizer's score, with XYZ
+    # scaled by the targets' 99th-percentile Y as the score scales it), or "xyz",
+    # the relative squared XYZ error.  The XYZ error is dominated by the bright
+    # pixels, the Oklab distance (a cube root) weighs the dark ones too.  The cube
+    # root is smoothed below oklab_epsilon (x (x^2 + eps^2)^(-1/3)) so that the
+    # gradient of the noisy 32-spp reconstructions stays finite near zero.
+    loss: str = "oklab"
+    oklab_epsilon: float = 1e-3
 
     @property
     def elevations(self) -> np.ndarray:
@@ -237,6 +250,41 @@ def target_xyz(cfg: PrimaryFitConfig):
 
 def _loss(xyz_hat, target, keep):
     return (keep * (xyz_hat - target) ** 2).sum() / (keep * target ** 2).sum()
+
+
+def oklab_smooth(xyz, eps: float):
+    """xyz_to_oklab with the signed cube root replaced by x (x^2 + eps^2)^(-1/3)
+    (equal to it for |x| >> eps, linear through zero)."""
+    import torch
+    m1 = torch.tensor(_OKLAB_M1, dtype=xyz.dtype, device=xyz.device)
+    m2 = torch.tensor(_OKLAB_M2, dtype=xyz.dtype, device=xyz.device)
+    lms = xyz @ m1.T
+    lms = lms * (lms * lms + eps * eps).pow(-1.0 / 3.0)
+    return lms @ m2.T
+
+
+class Objective:
+    """The fit's loss of a reconstruction xyz_hat [E, P, 3] against the targets
+    (PrimaryFitConfig.loss), over the pixels `keep` selects."""
+
+    def __init__(self, cfg: "PrimaryFitConfig", target, keep):
+        import torch
+        self.kind, self.target, self.keep = cfg.loss, target, keep
+        if self.kind not in ("oklab", "xyz"):
+            raise ValueError(f"unknown fit loss {self.kind!r}")
+        if self.kind == "oklab":
+            sel = keep[:, 0].bool()
+            y = torch.sort(target[:, sel, 1].reshape(-1)).values
+            self.scale = max(_percentile_sorted(y, 0.99), 1e-12)
+            self.eps = cfg.oklab_epsilon
+            self.lab = oklab_smooth(target / self.scale, self.eps)
+            self.count = float(keep.sum()) * target.shape[0]
+
+    def __call__(self, xyz_hat):
+        if self.kind == "xyz":
+            return _loss(xyz_hat, self.target, self.keep)
+        d = oklab_smooth(xyz_hat / self.scale, self.eps) - self.lab
+        return (self.keep * d * d).sum() / self.count
 
 
 def _schedule(opt, cfg: PrimaryFitConfig, iterations: int):
@@ -317,6 +365,7 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
                                           model.multipliers(lam), sun=s).reshape(-1, scene.band_count)
                               for s in suns]).double()
     keep = cfg.keep()
+    objective = Objective(cfg, target, keep)
     matrix = _initial_matrix(films0, target, keep).clone().requires_grad_(True)
     scale = float(matrix.detach().abs().mean())
     opt = torch.optim.Adam([{"params": [lam], "lr": cfg.lr_nm},
@@ -334,7 +383,7 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
         k = model.multipliers(lam)
         films = torch.stack([render_film(r, layer, k, sun=s, decorrelate=True).reshape(-1, scene.band_count)
                              for s in suns])
-        loss = _loss(films.double() @ matrix, target, keep) + spacing_penalty(lam, cfg)
+        loss = objective(films.double() @ matrix) + spacing_penalty(lam, cfg)
         loss.backward()
         opt.step()
         sched.step()
@@ -360,6 +409,7 @@ def fit_finite_differences(cfg: PrimaryFitConfig, target, iterations=None, log_e
     t_setup = time.perf_counter()
     films0 = render_band_films(_scene_at(cfg, cfg.primaries_nm), cfg, cfg.fit_spp, cfg.seed)[0]
     keep = cfg.keep()
+    objective = Objective(cfg, target, keep)
     matrix = _initial_matrix(films0, target, keep).clone().requires_grad_(True)
     scale = float(matrix.detach().abs().mean())
     opt = torch.optim.Adam([{"params": [lam], "lr": cfg.lr_nm},
@@ -375,7 +425,7 @@ def fit_finite_differences(cfg: PrimaryFitConfig, target, iterations=None, log_e
         l_now = lam.detach().cpu().numpy()
         films = render_band_films(_scene_at(cfg, l_now), cfg, cfg.fit_spp, seed)[0]
         opt.zero_grad()
-        loss = _loss(films @ matrix, target, keep)
+        loss = objective(films @ matrix)
         loss.backward()  # dLoss/dM
         grad = np.zeros(len(l_now))
         with torch.no_grad():
@@ -385,7 +435,7 @@ def fit_finite_differences(cfg: PrimaryFitConfig, target, iterations=None, log_e
                     one = render_band_films(_scene_at(cfg, [l_now[kk] + sign * h]), cfg, cfg.fit_spp, seed)[0]
                     f = films.clone()
                     f[..., kk] = one[..., 0]
-                    js.append(float(_loss(f @ matrix, target, keep)))
+                    js.append(float(objective(f @ matrix)))
                 grad[kk] = (js[0] - js[1]) / (2 * h)
         lam.grad = torch.as_tensor(grad, dtype=torch.float64, device="cuda")
         lam_p = lam.detach().clone().requires_grad_(True)

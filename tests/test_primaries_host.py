@@ -73,3 +73,29 @@ def test_spacing_penalty_pushes_close_primaries_apart():
     assert g[0] > 0 > g[1] and g[2] > 0 > g[3]
     off = PrimaryFitConfig(min_spacing_nm=0.0)
     assert float(spacing_penalty(lam.detach(), off)) == 0.0
+
+
+def test_oklab_objective_matches_score_and_stays_finite():
+    from sky_cuda.primaries import Objective, PrimaryFitConfig, oklab_smooth
+    gen = torch.Generator().manual_seed(7)
+    # away from zero the smoothed cube root is the exact one
+    xyz = torch.rand(500, 3, generator=gen, dtype=torch.float64) * 0.8 + 0.2
+    np.testing.assert_allclose(oklab_smooth(xyz, 1e-6).numpy(), xyz_to_oklab(xyz).numpy(), rtol=1e-9, atol=1e-9)
+    # the objective of two elevations x 40 pixels, pixel 0 of each row left out
+    cfg = PrimaryFitConfig(width=8, height=5)
+    target = torch.rand(2, 40, 3, generator=gen, dtype=torch.float64)
+    keep = (torch.arange(40) % 8 >= 1).to(torch.float64)[:, None]
+    obj = Objective(cfg, target, keep)
+    assert float(obj(target)) == 0.0
+    # it is the mean squared Oklab distance with XYZ scaled by the targets' p99 Y
+    # (the rmse term of the score, squared), here where no LMS value is near zero
+    xyz_hat = target * 1.05 + 0.01
+    sel = keep[:, 0].bool()
+    ref = oklab_score(xyz_hat[:, sel], target[:, sel])["rmse"] ** 2
+    assert float(obj(xyz_hat)) == pytest.approx(ref, rel=2e-3)
+    # finite gradients through reconstructions at and below zero
+    xyz_hat = torch.zeros(2, 40, 3, dtype=torch.float64, requires_grad=True)
+    obj(xyz_hat - 1e-9).backward()
+    assert torch.all(torch.isfinite(xyz_hat.grad))
+    with pytest.raises(ValueError):
+        Objective(PrimaryFitConfig(width=8, height=5, loss="l1"), target, keep)
