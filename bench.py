@@ -85,7 +85,7 @@ def parse_args():
     p.add_argument("--tuning", default="",
                    help="SkyTuning fields set before autotuning, e.g. variant=0,crossing_cost=0.25")
     p.add_argument("--tracking", type=int, default=2, help="SkyTracking (2 = residual carry, merged layers)")
-    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--e2e-steps", type=int, default=4)
     p.add_argument("--no-peak", action="store_true", help="skip the SGEMM FP32-peak measurement")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
