@@ -104,6 +104,10 @@ class AdjointRenderer:
         self.param_count = int(self.lib.sky_cuda_adjoint_param_count(gs.handle))
         self.layers = (self.param_count - 2) // PARAMS_PER_LAYER
         self._status = torch.zeros(1, dtype=torch.int32, device="cuda")
+        # render_film's forward and backward wait for the GPU and read the watchdog
+        # status after every call; a caller that queues many calls (one per sun
+        # elevation, say) sets this to False and calls check_status() once after them
+        self.check_each_call = True
 
     def _params(self, layer, band, sample_layer=None, sample_band=None, sun=None) -> SkyAdjointParams:
         for name, t, n in (("layer_params", layer, self.param_count), ("sample_layer_params", sample_layer,
@@ -122,6 +126,11 @@ class AdjointRenderer:
         p.sun_direction = (ctypes.c_float * 3)(*(sun if sun is not None else (0.0, 0.0, 0.0)))
         p.estimator = self.estimator
         return p
+
+    def check_status(self) -> None:
+        """Wait for the queued calls and raise RenderWatchdog if any of them
+        tripped the path watchdog since the last check."""
+        self._check_status()
 
     def _check_status(self) -> None:
         import torch
@@ -206,7 +215,7 @@ def _autograd_function():
         def forward(ctx, layer, band, renderer, sun, decorrelate):
             layer_c = layer.detach().contiguous()
             band_c = band.detach().contiguous() if band is not None else None
-            out = renderer.forward(layer_c, band_c, sun=sun)
+            out = renderer.forward(layer_c, band_c, sun=sun, check_status=renderer.check_each_call)
             ctx.renderer = renderer
             ctx.sun = sun
             ctx.decorrelate = decorrelate
@@ -221,7 +230,8 @@ def _autograd_function():
             band_c = band_c if ctx.has_band else None
             want_layer = ctx.needs_input_grad[0] or band_c is None
             lg, bg = ctx.renderer.backward(layer_c, band_c, grad_film.contiguous(), sun=ctx.sun,
-                                           decorrelate=ctx.decorrelate, layer_grad=want_layer)
+                                           decorrelate=ctx.decorrelate, layer_grad=want_layer,
+                                           check_status=ctx.renderer.check_each_call)
             gl = lg.to(layer_c.dtype).reshape(layer_c.shape) if lg is not None else None
             gb = bg.to(band_c.dtype).reshape(band_c.shape) if bg is not None else None
             return gl, gb, None, None, None

@@ -379,12 +379,14 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
         # the backward pass traces its own samples: the L2 loss's gradient is
         # then free of the film noise's correlation with its derivative
         r = AdjointRenderer(gs, cfg.render_config(cfg.fit_spp, cfg.seed + 1 + it))
+        r.check_each_call = False  # the elevations' renders queue back to back; one check per step
         opt.zero_grad()
         k = model.multipliers(lam)
         films = torch.stack([render_film(r, layer, k, sun=s, decorrelate=True).reshape(-1, scene.band_count)
                              for s in suns])
         loss = objective(films.double() @ matrix) + spacing_penalty(lam, cfg)
         loss.backward()
+        r.check_status()
         opt.step()
         sched.step()
         with torch.no_grad():
