@@ -95,6 +95,8 @@ def parse_args():
     p.add_argument("--fit-summary-iterations", type=int, default=60,
                    help="Adam steps of the cut-down fit in the default line (0 leaves the fit block out)")
     p.add_argument("--no-sweep", action="store_true", help="leave the elevation-sweep block out")
+    p.add_argument("--equal-slabs", action="store_true",
+                   help="N > 1: equal-row slabs instead of the cost-balanced ones of a pilot render")
     p.add_argument("--no-adjoint-checks", action="store_true",
                    help="time the differentiable render only (no gradient checks)")
     return p.parse_args()
@@ -733,7 +735,8 @@ def main():
     import torch.distributed as dist
     from sky_cuda import GpuScene, render
     from sky_cuda import _abi
-    from sky_cuda.parallel import gather_to_rank0, max_over_ranks, slab_config
+    from sky_cuda.parallel import (balanced_row_slabs, broadcast_object, broadcast_slabs, gather_to_rank0,
+                                   max_over_ranks, pilot_row_costs, slab_config)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -745,13 +748,25 @@ def main():
     w = WORKLOADS[args.workload]
     scene = make_scene(w)
     full = make_config(w, args)
-    # one render split into contiguous pixel-row slabs, one per rank (the whole image at N = 1)
-    cfg = slab_config(full, rank, world)
+    gs = apply_tuning(GpuScene(scene), args)
+    # one render split into contiguous pixel-row slabs, one per rank (the whole image at N = 1):
+    # slabs of equal cost from rank 0's pilot render, broadcast to every rank
+    slabs, slab_log = None, "whole image"
+    if world > 1:
+        if args.equal_slabs:
+            slab_log = "equal rows"
+        else:
+            if rank == 0:
+                t0 = time.perf_counter()
+                slabs = balanced_row_slabs(pilot_row_costs(gs, full), world)
+                slab_log = f"cost-balanced: pilot of 16 row blocks at 32 spp on rank 0, {time.perf_counter() - t0:.2f} s"
+            slabs = broadcast_slabs(slabs)
+            slab_log = broadcast_object(slab_log)
+    cfg = slab_config(full, rank, world, slabs)
     B = scene.band_count
     cells = cfg.pixels * B
     full_chains = full.pixels * B * full.spp
 
-    gs = apply_tuning(GpuScene(scene), args)
     tuning_log = None
     if not args.no_autotune:
         from sky_cuda.autotune import DEFAULT_SPACE, autotune
@@ -864,7 +879,7 @@ def main():
             "config": workload_config(args.workload, w, world),
             "algorithm": {"tracking": TRACKING_NAMES[cfg.tracking],
                           "kernel": ("wavefront", "plain", "wavefront")[cfg.kernel],
-                          "slab_rows": [cfg.row_begin, cfg.rows], "tuning": gs.get_tuning(),
+                          "slab_rows": [cfg.row_begin, cfg.rows], "slabs": slab_log, "tuning": gs.get_tuning(),
                           "autotune": tuning_log},
             "e2e": {"value": full_chains / e2e_s if e2e_times else None, "unit": "chains/s",
                     "h2d_bytes_per_step": int(desc_bytes),

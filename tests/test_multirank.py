@@ -60,18 +60,22 @@ def _worker(rank, world, port, q):
     for p in (os.path.join(here, "..", "sky-tracer_gb300"), os.path.join(here, "..", "oracle"), here):
         sys.path.insert(0, p)
     import torch.distributed as dist
-    from sky_cuda.parallel import elevation_shard, gather_to_rank0, max_over_ranks, render_split
+    from sky_cuda.parallel import (balanced_row_slabs, broadcast_slabs, elevation_shard, gather_to_rank0,
+                                   max_over_ranks, render_split)
     from sky_cuda.sweep import elevation_schedule
     dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
     scene, cfg = _scene_and_config()
     fake = render_split(lambda c: fake_slab(c, 3), cfg, rank, world, 3)
-    orc = render_split(lambda c: oracle_slab(scene, c), cfg, rank, world, scene.band_count)
+    # cost-balanced slabs: rank 0 alone knows the row costs (its pilot) and broadcasts the cut
+    slabs = balanced_row_slabs([5.0, 1.0, 1.0, 1.0, 1.0], world) if rank == 0 else None
+    slabs = broadcast_slabs(slabs)
+    orc = render_split(lambda c: oracle_slab(scene, c), cfg, rank, world, scene.band_count, slabs=slabs)
     elev = elevation_schedule(32)
     mine = [float(elev[i]) for i in elevation_shard(len(elev), rank, world)]
     sweep = gather_to_rank0(mine)
     t = max_over_ranks(1.0 + rank)
     if rank == 0:
-        q.put((t, fake, orc, sweep))
+        q.put((t, fake, orc, sweep, slabs))
     dist.barrier()
     dist.destroy_process_group()
 
@@ -89,8 +93,9 @@ def test_two_rank_row_split_equals_whole_render():
     for p in procs:
         p.join(timeout=180)
         assert p.exitcode == 0
-    t, fake, orc, sweep = q.get()
+    t, fake, orc, sweep, slabs = q.get()
     assert t == 2.0
+    assert slabs == [(0, 1), (1, 4)]  # the costly first row alone on rank 0
     scene, cfg = _scene_and_config()
     np.testing.assert_array_equal(fake, fake_slab(cfg, 3))
     whole, _, _, _ = sky_oracle.render(scene, cfg, threads=1)
@@ -118,3 +123,37 @@ def test_row_slabs_partition_the_image():
     assert [list(elevation_shard(5, r, 2)) for r in range(2)] == [[0, 1, 2], [3, 4]]
     with pytest.raises(ValueError):
         elevation_shard(5, 2, 2)
+
+
+def test_balanced_slabs_minimise_the_largest_slab():
+    import itertools
+    from sky_cuda import RenderConfig
+    from sky_cuda.parallel import balanced_row_slabs, slab_config
+    rng = np.random.default_rng(3)
+    for trial in range(60):
+        height = int(rng.integers(1, 11))
+        world = int(rng.integers(1, height + 1))
+        cost = rng.choice([0.0, 0.5, 1.0, 3.0, 10.0], size=height)
+        slabs = balanced_row_slabs(cost, world)
+        assert len(slabs) == world and slabs[0][0] == 0 and all(n >= 1 for _, n in slabs)
+        assert all(b1 == b0 + n0 for (b0, n0), (b1, _) in zip(slabs, slabs[1:]))
+        assert sum(n for _, n in slabs) == height
+        got = max(cost[b:b + n].sum() for b, n in slabs)
+        best = min(max(cost[a:b].sum() for a, b in zip((0,) + cuts, cuts + (height,)))
+                   for cuts in itertools.combinations(range(1, height), world - 1))
+        assert got <= best * (1 + 1e-9) + 1e-12, (cost, world, slabs)
+    # the panorama's profile: the ground rows cost ~2.6x the sky rows
+    cost = np.repeat([1.0, 2.6], 128)
+    slabs = balanced_row_slabs(cost, 4)
+    parts = [cost[b:b + n].sum() for b, n in slabs]
+    assert max(parts) / (cost.sum() / 4) < 1.01
+    for bad in ([1.0, -1.0], [np.nan, 1.0]):
+        with pytest.raises(ValueError):
+            balanced_row_slabs(bad, 1)
+    with pytest.raises(ValueError):
+        balanced_row_slabs([1.0], 2)
+    cfg = RenderConfig(width=4, height=10, spp=1)
+    assert slab_config(cfg, 1, 2, [(0, 3), (3, 7)]).row_begin == 3
+    for bad in ([(0, 3), (4, 6)], [(0, 3)], [(0, 0), (0, 10)], [(1, 3), (4, 6)]):
+        with pytest.raises(ValueError):
+            slab_config(cfg, 0, len(bad), bad)
