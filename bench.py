@@ -313,12 +313,13 @@ def sweep_report(args, steps, warmup, rank=0, world=1):
     """Batched elevation sweep (one wavefront launch of 32 jobs replayed as a
     CUDA graph, per-elevation budgets) against 32 separate plain-kernel
     launches and 32 separate single-job wavefront launches.  Under N ranks
-    each renders a contiguous block of whole elevations (the budgets come from
-    a pilot of all elevations, the same on every rank)."""
+    each renders whole elevations, dealt out by their sample budgets (from a
+    pilot of all elevations) so that the ranks' totals are close; rank 0's
+    assignment is broadcast to all."""
     import torch
     from sky_cuda import GpuScene, RenderConfig, synthetic_scene, wavelengths
     from sky_cuda import _abi
-    from sky_cuda.parallel import elevation_shard, max_over_ranks
+    from sky_cuda.parallel import balanced_shards, broadcast_object, max_over_ranks
     from sky_cuda.sweep import Sweep, elevation_schedule, p95_relative_error, plan_budgets, spp_for_target
     scene = synthetic_scene(wavelengths(380.0, 780.0, 40), DATA_DIR, sun_elevation_deg=10.0)
     base = RenderConfig(width=256, height=128, spp=64, phase_sampling=_abi.PHASE_TABULATED,
@@ -327,8 +328,12 @@ def sweep_report(args, steps, warmup, rank=0, world=1):
     stream = torch.cuda.current_stream().cuda_stream
     gs = apply_tuning(GpuScene(scene), args)
     all_budgets, pilot_p95 = plan_budgets(gs, base, all_elev, pilot_spp=16)
-    mine = elevation_shard(len(all_elev), rank, world)
-    elevations, budgets = all_elev[mine.start:mine.stop], all_budgets[mine.start:mine.stop]
+    # the twilight elevations need up to 16x the samples of the high ones: equal-count blocks
+    # would leave rank 0 with ~40 % of the work at N = 8
+    shards = broadcast_object(balanced_shards(all_budgets, world) if rank == 0 else None) if world > 1 else None
+    mine = shards[rank] if shards else list(range(len(all_elev)))
+    elevations = np.asarray(all_elev)[mine]
+    budgets = np.asarray(all_budgets)[mine]
     seeded = RenderConfig(**{**base.__dict__, "seed": 0x5EC7_2026_0430})
     sweep = Sweep(gs, seeded, elevations, budgets)
     sweep.capture()
@@ -397,7 +402,7 @@ def sweep_report(args, steps, warmup, rank=0, world=1):
     speed_vs_plain = t_plain_budget / t_batched
     rep = {
         "elevations": [round(float(e), 3) for e in elevations], "spp_per_elevation": [int(b) for b in budgets],
-        "pilot_spp": 16, "pilot_p95": [round(float(p), 5) for p in pilot_p95[mine.start:mine.stop]],
+        "pilot_spp": 16, "pilot_p95": [round(float(pilot_p95[i]), 5) for i in mine],
         "batched_graph_s": t_batched, "batched_chains": chains_batched,
         "batched_chains_per_s": chains_batched / t_batched,
         "batched_p95_error_max": max(errs_batched), "batched_p95_error": [round(x, 5) for x in errs_batched],

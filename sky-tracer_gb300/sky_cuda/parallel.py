@@ -10,8 +10,9 @@ order.  Pixels keep their whole-image index in the random-number counter, so
 the concatenation is the whole render: bit-identical with the plain kernel,
 equal to FP64 rounding of the cell sums with the wavefront kernel.  The
 reference's sweep is a loop over elevations
-(scripts/bake_skyview_elevations.ps1:16-35); a sweep is cut into contiguous
-blocks of whole elevations.
+(scripts/bake_skyview_elevations.ps1:16-35); a sweep is dealt out in whole
+elevations, by sample budget (balanced_shards), or in contiguous blocks
+(elevation_shard).
 
 Rows do not cost the same: on a panorama the rows below the horizon (camera
 rays that reach the ground, then ground NEE and continuations) cost about 2.6
@@ -156,6 +157,25 @@ def elevation_shard(count: int, rank: int, world: int) -> range:
     base, extra = divmod(count, world)
     begin = rank * base + min(rank, extra)
     return range(begin, begin + base + (1 if rank < extra else 0))
+
+
+def balanced_shards(costs, world: int) -> list[list[int]]:
+    """Whole items (e.g. a sweep's elevations) of the given costs dealt to
+    `world` ranks, largest first to the least loaded rank (the LPT rule: the
+    largest load is at most 4/3 of the optimum); each rank's indices in
+    ascending order."""
+    c = np.asarray(costs, dtype=np.float64).reshape(-1)
+    if world < 1:
+        raise ValueError(f"world size must be positive, got {world}")
+    if not np.all(np.isfinite(c)) or np.any(c < 0.0):
+        raise ValueError("costs must be finite and non-negative")
+    load = [0.0] * world
+    shards = [[] for _ in range(world)]
+    for i in sorted(range(c.size), key=lambda k: (-c[k], k)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        shards[r].append(i)
+        load[r] += c[i]
+    return [sorted(sh) for sh in shards]
 
 
 def concat_slabs(slabs, width: int, channels: int) -> np.ndarray:

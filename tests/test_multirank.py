@@ -157,3 +157,21 @@ def test_balanced_slabs_minimise_the_largest_slab():
     for bad in ([(0, 3), (4, 6)], [(0, 3)], [(0, 0), (0, 10)], [(1, 3), (4, 6)]):
         with pytest.raises(ValueError):
             slab_config(cfg, 0, len(bad), bad)
+
+
+def test_balanced_shards_deal_whole_elevations():
+    from sky_cuda.parallel import balanced_shards
+    # the sweep's pilot budgets: twilight elevations need up to 16x the samples
+    budgets = [992, 1024, 1024, 1024, 1024, 1024, 1024, 672, 352, 192, 160, 128, 96, 96, 96, 96] + [64] * 16
+    for world in (1, 2, 4, 8, 32, 40):
+        shards = balanced_shards(budgets, world)
+        assert len(shards) == world
+        assert sorted(i for sh in shards for i in sh) == list(range(len(budgets)))
+        assert all(sh == sorted(sh) for sh in shards)
+        loads = [sum(budgets[i] for i in sh) for sh in shards]
+        # LPT: within 4/3 of the lower bound on the optimum
+        assert max(loads) <= 4.0 / 3.0 * max(max(budgets), sum(budgets) / world) + 1e-9
+    loads8 = [sum(budgets[i] for i in sh) for sh in balanced_shards(budgets, 8)]
+    assert sum(budgets) / (8 * max(loads8)) > 0.95
+    with pytest.raises(ValueError):
+        balanced_shards([1.0, -2.0], 2)
