@@ -415,6 +415,21 @@ cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
     if (smem > 48u * 1024u &&
         (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
         return e;
+    // Prefer the smallest shared-memory carveout that holds kMinBlocks blocks' tables: the
+    // rest of the SM's L1/shared array caches the phase tables, extinction rows and merged
+    // grid (the largest carveout costs 6 % on the production render).  A hint: if the
+    // driver refuses it, the launch goes ahead with its own choice.
+    int smem_sm = 0, reserved = 0;
+    if (cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess &&
+        smem_sm > 0) {
+        const size_t need = size_t(kMinBlocks) * (smem + size_t(reserved));
+        const int pct = int(std::min<size_t>(100u, (need * 100u + size_t(smem_sm) - 1u) / size_t(smem_sm)));
+        if (cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, std::max(pct, 1)) != cudaSuccess)
+            (void)cudaGetLastError();  // clear the refused hint so the launch check does not see it
+    } else {
+        (void)cudaGetLastError();
+    }
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kWaveThreads, smem)) != cudaSuccess) return e;
     per_sm = std::max(per_sm, 1);
     if (w.max_blocks_per_sm) per_sm = std::min(per_sm, int(w.max_blocks_per_sm));
