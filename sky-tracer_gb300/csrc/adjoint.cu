@@ -624,19 +624,23 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                 const uint32_t need = __ballot_sync(0xffffffffu, next == kNextIdle);
                 if (need == 0u || exhausted) break;
                 if (claim_next >= L.spp) {
+                    // claims run band-major, as in the wavefront tracer (the warps of an SM
+                    // share a band's tables in L1); cells keep the pixel-major layout
+                    const uint32_t npix = L.width * L.rows;
                     uint32_t cn = 0u;
                     if (lane == 0u) {
                         do cn = atomicAdd(next_cell, 1u);
-                        while (kGrad && cn < cells && __ldg(dloss + cn) == 0.0f);  // no loss: no gradient
+                        while (kGrad && cn < cells &&
+                               __ldg(dloss + (cn % npix) * L.band_count + cn / npix) == 0.0f);  // no loss: no gradient
                     }
                     cn = __shfl_sync(0xffffffffu, cn, 0);
                     if (cn >= cells) {
                         exhausted = true;
                         break;
                     }
-                    claim_cell = cn;
-                    const uint32_t pixel = cn / L.band_count;
-                    claim_band = cn - pixel * L.band_count;
+                    claim_band = cn / npix;
+                    const uint32_t pixel = cn - claim_band * npix;
+                    claim_cell = pixel * L.band_count + claim_band;
                     const uint32_t row = pixel / L.width;  // row within the slab
                     claim_x = pixel - row * L.width;
                     claim_y = row + L.row_begin;

@@ -176,8 +176,15 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 }
                 claim_job = job_of(jobs, num_jobs, gc);
                 const uint32_t c = gc - __ldg(&jobs[claim_job].cell_begin);
-                const uint32_t pixel = c / S.band_count, width = __ldg(&jobs[claim_job].L.width);
-                claim_band = c - pixel * S.band_count;
+                // claims run band-major (all pixels of a band, then the next band), so the
+                // warps of an SM work on one or two bands at a time and that band's
+                // extinction row, merged grid and phase rows stay in L1 (-0.9 % on the
+                // production render, -4 % on a 128x64 one); the sums keep their
+                // pixel-major, band-minor layout
+                const uint32_t width = __ldg(&jobs[claim_job].L.width);
+                const uint32_t npix = width * __ldg(&jobs[claim_job].L.rows);
+                claim_band = c / npix;
+                const uint32_t pixel = c - claim_band * npix;
                 const uint32_t row = pixel / width;  // row within the job's slab
                 claim_x = pixel - row * width;
                 claim_y = row + __ldg(&jobs[claim_job].L.row_begin);
