@@ -507,10 +507,13 @@ __global__ void __launch_bounds__(256) adjoint_primal_kernel(const __grid_consta
                                                              unsigned long long* __restrict__ counters,
                                                              uint32_t* __restrict__ status, uint64_t cells) {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
-    const uint32_t band = uint32_t(cell % L.band_count);
-    const uint64_t pixel = cell / L.band_count;  // pixel of the slab; y is the image row
+    const uint64_t q = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (q >= cells) return;  // whole warps only: blockDim is a multiple of 32
+    // band-major warps, pixel-major cells (as the plain tracer)
+    const uint64_t npix = cells / L.band_count;
+    const uint32_t band = uint32_t(q / npix);
+    const uint64_t pixel = q - uint64_t(band) * npix;  // pixel of the slab; y is the image row
+    const uint64_t cell = pixel * L.band_count + band;
     const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width) + L.row_begin;
     const AdjSet P = resolve(A.P, A.S.layer_count, band);
     const AdjSet Q = A.distinct ? resolve(A.Q, A.S.layer_count, band) : P;

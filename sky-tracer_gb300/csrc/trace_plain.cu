@@ -140,10 +140,14 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch 
                                                           uint32_t* __restrict__ status, uint64_t cells,
                                                           uint32_t accumulate) {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t cell = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (cell >= cells) return;  // whole warps only: blockDim is a multiple of 32
-    const uint32_t band = uint32_t(cell % L.band_count);
-    const uint64_t pixel = cell / L.band_count;  // pixel of the slab; y is the image row
+    const uint64_t q = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (q >= cells) return;  // whole warps only: blockDim is a multiple of 32
+    // warps run band-major (consecutive warps: consecutive pixels of one band), so the
+    // resident warps share one band's tables in L1; the cells keep the pixel-major layout
+    const uint64_t npix = cells / L.band_count;
+    const uint32_t band = uint32_t(q / npix);
+    const uint64_t pixel = q - uint64_t(band) * npix;  // pixel of the slab; y is the image row
+    const uint64_t cell = pixel * L.band_count + band;
     const uint32_t x = uint32_t(pixel % L.width), y = uint32_t(pixel / L.width) + L.row_begin;
     Counters n;
     n.clear();
