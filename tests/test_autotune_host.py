@@ -51,8 +51,8 @@ def test_autotune_keeps_the_fastest(fake_timing):
     assert best["variant"] == 0 and best["crossing_cost"] == 0.5
     assert gs.get_tuning() == best
     assert sorted(ms for _, ms in trials)[0] == _cost(best)
-    # the probe is the caller's image at spp / 8 from sample 0, without flags
-    assert all(p.spp == 32 and p.sample_offset == 0 and p.flags == 0 and p.width == 64 for p in fake_timing)
+    # the probe is the caller's image at spp / 8 (at least 64) from sample 0, without flags
+    assert all(p.spp == 64 and p.sample_offset == 0 and p.flags == 0 and p.width == 64 for p in fake_timing)
 
 
 def test_autotune_restores_the_shape_when_not_applying(fake_timing):
@@ -63,8 +63,8 @@ def test_autotune_restores_the_shape_when_not_applying(fake_timing):
     assert best["crossing_cost"] == 0.25 and best["variant"] == before["variant"]
     assert gs.get_tuning() == before
     assert [t["crossing_cost"] for t, _ in trials] == [0.25, 1.0]
-    # small renders probe at least 4 samples
-    assert all(p.spp == 4 for p in fake_timing)
+    # below 64 spp the probe is the whole render
+    assert all(p.spp == 16 for p in fake_timing)
 
 
 def test_autotune_probe_spp_override(fake_timing):
