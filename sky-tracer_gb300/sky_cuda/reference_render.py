@@ -53,7 +53,7 @@ def parse_args(argv=None):
     p.add_argument("--png-exposure", type=float, default=0.05)
     p.add_argument("--sky-view-lut", action="store_true")
     p.add_argument("--rebuild-rgb-only", action="store_true")
-    # extensions of this build (the reference's behaviour when left at their defaults)
+    # flags the reference CLI does not have (its behaviour when left at their defaults)
     p.add_argument("--mie-g", type=float, default=0.76,
                    help="HG asymmetry of the phase tables used when data/mie_phase.csv is absent")
     p.add_argument("--phase-sampling", choices=("isotropic", "tabulated"), default="isotropic")
