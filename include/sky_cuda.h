@@ -158,6 +158,11 @@ typedef enum SkyKernel {
  * (progressive rendering; the reference accumulates 2-spp dispatches the
  * same way, integrator.rs:252-283). */
 #define SKY_FLAG_ACCUMULATE 1u
+/* Fill SkyRenderStats.events in sky_cuda_render / _xyz / _rgb.  The kernels
+ * that count events run ~3 % slower, so without this flag the events are
+ * left zero.  (sky_cuda_render_device counts into SkyDeviceOutputs.counters
+ * whenever that pointer is given.) */
+#define SKY_FLAG_COUNT_EVENTS 2u
 
 /*
  * = RenderConfig (config.rs:2-12) followed by extensions.  A config whose
@@ -212,7 +217,7 @@ typedef struct SkyRenderStats {
     double kernel_ms;       /* device time of the tracing kernel(s), CUDA events */
     double total_ms;        /* host wall time of the call                         */
     uint64_t chains;        /* pixel x band x sample paths traced                 */
-    uint64_t events[SKY_EVENT_COUNT];  /* counted only when stats are requested */
+    uint64_t events[SKY_EVENT_COUNT];  /* counted only with SKY_FLAG_COUNT_EVENTS, else 0 */
     uint32_t watchdog;      /* nonzero when a path reached the watchdog           */
     uint32_t kernel_used;   /* SkyKernel actually launched                         */
 } SkyRenderStats;

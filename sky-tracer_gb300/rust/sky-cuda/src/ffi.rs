@@ -15,6 +15,10 @@ pub const SKY_ERR_OUT_OF_MEMORY: c_int = 7;
 pub const SKY_ERR_LAUNCH: c_int = 8;
 pub const SKY_ERR_IO: c_int = 9;
 
+/// SkyRenderConfig.flags bits.
+pub const SKY_FLAG_ACCUMULATE: u32 = 1;
+pub const SKY_FLAG_COUNT_EVENTS: u32 = 2;
+
 /// = GpuBand (integrator.rs:79-86), 24 bytes.
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]

@@ -41,6 +41,7 @@ KERNEL_AUTO = 0
 KERNEL_PLAIN = 1
 KERNEL_WAVEFRONT = 2
 FLAG_ACCUMULATE = 1
+FLAG_COUNT_EVENTS = 2
 
 EVENT_NAMES = ("track_step", "segment", "boundary", "scatter", "nee", "ground", "chain")
 EVENT_COUNT = 8

@@ -158,33 +158,42 @@ class GpuScene:
             setattr(t, k, v)
         check(self.lib.sky_cuda_scene_set_tuning(self.handle, ctypes.byref(t)), self.lib)
 
-    def render(self, config: RenderConfig) -> tuple[Film, RenderStats]:
+    @staticmethod
+    def _c_config(config: RenderConfig, count_events: bool):
+        c = config.to_c()
+        if count_events:
+            c.flags |= _abi.FLAG_COUNT_EVENTS
+        return c
+
+    def render(self, config: RenderConfig, count_events: bool = False) -> tuple[Film, RenderStats]:
+        """Film and stats; the stats' event counts are filled with
+        count_events=True (the counting kernels run ~3 % slower)."""
         film = np.empty(config.pixels * self.band_count, dtype=np.float32)
         stats = SkyRenderStats()
-        check(self.lib.sky_cuda_render(self.handle, ctypes.byref(config.to_c()), _fptr(film), film.size,
-                                       ctypes.byref(stats)), self.lib)
+        check(self.lib.sky_cuda_render(self.handle, ctypes.byref(self._c_config(config, count_events)), _fptr(film),
+                                       film.size, ctypes.byref(stats)), self.lib)
         return Film(config.width, config.rows, self.band_count, film), RenderStats.from_c(stats)
 
-    def render_xyz(self, config: RenderConfig, with_film: bool = True):
+    def render_xyz(self, config: RenderConfig, with_film: bool = True, count_events: bool = False):
         """Film, per-pixel XYZ [pixels, 3] (FP64) and its variance, and stats."""
         film = np.empty(config.pixels * self.band_count, dtype=np.float32) if with_film else None
         xyz = np.empty((config.pixels, 3), dtype=np.float64)
         var = np.empty((config.pixels, 3), dtype=np.float64)
         stats = SkyRenderStats()
-        check(self.lib.sky_cuda_render_xyz(self.handle, ctypes.byref(config.to_c()),
+        check(self.lib.sky_cuda_render_xyz(self.handle, ctypes.byref(self._c_config(config, count_events)),
                                            _fptr(film) if film is not None else None,
                                            film.size if film is not None else 0, _dptr(xyz), _dptr(var),
                                            config.pixels, ctypes.byref(stats)), self.lib)
         f = Film(config.width, config.rows, self.band_count, film) if film is not None else None
         return f, xyz, var, RenderStats.from_c(stats)
 
-    def render_rgb(self, config: RenderConfig, with_film: bool = True):
+    def render_rgb(self, config: RenderConfig, with_film: bool = True, count_events: bool = False):
         """Film and per-pixel white-balanced linear sRGB [pixels, 3] (float32,
         from the kernel epilogue), and stats."""
         film = np.empty(config.pixels * self.band_count, dtype=np.float32) if with_film else None
         rgb = np.empty((config.pixels, 3), dtype=np.float32)
         stats = SkyRenderStats()
-        check(self.lib.sky_cuda_render_rgb(self.handle, ctypes.byref(config.to_c()),
+        check(self.lib.sky_cuda_render_rgb(self.handle, ctypes.byref(self._c_config(config, count_events)),
                                            _fptr(film) if film is not None else None,
                                            film.size if film is not None else 0, _fptr(rgb), config.pixels,
                                            ctypes.byref(stats)), self.lib)

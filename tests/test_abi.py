@@ -25,6 +25,14 @@ def test_header_and_ctypes_agree_on_functions():
     assert _declared_functions(HEADER) == sorted(_abi.declared_symbols())
 
 
+def test_header_flags_match_the_mirrors():
+    """SKY_FLAG_* of the header = the Python and Rust constants."""
+    flags = dict((k, int(v)) for k, v in re.findall(r"#define SKY_FLAG_(\w+) (\d+)u", HEADER.read_text()))
+    assert flags == {"ACCUMULATE": _abi.FLAG_ACCUMULATE, "COUNT_EVENTS": _abi.FLAG_COUNT_EVENTS}
+    rust = (ROOT / "sky-tracer_gb300" / "rust" / "sky-cuda" / "src" / "ffi.rs").read_text()
+    assert dict((k, int(v)) for k, v in re.findall(r"pub const SKY_FLAG_(\w+): u32 = (\d+);", rust)) == flags
+
+
 def test_library_exports_every_declared_symbol(lib_built):
     out = subprocess.run(["nm", "-D", "--defined-only", str(lib_built)], capture_output=True, text=True,
                          check=True).stdout

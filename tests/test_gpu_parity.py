@@ -219,7 +219,9 @@ def test_film_matches_sums_and_progressive_is_exact(gpu, dome_scene, kernel):
     cfg = RenderConfig(width=16, height=8, spp=64, phase_sampling=_abi.PHASE_TABULATED,
                        tracking=_abi.TRACKING_MERGED_LAYERS, kernel=kernel)
     with GpuScene(dome_scene) as gs:
-        film, stats = gs.render(cfg)
+        film, stats = gs.render(cfg, count_events=True)
+        _, uncounted = gs.render(cfg)  # events only on request (SKY_FLAG_COUNT_EVENTS)
+        assert all(v == 0 for v in uncounted.events.values()) and uncounted.chains == stats.chains
         s, q, _, _ = gpu_sums(gs, cfg)
         np.testing.assert_array_equal(film.values, np.maximum((s / 64).astype(np.float32), 0).ravel())
         # two progressive halves == one render, bit for bit
