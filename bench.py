@@ -400,6 +400,34 @@ def sweep_report(args, steps, warmup, rank=0, world=1):
     need_u = spp_for_target(errs_plain, [uniform] * len(elevations), 0.01)
     t1_plain_uniform = t_plain_uniform * float(need_u.max()) / uniform
     speed_vs_plain = t_plain_budget / t_batched
+
+    # where batching itself pays: small jobs (one band at 550 nm per elevation, 32 spp: ~1 M
+    # chains each), one graph replay of all of them against one single-job launch per job
+    small_scene = synthetic_scene(np.array([550.0]), DATA_DIR, sun_elevation_deg=10.0)
+    gsm = apply_tuning(GpuScene(small_scene), args)
+    small = Sweep(gsm, seeded, elevations, 32)
+    small.capture()
+    solo = [(c, sun, {**o, "status": small.status.data_ptr()}) for c, sun, o in small.jobs]
+
+    def timed_small(run, reps=5):
+        ts = []
+        for _ in range(reps + 2):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+        return max_over_ranks(statistics.median(ts[2:]))
+
+    t_small_batched = timed_small(lambda: small.replay(stream))
+    t_small_singles = timed_small(lambda: [gsm.render_batch([j], stream) for j in solo])
+    if int(small.status.item()) != 0:
+        raise SystemExit("watchdog tripped in the small-job sweep")
+    small_block = {"jobs": len(solo), "chains_per_job": small.chains // max(len(solo), 1),
+                   "batched_graph_s": t_small_batched, "single_launches_s": t_small_singles,
+                   "speedup_batching": t_small_singles / t_small_batched}
+    gsm.close()
     rep = {
         "elevations": [round(float(e), 3) for e in elevations], "spp_per_elevation": [int(b) for b in budgets],
         "pilot_spp": 16, "pilot_p95": [round(float(pilot_p95[i]), 5) for i in mine],
@@ -420,6 +448,7 @@ def sweep_report(args, steps, warmup, rank=0, world=1):
         "target_value": speed_vs_plain, "target_met": bool(speed_vs_plain >= 3.0),
         "plain_crossing_cost": round(float(plain_tuning["crossing_cost"]), 3),
         "batched_tuning": shape, "gpu_launches_per_replay": 3,
+        "small_jobs": small_block,
     }
     for g in singles:
         g.close()

@@ -53,7 +53,7 @@ def test_batch_equals_separate_renders(gpu, dome_scene):
     elevations = [-3.0, 2.0, 45.0]
     spp = [32, 64, 16]
     with GpuScene(dome_scene) as gs:
-        sweep = Sweep(gs, base, elevations, spp)
+        sweep = Sweep(gs, base, elevations, spp, count_events=True)
         sweep.launch(torch.cuda.current_stream().cuda_stream)
         torch.cuda.synchronize()
         assert int(sweep.status.item()) == 0
