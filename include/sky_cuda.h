@@ -259,7 +259,10 @@ typedef struct SkyTuning {
     uint32_t variant;            /* resident blocks of 256 threads per SM the kernel is compiled
                                     for: 0 = 3 (80 registers), 1 = 2 (128), 2 = 4 (64)         */
     uint32_t max_blocks_per_sm;  /* 0 = occupancy limit                                          */
-    uint32_t _unused[2];         /* zero                                                         */
+    uint32_t all_species;        /* 1 = the kernels evaluate all four aerosol species; 0 = only
+                                    species 0 when species 1-3 carry no aerosol anywhere in the
+                                    scene (the default: same results, fewer instructions)      */
+    uint32_t _unused;            /* zero                                                         */
     float crossing_cost;         /* merged tracking grid: cost of a layer crossing relative to a
                                     null collision; <= 0 leaves the grid as it is              */
     uint32_t iteration_limit;    /* backstop of the wavefront kernel: loop iterations (one ray

@@ -280,6 +280,7 @@ WaveLaunch wave_launch(const SkyScene* s, const DevJob& first, const DevJob* dev
     w.counters = counters;
     w.status = status;
     w.iteration_limit = s->tuning.iteration_limit;
+    w.aerosol_species = aerosol_species(first.S, s->tuning.all_species != 0u);
     return w;
 }
 
@@ -301,7 +302,8 @@ int launch_render(SkyScene* s, const SkyRenderConfig* c, const SkyDeviceOutputs*
     float* rgb = s->has_xyz ? o->rgb : nullptr;
     if (c->kernel == SKY_KERNEL_PLAIN) {
         if (timed) cudaEventRecord(s->ev_start, stream);
-        e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate, stream);
+        e = launch_trace_plain(s->dev, L, o->cell_sum, o->cell_sumsq, o->counters, o->status, accumulate,
+                               aerosol_species(s->dev, s->tuning.all_species != 0u), stream);
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "tracing kernel launch", e);
         if (timed) cudaEventRecord(s->ev_stop, stream);
         e = launch_finalize(s->dev, pixels, total_spp, o->cell_sum, o->cell_sumsq, o->film, xyz, xyz_var, rgb,
@@ -473,6 +475,7 @@ int sky_cuda_scene_set_tuning(SkyScene* s, const SkyTuning* t) {
     if (!s || !t) return set_error(SKY_ERR_INVALID_CONFIG, "scene and tuning must not be null");
     if (t->variant >= kWaveVariants) return set_error(SKY_ERR_INVALID_CONFIG, "unknown wavefront kernel variant");
     if (t->max_blocks_per_sm > 64) return set_error(SKY_ERR_INVALID_CONFIG, "max_blocks_per_sm out of range");
+    if (t->all_species > 1u) return set_error(SKY_ERR_INVALID_CONFIG, "all_species must be 0 or 1");
     if (!(t->crossing_cost <= 0.0f) && !(t->crossing_cost < 1e6f))
         return set_error(SKY_ERR_INVALID_CONFIG, "crossing_cost out of range");
     if (cudaSetDevice(s->device) != cudaSuccess) return set_error(SKY_ERR_NO_DEVICE, "cannot select the device");

@@ -298,6 +298,16 @@ struct Coeffs {  // MediumCoefficients (sky_trace.wgsl:101-106)
 
 // coefficients_at (sky_trace.wgsl:356-386) from the band-independent knot
 // profile and the per-band cross sections.
+//
+// kAer: the aerosol species evaluated, the first kAer of the four.  A kernel
+// instantiated with kAer = 1 serves scenes whose species 1-3 carry no
+// aerosol (DevScene::aerosol_mask): their terms are exactly +0 in the
+// four-species evaluation (the clamped masses are 0, or their optics are),
+// so both forms return the same bits, and the single-species one skips
+// three species' loads and arithmetic in every medium evaluation (-7.5 % on
+// a 512x256, 81-band, 256-spp render).  The phase functions below take the
+// same parameter; the species beyond kAer have sca[i] = 0.
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const Medium& M, uint32_t band, float alt) {
     Coeffs c;
     c.rayleigh = 0.0f;
@@ -317,7 +327,7 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const Mediu
     float absorption = fmaxf(ozone * B.ozone_xs, 0.0f);
     float scattering = c.rayleigh;
 #pragma unroll
-    for (int i = 0; i < int(kSpecies); ++i) {
+    for (int i = 0; i < kAer; ++i) {
         float mass = fmaxf(fmaf(dz, P.mass_slope[i], P.mass[i]), 0.0f);
         SkyAerosolOptics o = M.optics[band * kSpecies + i];
         c.sca[i] = fmaxf(mass * o.scattering_km_inv_per_g_m3, 0.0f);
@@ -331,9 +341,10 @@ __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const Mediu
 }
 
 // The same from the scene's global tables.
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ Coeffs coefficients_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
                                                   uint32_t band, float alt) {
-    return coefficients_at(S, Medium{knot_z, finder, S.profile, S.bands, S.optics}, band, alt);
+    return coefficients_at<kAer>(S, Medium{knot_z, finder, S.profile, S.bands, S.optics}, band, alt);
 }
 
 // ---- phase functions ----------------------------------------------------------------
@@ -364,18 +375,20 @@ __device__ __forceinline__ float mie_phase_u(const DevScene& S, uint32_t species
 }
 
 // mixed_phase_value (sky_trace.wgsl:496-510), at grid position u of mu.
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ float mixed_phase_u(const DevScene& S, const Coeffs& c, uint32_t band, float mu, float u) {
     if (c.scattering <= 0.0f) return 0.0f;
     float acc = c.rayleigh * rayleigh_phase(mu);
 #pragma unroll
-    for (int i = 0; i < int(kSpecies); ++i)
+    for (int i = 0; i < kAer; ++i)
         if (c.sca[i] > 0.0f) acc = fmaf(c.sca[i], mie_phase_u(S, uint32_t(i), band, u), acc);
     return acc / c.scattering;
 }
 
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ float mixed_phase(const DevScene& S, const Coeffs& c, uint32_t band, float mu) {
     if (c.scattering <= 0.0f) return 0.0f;
-    return mixed_phase_u(S, c, band, mu, phase_grid_u(mu));
+    return mixed_phase_u<kAer>(S, c, band, mu, phase_grid_u(mu));
 }
 
 // phase.rs:137-140
@@ -484,6 +497,7 @@ __device__ __forceinline__ V3 sample_cosine_hemisphere(V3 axis, Rng& rng, float&
 // Tabulated continuation (phase.rs:53-75, sampling.rs:182-185): component by
 // sigma_s,i / sigma_s, mu from its inverse CDF, and the draw for phi; returns
 // mixed_phase(mu) / mixture_pdf(mu), which does not depend on phi.
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ float tabulated_mu(const DevScene& S, const Coeffs& c, uint32_t band, Rng& rng, float& mu,
                                              float& xi_phi) {
     float target = rng.next() * c.scattering;
@@ -491,14 +505,14 @@ __device__ __forceinline__ float tabulated_mu(const DevScene& S, const Coeffs& c
     float acc = c.rayleigh;
     if (target < acc) chosen = 0;
 #pragma unroll
-    for (int i = 0; i < int(kSpecies); ++i) {
+    for (int i = 0; i < kAer; ++i) {
         acc = acc + c.sca[i];
         if (chosen < 0 && target < acc) chosen = i + 1;
     }
     if (chosen < 0) {
         chosen = 0;
 #pragma unroll
-        for (int i = 0; i < int(kSpecies); ++i)
+        for (int i = 0; i < kAer; ++i)
             if (c.sca[i] > 0.0f) chosen = i + 1;
     }
     float xi_mu = rng.next();
@@ -508,16 +522,17 @@ __device__ __forceinline__ float tabulated_mu(const DevScene& S, const Coeffs& c
     const float u = phase_grid_u(mu);  // shared by the pdf and the phase lookups
     float pdf = c.rayleigh * inv_s * rayleigh_phase(mu);
 #pragma unroll
-    for (int i = 0; i < int(kSpecies); ++i)
+    for (int i = 0; i < kAer; ++i)
         if (c.sca[i] > 0.0f) pdf = fmaf(c.sca[i] * inv_s, mie_sampling_pdf_u(S, uint32_t(i), band, u), pdf);
-    return mixed_phase_u(S, c, band, mu, u) / pdf;
+    return mixed_phase_u<kAer>(S, c, band, mu, u) / pdf;
 }
 
 // The tabulated continuation direction around `axis`; returns the weight.
+template <int kAer = int(kSpecies)>
 __device__ __forceinline__ float sample_tabulated(const DevScene& S, const Coeffs& c, uint32_t band, V3 axis,
                                                   Rng& rng, V3& out_dir) {
     float mu, xi_phi;
-    const float w = tabulated_mu(S, c, band, rng, mu, xi_phi);
+    const float w = tabulated_mu<kAer>(S, c, band, rng, mu, xi_phi);
     out_dir = direction_from_axis_mu(axis, mu, xi_phi);
     return w;
 }
@@ -600,17 +615,9 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const Medium
     float tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
     uint32_t guard = 0;
     for (;;) {
+        // the crossings up to the segment that holds the next tentative collision
         float dt = tau / maj;
-        if (t + dt < t_seg) {
-            t = t + dt;
-            ++n.e[SKY_EVENT_TRACK_STEP];
-            float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
-            if (rng.next() * maj < sig) {
-                t_hit = t;
-                return true;
-            }
-            tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
-        } else {
+        while (!(t + dt < t_seg)) {
             if (dir == 0) return false;
             if (++guard > 100000u) {
                 watchdog = true;
@@ -622,7 +629,16 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const Medium
             t_seg = merged_crossing(G, g, m, t, t_max, dir);
             maj = __ldg(G.maj + m);
             ++n.e[SKY_EVENT_SEGMENT];
+            dt = tau / maj;
         }
+        t = t + dt;
+        ++n.e[SKY_EVENT_TRACK_STEP];
+        float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
+        if (rng.next() * maj < sig) {
+            t_hit = t;
+            return true;
+        }
+        tau = -__logf(fmaxf(1.0f - rng.next(), 0.0000001f));
     }
 }
 

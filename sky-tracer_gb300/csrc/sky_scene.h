@@ -70,7 +70,8 @@ struct DevScene {
     float cos_max;           // cos(sun angular radius)
     float one_minus_cos_max;
     float light_pdf;         // 1 / (2 pi (1 - cos_max))
-    uint32_t aerosol_mask;   // bit i set when species i has mass and optics: the others add exactly 0
+    uint32_t aerosol_mask;   // bit i set when species i has mass and optics somewhere: the others add
+                             // exactly 0 to every coefficient, and the kernels skip them
     // device tables
     const float* knot_z;               // [K]
     const uint16_t* finder;            // [kFinderCells] knot interval of each cell's lower edge

@@ -9,11 +9,18 @@
 
 namespace sky {
 
+// Aerosol species the tracing kernels evaluate for a scene: 1 when species
+// 1-3 carry no aerosol (DevScene::aerosol_mask), else all four; `all_species`
+// (SkyTuning) asks for all four always.  Either count gives the same results.
+inline uint32_t aerosol_species(const DevScene& S, bool all_species) {
+    return (all_species || (S.aerosol_mask & ~1u) != 0u) ? kSpecies : 1u;
+}
+
 // Plain tracer: writes per-cell sums / sums of squares of this launch's
 // samples into cell_sum / cell_sumsq, or adds to them when `accumulate`.
 cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                unsigned long long* counters, uint32_t* status, bool accumulate,
-                               cudaStream_t stream);
+                               uint32_t aerosol_species, cudaStream_t stream);
 
 // Persistent wavefront tracer (trace_wave.cu): a ray loop with per-lane chain
 // regeneration over a job table.
@@ -31,6 +38,7 @@ struct WaveLaunch {
     uint32_t variant;              // kernel shape, < kWaveVariants
     uint32_t max_blocks_per_sm;    // 0 = as many as fit
     uint32_t tracking, phase_sampling;
+    uint32_t aerosol_species;      // 1 or kSpecies (aerosol_species())
     uint32_t* work_counter;        // reset by the launch itself
     unsigned long long* counters;  // may be null
     uint32_t* status;

@@ -31,7 +31,7 @@ __device__ __forceinline__ float shadow_transmittance(const DevScene& S, V3 pos,
 }
 
 // trace_path (sky_trace.wgsl:703-776) for one chain.
-template <int kTracking, int kPhase>
+template <int kTracking, int kPhase, int kAer>
 __device__ float trace_chain(const DevScene& S, const DevLaunch& L, uint32_t x, uint32_t y, uint32_t band,
                              uint32_t sample, Counters& n, bool& watchdog) {
     const uint32_t pixel = y * L.width + x;
@@ -58,7 +58,7 @@ __device__ float trace_chain(const DevScene& S, const DevLaunch& L, uint32_t x, 
         if (track_ray<kTracking>(S, global_medium(S), g, t_b, band, rng, t_hit, n, watchdog, false)) {
             ++n.e[SKY_EVENT_SCATTER];
             V3 pos = madd(org, dir, t_hit);
-            Coeffs c = coefficients_at(S, S.knot_z, S.finder, band, altitude_at(g, t_hit, S.ground_radius));
+            Coeffs c = coefficients_at<kAer>(S, S.knot_z, S.finder, band, altitude_at(g, t_hit, S.ground_radius));
             if (c.extinction <= 0.0f || c.scattering <= 0.0f) break;
             throughput *= fminf(fmaxf(c.scattering / c.extinction, 0.0f), 1.0f);
             if (throughput <= 0.0f) break;
@@ -68,15 +68,15 @@ __device__ float trace_chain(const DevScene& S, const DevLaunch& L, uint32_t x, 
                 V3 ldir = sample_sun_cone(S, rng);
                 ++n.e[SKY_EVENT_NEE];
                 float trans = shadow_transmittance<kTracking>(S, pos, ldir, band, rng, n, watchdog);
-                if (trans > 0.0f) nee += l_sun * trans * mixed_phase(S, c, band, dot3(dir, ldir)) / S.light_pdf;
+                if (trans > 0.0f) nee += l_sun * trans * mixed_phase<kAer>(S, c, band, dot3(dir, ldir)) / S.light_pdf;
             }
             radiance += throughput * (nee * inv_lights);
             V3 new_dir;
             if (kPhase == SKY_PHASE_TABULATED) {
-                throughput *= sample_tabulated(S, c, band, dir, rng, new_dir);
+                throughput *= sample_tabulated<kAer>(S, c, band, dir, rng, new_dir);
             } else {
                 new_dir = sample_isotropic(rng);
-                throughput *= mixed_phase(S, c, band, dot3(dir, new_dir)) / kIsotropicPdf;
+                throughput *= mixed_phase<kAer>(S, c, band, dot3(dir, new_dir)) / kIsotropicPdf;
             }
             if (depth >= L.rr_start_depth) {  // russian_roulette (sky_trace.wgsl:691-701)
                 float q = fminf(fmaxf(throughput, 0.05f), 0.95f);
@@ -133,7 +133,8 @@ __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
     return v;
 }
 
-template <int kTracking, int kPhase>
+// kAer: aerosol species the medium functions evaluate (coefficients_at()).
+template <int kTracking, int kPhase, int kAer>
 __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch L, double* __restrict__ cell_sum,
                                                           double* __restrict__ cell_sumsq,
                                                           unsigned long long* __restrict__ counters,
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch 
         const uint32_t s_local = base + lane;
         float r = 0.0f;
         if (s_local < L.spp)
-            r = trace_chain<kTracking, kPhase>(S, L, x, y, band, L.sample_offset + s_local, n, watchdog);
+            r = trace_chain<kTracking, kPhase, kAer>(S, L, x, y, band, L.sample_offset + s_local, n, watchdog);
         const double rd = double(r);
         sum += warp_sum(rd);
         sumsq += warp_sum(rd * rd);
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(256) trace_plain_kernel(DevScene S, DevLaunch 
 
 cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
                                unsigned long long* counters, uint32_t* status, bool accumulate,
-                               cudaStream_t stream) {
+                               uint32_t aerosol_species, cudaStream_t stream) {
     const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;
     const uint32_t block = 256;
     const uint64_t blocks = (cells * 32u + block - 1) / block;
@@ -196,8 +197,12 @@ cudaError_t launch_trace_plain(const DevScene& S, const DevLaunch& L, double* ce
     const uint32_t acc = accumulate ? 1u : 0u;
 #define SKY_PLAIN_CASE(TR, PH)                                                                                   \
     if (L.tracking == TR && L.phase_sampling == PH) {                                                            \
-        trace_plain_kernel<TR, PH><<<grid, block, 0, stream>>>(S, L, cell_sum, cell_sumsq, counters, status,     \
-                                                               cells, acc);                                      \
+        if (aerosol_species == 1u)                                                                               \
+            trace_plain_kernel<TR, PH, 1><<<grid, block, 0, stream>>>(S, L, cell_sum, cell_sumsq, counters,      \
+                                                                      status, cells, acc);                       \
+        else                                                                                                     \
+            trace_plain_kernel<TR, PH, int(kSpecies)><<<grid, block, 0, stream>>>(S, L, cell_sum, cell_sumsq,    \
+                                                                                  counters, status, cells, acc); \
         return cudaGetLastError();                                                                               \
     }
     SKY_PLAIN_CASE(SKY_TRACKING_SEGMENT_RESTART, SKY_PHASE_ISOTROPIC)

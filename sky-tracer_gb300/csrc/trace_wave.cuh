@@ -115,10 +115,50 @@ __device__ __forceinline__ Medium stage_medium(const DevScene& S, unsigned char*
     return Medium{knot_z, finder, profile, bands, optics};
 }
 
+// The medium coefficients at each lane's current scattering vertex, kept in
+// shared memory (one word per thread per value, thread-minor) from the real
+// collision that made the vertex to its NEE terms and its continuation, so
+// that a vertex evaluates coefficients_at() once instead of three times
+// (-1.6 % on the production render): the Rayleigh coefficient, the kAer
+// species' scattering coefficients and the total scattering coefficient.
+template <int kAer>
+struct VertexCoeffCache {
+    float* at;  // this thread's first word
+    __device__ __forceinline__ void store(const Coeffs& c) const {
+        at[0] = c.rayleigh;
+#pragma unroll
+        for (int i = 0; i < kAer; ++i) at[(1 + i) * kWaveThreads] = c.sca[i];
+        at[(1 + kAer) * kWaveThreads] = c.scattering;
+    }
+    // What the NEE term and the continuation read: rayleigh, sca[] and
+    // scattering (the species beyond kAer are 0; absorption is not kept).
+    __device__ __forceinline__ Coeffs load() const {
+        Coeffs c;
+        c.rayleigh = at[0];
+#pragma unroll
+        for (int i = 0; i < int(kSpecies); ++i) c.sca[i] = i < kAer ? at[(1 + i) * kWaveThreads] : 0.0f;
+        c.scattering = at[(1 + kAer) * kWaveThreads];
+        c.abs_total = 0.0f;
+        c.extinction = c.scattering;
+        return c;
+    }
+};
+
+// Byte offset of the vertex cache in the dynamic shared memory (after the
+// staged medium tables) and the block's total dynamic shared memory.
+__host__ __device__ inline size_t vertex_cache_offset(uint32_t knots, uint32_t bands) {
+    return (staged_medium_bytes(knots, bands) + 15u) & ~size_t(15u);
+}
+__host__ __device__ inline size_t wave_smem_bytes(uint32_t knots, uint32_t bands, uint32_t aerosol_species) {
+    return vertex_cache_offset(knots, bands) + size_t(2u + aerosol_species) * kWaveThreads * sizeof(float);
+}
+
 // kCount: count events (SkyDeviceOutputs.counters given).  Without it the
 // counters are never read, so their increments compile away (the registers
 // they would hold are worth ~5 % at 64 registers per lane).
-template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount>
+// kAer: aerosol species evaluated by the medium functions (1 or kSpecies,
+// coefficients_at()).
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount, int kAer>
 __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     wave_kernel(const __grid_constant__ DevScene S, const __grid_constant__ DevLaunch L0,
                 const DevJob* __restrict__ jobs, uint32_t num_jobs,
@@ -126,6 +166,8 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                 uint32_t* __restrict__ status, uint32_t iteration_limit) {
     extern __shared__ __align__(16) unsigned char medium_smem[];
     const Medium M = stage_medium(S, medium_smem);
+    const VertexCoeffCache<kAer> vc{
+        reinterpret_cast<float*>(medium_smem + vertex_cache_offset(S.knot_count, S.band_count)) + threadIdx.x};
     const uint32_t lane = threadIdx.x & 31u;
     Counters n;
     n.clear();
@@ -264,15 +306,15 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
                     float cos_t = 1.0f, sin_t = 0.0f, xi_phi = 0.0f, weight = 1.0f;
                     bool framed = true;
                     if (!ground) {
-                        const Coeffs c = coefficients_at(S, M, band, alt);
+                        const Coeffs c = vc.load();
                         if (kPhase == SKY_PHASE_TABULATED) {
                             float mu;
-                            weight = tabulated_mu(S, c, band, rng, mu, xi_phi);
+                            weight = tabulated_mu<kAer>(S, c, band, rng, mu, xi_phi);
                             cos_t = fminf(fmaxf(mu, -1.0f), 1.0f);
                             sin_t = sqrtf(fmaxf(1.0f - cos_t * cos_t, 0.0f));
                         } else {
                             nd = sample_isotropic(rng);
-                            weight = mixed_phase(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
+                            weight = mixed_phase<kAer>(S, c, band, dot3(dir, nd)) / kIsotropicPdf;
                             framed = false;
                         }
                     } else {
@@ -347,20 +389,24 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
         if (tracing) {
             float t_hit = 0.0f;
             const bool hit = track_ray<kTracking>(S, M, g, t_max, band, rng, t_hit, n, watchdog, shadow_ray);
-            // the medium coefficients at a real collision (albedo) and at the vertex of
-            // an unblocked shadow ray (phase of its NEE term): one call for both kinds
+            // the medium coefficients at a real collision (albedo; kept for the new
+            // vertex's NEE terms and continuation) and at the vertex of an unblocked
+            // shadow ray (phase of its NEE term, from the vertex cache)
             const bool lit = shadow_ray && !hit;
+            Coeffs c;
             if (!shadow_ray && hit) {
                 org = madd(org, dir, t_hit);
                 alt = altitude_at(g, t_hit, S.ground_radius);
+                c = coefficients_at<kAer>(S, M, band, alt);
+                vc.store(c);
+            } else if (lit && !ground) {
+                c = vc.load();
             }
-            Coeffs c;
-            if ((!shadow_ray && hit) || (lit && !ground)) c = coefficients_at(S, M, band, alt);
             if (shadow_ray) {
                 if (lit) {  // the sample's term, transmittance 1 (sky_trace.wgsl:566-608)
                     const float l_sun = M.bands[band].solar_radiance;
                     nee += ground ? S.ground_albedo * kInvPi * l_sun * 1.0f * nee_mu / S.light_pdf
-                                  : l_sun * 1.0f * mixed_phase(S, c, band, nee_mu) / S.light_pdf;
+                                  : l_sun * 1.0f * mixed_phase<kAer>(S, c, band, nee_mu) / S.light_pdf;
                 }
                 next = kLights;
             } else if (hit) {
@@ -409,16 +455,18 @@ __global__ void __launch_bounds__(kWaveThreads, kMinBlocks)
     if (__any_sync(kFull, watchdog) && lane == 0u) atomicOr(status, 1u);
 }
 
-template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount>
+template <int kTracking, int kPhase, int kMinBlocks, bool kSingle, bool kCount, int kAer>
 cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
-    const void* k = reinterpret_cast<const void*>(wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount>);
+    const void* k =
+        reinterpret_cast<const void*>(wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount, kAer>);
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    // the staged medium tables: 10 KB for 81 bands over 68 knots; the largest scenes the library
-    // accepts (1024 knots, 256 bands) need 71 KB, beyond the 48 KB a launch gets without opting in
-    const size_t smem = staged_medium_bytes(w.scene.knot_count, w.scene.band_count);
+    // the staged medium tables and the vertex cache: 12.7 KB for 81 bands over 68 knots and one
+    // aerosol species; the largest scenes the library accepts (1024 knots, 256 bands) need 77 KB,
+    // beyond the 48 KB a launch gets without opting in
+    const size_t smem = wave_smem_bytes(w.scene.knot_count, w.scene.band_count, uint32_t(kAer));
     if (smem > 48u * 1024u &&
         (e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
         return e;
@@ -443,29 +491,36 @@ cudaError_t launch_wave_shape(const WaveLaunch& w, cudaStream_t stream) {
     // a warp per cell at most
     const uint64_t want = (uint64_t(w.total_cells) * 32u + kWaveThreads - 1u) / kWaveThreads;
     const uint32_t blocks = uint32_t(std::max<uint64_t>(1u, std::min<uint64_t>(uint64_t(per_sm) * sms, want)));
-    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount><<<blocks, kWaveThreads, smem, stream>>>(
+    wave_kernel<kTracking, kPhase, kMinBlocks, kSingle, kCount, kAer><<<blocks, kWaveThreads, smem, stream>>>(
         w.scene, w.launch0, w.jobs, w.num_jobs, w.total_cells, w.work_counter, w.counters, w.status,
         w.iteration_limit ? w.iteration_limit : kMaxIterations);
     return cudaGetLastError();
 }
 
-template <int kTracking, int kPhase, bool kSingle, bool kCount>
+template <int kTracking, int kPhase, bool kSingle, bool kCount, int kAer>
 cudaError_t launch_wave_variant(const WaveLaunch& w, cudaStream_t stream) {
     switch (w.variant) {
-        case 0: return launch_wave_shape<kTracking, kPhase, 3, kSingle, kCount>(w, stream);
-        case 1: return launch_wave_shape<kTracking, kPhase, 2, kSingle, kCount>(w, stream);
-        case 2: return launch_wave_shape<kTracking, kPhase, 4, kSingle, kCount>(w, stream);
+        case 0: return launch_wave_shape<kTracking, kPhase, 3, kSingle, kCount, kAer>(w, stream);
+        case 1: return launch_wave_shape<kTracking, kPhase, 2, kSingle, kCount, kAer>(w, stream);
+        case 2: return launch_wave_shape<kTracking, kPhase, 4, kSingle, kCount, kAer>(w, stream);
         default: return cudaErrorInvalidValue;
     }
 }
 
+template <int kTracking, int kPhase, int kAer>
+cudaError_t launch_wave_species(const WaveLaunch& w, cudaStream_t stream) {
+    if (w.num_jobs == 1u)
+        return w.counters ? launch_wave_variant<kTracking, kPhase, true, true, kAer>(w, stream)
+                          : launch_wave_variant<kTracking, kPhase, true, false, kAer>(w, stream);
+    return w.counters ? launch_wave_variant<kTracking, kPhase, false, true, kAer>(w, stream)
+                      : launch_wave_variant<kTracking, kPhase, false, false, kAer>(w, stream);
+}
+
 template <int kTracking, int kPhase>
 cudaError_t launch_wave_mode(const WaveLaunch& w, cudaStream_t stream) {
-    if (w.num_jobs == 1u)
-        return w.counters ? launch_wave_variant<kTracking, kPhase, true, true>(w, stream)
-                          : launch_wave_variant<kTracking, kPhase, true, false>(w, stream);
-    return w.counters ? launch_wave_variant<kTracking, kPhase, false, true>(w, stream)
-                      : launch_wave_variant<kTracking, kPhase, false, false>(w, stream);
+    if (w.aerosol_species == 1u) return launch_wave_species<kTracking, kPhase, 1>(w, stream);
+    if (w.aerosol_species == kSpecies) return launch_wave_species<kTracking, kPhase, int(kSpecies)>(w, stream);
+    return cudaErrorInvalidValue;
 }
 
 // The kernels of one tracking mode, both phase samplings.

@@ -107,7 +107,7 @@ class SkyDeviceOutputs(ctypes.Structure):
 
 class SkyTuning(ctypes.Structure):
     _fields_ = [
-        ("variant", _u32), ("max_blocks_per_sm", _u32), ("_unused", _u32 * 2),
+        ("variant", _u32), ("max_blocks_per_sm", _u32), ("all_species", _u32), ("_unused", _u32),
         ("crossing_cost", _f), ("iteration_limit", _u32), ("_reserved", _u32 * 2),
     ]
 

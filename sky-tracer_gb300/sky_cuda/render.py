@@ -147,7 +147,8 @@ class GpuScene:
         t = SkyTuning()
         check(self.lib.sky_cuda_scene_get_tuning(self.handle, ctypes.byref(t)), self.lib)
         return {"variant": t.variant, "max_blocks_per_sm": t.max_blocks_per_sm,
-                "crossing_cost": float(t.crossing_cost), "iteration_limit": t.iteration_limit}
+                "crossing_cost": float(t.crossing_cost), "iteration_limit": t.iteration_limit,
+                "all_species": t.all_species}
 
     def set_tuning(self, **kw) -> None:
         """Set launch-shape fields of SkyTuning (unnamed fields keep their value)."""

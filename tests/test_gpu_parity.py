@@ -347,6 +347,56 @@ def test_event_counting_does_not_change_the_render(gpu, dome_scene, tracking):
     assert runs[1][2][6] == cells * cfg.spp and runs[1][2][0] > 0
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("phase", [_abi.PHASE_ISOTROPIC, _abi.PHASE_TABULATED])
+def test_single_species_kernels_match_four_species(gpu, dome_scene, kernel, phase):
+    """The synthetic scene carries aerosol in species 0 only, so the kernels
+    evaluate that species alone; SkyTuning.all_species = 1 forces the
+    four-species instantiations.  Both trace the same chains: the plain
+    kernel's sums are equal bit for bit, the wavefront kernel's to FP64
+    rounding (its lanes add to a cell in no fixed order), and the event
+    counts are equal."""
+    cfg = RenderConfig(width=32, height=16, spp=16, phase_sampling=phase, tracking=_abi.TRACKING_MERGED_LAYERS,
+                       rr_start_depth=8, kernel=kernel)
+    with GpuScene(dome_scene) as gs:
+        assert gs.get_tuning()["all_species"] == 0
+        a, qa, ca, sa = gpu_sums(gs, cfg)
+        gs.set_tuning(all_species=1)
+        assert gs.get_tuning()["all_species"] == 1
+        b, qb, cb, sb = gpu_sums(gs, cfg)
+        with pytest.raises(SkyCudaError):
+            gs.set_tuning(all_species=2)
+    assert sa == 0 and sb == 0 and ca[6] == cfg.pixels * dome_scene.band_count * cfg.spp
+    if kernel == _abi.KERNEL_PLAIN:
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(qa, qb)
+    else:
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(qa, qb, rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(ca, cb)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_four_species_chains_match_oracle(gpu, ref_scene, kernel):
+    """The reference tables carry four aerosol species, so the four-species
+    instantiations run: chain by chain against the oracle."""
+    agree = total = 0
+    with GpuScene(ref_scene) as gs:
+        for offset in (0, 11):
+            cfg = RenderConfig(width=16, height=8, spp=1, sample_offset=offset, seed=0x5EC7_2026_0430 + offset,
+                               phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS,
+                               max_orders=16, kernel=kernel)
+            g, _, _, st = gpu_sums(gs, cfg)
+            o, _, _, wd = oracle.render(ref_scene, cfg)
+            assert st == 0 and wd == 0
+            close = np.abs(g - o) <= 2e-3 * np.maximum(np.abs(g), np.abs(o)) + 1e-9
+            agree += int(close.sum())
+            total += close.size
+    frac = agree / total
+    print(f"four aerosol species, chain agreement kernel={kernel}: {frac:.4f} of {total}")
+    assert frac >= 0.95
+
+
 def _device_buffers(cells: int, pixels: int):
     import torch
     return {"s": torch.zeros(cells, dtype=torch.float64, device="cuda"),
