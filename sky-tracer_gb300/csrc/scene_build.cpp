@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 
 namespace sky {
 namespace {
@@ -313,6 +314,16 @@ int build_host_tables(const SkySceneDesc* d, HostTables& out, std::string& err, 
         while (k + 2 < K && double(z[k + 1]) <= edge) ++k;
         out.finder[c] = uint16_t(k);
     }
+    // Per band and finder cell, the knot interval at the cell's lower edge with its next
+    // knot: below that knot a lookup needs no search (sigma_t_at).
+    out.sig_cell.assign(size_t(B) * kFinderCells, float4{0.0f, 0.0f, 0.0f, 0.0f});
+    for (uint32_t b = 0; b < B; ++b)
+        for (uint32_t c = 0; c < kFinderCells; ++c) {
+            const uint32_t k = out.finder[c];
+            const float2 e = out.sigma_t[size_t(b) * K + k];
+            const float next = k + 2 < K ? z[k + 1] : std::numeric_limits<float>::infinity();
+            out.sig_cell[size_t(b) * kFinderCells + c] = float4{e.x, e.y, z[k], next};
+        }
     out.knot_z = z;
     out.majorants.assign(d->majorants_km_inv, d->majorants_km_inv + nmaj);
 

@@ -15,6 +15,7 @@ struct HostTables {
     std::vector<float> knot_z;
     std::vector<uint16_t> finder;
     std::vector<float2> sigma_t;
+    std::vector<float4> sig_cell;
     std::vector<float> majorants;
     std::vector<DevBand> bands;
     std::vector<DevProfileKnot> profile;

@@ -546,6 +546,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     size_t o_knot = reserve(h.knot_z.size() * sizeof(float));
     size_t o_finder = reserve(h.finder.size() * sizeof(uint16_t));
     size_t o_sig = reserve(h.sigma_t.size() * sizeof(float2));
+    size_t o_cell = reserve(h.sig_cell.size() * sizeof(float4));
     size_t o_maj = reserve(h.majorants.size() * sizeof(float));
     size_t o_band = reserve(h.bands.size() * sizeof(DevBand));
     size_t o_prof = reserve(h.profile.size() * sizeof(DevProfileKnot));
@@ -560,6 +561,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     put(o_knot, h.knot_z.data(), h.knot_z.size() * sizeof(float));
     put(o_finder, h.finder.data(), h.finder.size() * sizeof(uint16_t));
     put(o_sig, h.sigma_t.data(), h.sigma_t.size() * sizeof(float2));
+    put(o_cell, h.sig_cell.data(), h.sig_cell.size() * sizeof(float4));
     put(o_maj, h.majorants.data(), h.majorants.size() * sizeof(float));
     put(o_band, h.bands.data(), h.bands.size() * sizeof(DevBand));
     put(o_prof, h.profile.data(), h.profile.size() * sizeof(DevProfileKnot));
@@ -583,6 +585,7 @@ int sky_cuda_scene_create(const SkySceneDesc* desc, SkyScene** out_scene) {
     s->dev.knot_z = reinterpret_cast<const float*>(base + o_knot);
     s->dev.finder = reinterpret_cast<const uint16_t*>(base + o_finder);
     s->dev.sigma_t = reinterpret_cast<const float2*>(base + o_sig);
+    s->dev.sig_cell = reinterpret_cast<const float4*>(base + o_cell);
     s->dev.majorants = reinterpret_cast<const float*>(base + o_maj);
     s->dev.bands = reinterpret_cast<const DevBand*>(base + o_band);
     s->dev.profile = reinterpret_cast<const DevProfileKnot*>(base + o_prof);

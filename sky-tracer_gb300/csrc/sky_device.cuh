@@ -278,13 +278,22 @@ __device__ __forceinline__ uint32_t knot_interval(const DevScene& S, const float
     return k;
 }
 
-// Total extinction of `band` at `alt` (extinction_total(coefficients_at()),
-// sky_trace.wgsl:356-403), from the per-band (value, slope) knot table.
+// Total extinction of a band at `alt` (extinction_total(coefficients_at()),
+// sky_trace.wgsl:356-403), from the band's (value, slope) knot table
+// `sig_row` and its finder-cell table `cell_row` (DevScene::sig_cell).  A
+// tentative collision reads one 16-byte cell entry: the knot interval that
+// holds the cell's lower edge, with its value, slope, knot and the next knot.
+// Below the next knot the interval is the one knot_interval() finds, so the
+// result is the same FMA on the same operands; above it (the cell holds a
+// knot) the knot search runs.
 __device__ __forceinline__ float sigma_t_at(const DevScene& S, const float* knot_z, const uint16_t* finder,
-                                            const float2* sigma_t, uint32_t band, float alt) {
+                                            const float2* sig_row, const float4* cell_row, float alt) {
     if (!(alt >= 0.0f && alt <= S.top_altitude)) return 0.0f;
-    uint32_t k = knot_interval(S, knot_z, finder, alt);
-    float2 e = sigma_t[band * S.knot_count + k];
+    const int cell = min(int(alt * S.finder_scale), int(kFinderCells) - 1);
+    const float4 c = __ldg(cell_row + cell);
+    if (alt < c.w) return fmaf(alt - c.z, c.y, c.x);
+    const uint32_t k = knot_interval(S, knot_z, finder, alt);
+    const float2 e = sig_row[k];
     return fmaf(alt - knot_z[k], e.y, e.x);
 }
 
@@ -577,14 +586,22 @@ __device__ __forceinline__ V3 sky_view_lut_dir(const DevLaunch& L, float u_in, f
     return normalize_or_y(mk(sin_view * h.x, view_zenith_cos + sin_view * h.y, sin_view * h.z));
 }
 
+// (i + offset) / n correctly rounded, as the shader divides: a product with the
+// exact reciprocal 1/n when n is a power of two (the same bits, without the
+// division's instruction sequence), else the division.
+__device__ __forceinline__ float pixel_coord(uint32_t i, float offset, uint32_t n, float inv_n) {
+    const float a = __fadd_rn(float(i), offset);
+    return (n & (n - 1u)) == 0u ? __fmul_rn(a, inv_n) : __fdiv_rn(a, float(n));
+}
+
 // Camera ray of sample `rng` for pixel (x, y) (sky_trace.wgsl:800-807): two
 // jitter draws are always consumed, also for the sky-view LUT.
 __device__ __forceinline__ V3 camera_dir(const DevLaunch& L, uint32_t x, uint32_t y, Rng& rng) {
-    float u = __fdiv_rn(float(x) + rng.next(), float(L.width));
-    float v = __fdiv_rn(float(y) + rng.next(), float(L.height));
+    float u = pixel_coord(x, rng.next(), L.width, L.inv_width);
+    float v = pixel_coord(y, rng.next(), L.height, L.inv_height);
     if (L.projection == SKY_PROJECTION_SKY_VIEW_LUT) {
-        u = __fdiv_rn(float(x) + 0.5f, float(L.width));
-        v = __fdiv_rn(float(y) + 0.5f, float(L.height));
+        u = pixel_coord(x, 0.5f, L.width, L.inv_width);
+        v = pixel_coord(y, 0.5f, L.height, L.inv_height);
         return sky_view_lut_dir(L, u, v);
     }
     return panorama_dir(u, v);
@@ -606,6 +623,7 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const Medium
                                                  bool shadow) {
     const MergedGrid G = merged_grid(S, band);
     const float2* sig_row = S.sigma_t + band * S.knot_count;
+    const float4* cell_row = S.sig_cell + band * kFinderCells;
     float t = 0.0f;
     int m = merged_layer_at(S, G, altitude_at(g, fminf(kRayEpsilonKm, t_max), S.ground_radius));
     int dir;
@@ -633,7 +651,7 @@ __device__ __forceinline__ bool track_ray_merged(const DevScene& S, const Medium
         }
         t = t + dt;
         ++n.e[SKY_EVENT_TRACK_STEP];
-        float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, altitude_at(g, t, S.ground_radius));
+        float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, cell_row, altitude_at(g, t, S.ground_radius));
         if (rng.next() * maj < sig) {
             t_hit = t;
             return true;
@@ -650,6 +668,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const Medium& M, co
         return track_ray_merged(S, M, g, t_max, band, rng, t_hit, n, watchdog, shadow);
     const float* maj_row = S.majorants + band * S.layer_count;
     const float2* sig_row = S.sigma_t + band * S.knot_count;
+    const float4* cell_row = S.sig_cell + band * kFinderCells;
     float t = 0.0f;
     uint32_t guard = 0;
     float tau = 0.0f;
@@ -680,7 +699,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const Medium& M, co
                 need_draw = true;
                 ++n.e[SKY_EVENT_TRACK_STEP];
                 float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, alt);
+                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, cell_row, alt);
                 if (rng.next() * maj < sig) {
                     t_hit = t;
                     return true;
@@ -694,7 +713,7 @@ __device__ __forceinline__ bool track_ray(const DevScene& S, const Medium& M, co
                 if (t >= seg_end) break;
                 ++n.e[SKY_EVENT_TRACK_STEP];
                 float alt = altitude_at(g, t, S.ground_radius);
-                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, 0u, alt);
+                float sig = sigma_t_at(S, M.knot_z, M.finder, sig_row, cell_row, alt);
                 if (rng.next() * maj < sig) {
                     t_hit = t;
                     return true;

@@ -76,6 +76,9 @@ struct DevScene {
     const float* knot_z;               // [K]
     const uint16_t* finder;            // [kFinderCells] knot interval of each cell's lower edge
     const float2* sigma_t;             // [B][K] extinction (value, slope) per knot interval
+    const float4* sig_cell;            // [B][kFinderCells] per finder cell: the knot interval k that holds
+                                       // its lower edge as (value, slope, knot_z[k], knot_z[k + 1]; +inf for
+                                       // the last interval)
     const float* majorants;            // [B][L]
     const DevBand* bands;              // [B]
     const DevProfileKnot* profile;     // [K]
