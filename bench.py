@@ -557,28 +557,36 @@ def adjoint_report(args, steps, warmup, checks=True):
     def dloss(out):
         return (2.0 * keep * (xyz_of(out, cfg.spp) - txyz) @ w.T).float()
 
+    # the forward keeps each chain's radiance (one float per chain), so the backward
+    # replays each chain once (as the autograd Function does)
+    chain_buf = r.new_chain_buffer()
+
     def step():
-        out = r.forward(th0, check_status=False)
-        return out, r.backward(th0, None, dloss(out), check_status=False)
+        out = r.forward(th0, check_status=False, chains=chain_buf)
+        return out, r.backward(th0, None, dloss(out), check_status=False, chains=chain_buf)
 
     for _ in range(max(warmup, 1)):
         step()
     torch.cuda.synchronize()
-    fwd_ms, bwd_ms = [], []
+    fwd_ms, bwd_ms, bwd_retrace_ms = [], [], []
     stream = torch.cuda.current_stream()
     for _ in range(steps):
-        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
         e0.record(stream)
-        out = r.forward(th0, check_status=False)
+        out = r.forward(th0, check_status=False, chains=chain_buf)
         e1.record(stream)
         d = dloss(out)
         e_b = torch.cuda.Event(enable_timing=True)
         e_b.record(stream)
-        grad, _ = r.backward(th0, None, d, check_status=False)
+        grad, _ = r.backward(th0, None, d, check_status=False, chains=chain_buf)
         e2.record(stream)
-        e2.synchronize()
+        # the same backward without the chain buffer: every chain traced twice
+        r.backward(th0, None, d, check_status=False)
+        e3.record(stream)
+        e3.synchronize()
         fwd_ms.append(e0.elapsed_time(e1))
         bwd_ms.append(e_b.elapsed_time(e2))
+        bwd_retrace_ms.append(e2.elapsed_time(e3))
     r._check_status()
     chains = cells * cfg.spp
     f_ms, b_ms = statistics.median(fwd_ms), statistics.median(bwd_ms)
@@ -586,6 +594,7 @@ def adjoint_report(args, steps, warmup, checks=True):
            "forward_ms": f_ms, "backward_ms": b_ms, "step_ms": f_ms + b_ms,
            "forward_chains_per_s": chains / (f_ms * 1e-3), "backward_chains_per_s": chains / (b_ms * 1e-3),
            "step_chains_per_s": chains / ((f_ms + b_ms) * 1e-3), "estimator": "segment integrals",
+           "chain_buffer_bytes": chains * 4, "backward_ms_without_chain_buffer": statistics.median(bwd_retrace_ms),
            "gpu_launches_per_step": 5}
     if not checks:
         gs.close()

@@ -455,6 +455,17 @@ typedef enum SkyAdjointEstimator {
     SKY_ADJOINT_NULL_COLLISIONS = 1
 } SkyAdjointEstimator;
 
+/*
+ * chain_radiance (optional, device float [slab pixels][band_count][spp],
+ * the slab's cells in film order, each cell's samples in order): a forward
+ * call writes every chain's radiance into it (before the band's solar
+ * multiplier); a backward call at the same config, parameters and sun reads
+ * it instead of tracing each chain a first time for its radiance, and skips
+ * the chains whose radiance is zero (they carry no gradient).  Path replay
+ * still stores no path: one float per chain.  Not with sample_* parameters;
+ * a backward given a buffer that another config or parameter set wrote
+ * returns a wrong gradient.
+ */
 typedef struct SkyAdjointParams {
     const float* layer_params;
     const float* band_params;
@@ -462,6 +473,7 @@ typedef struct SkyAdjointParams {
     const float* sample_band_params;
     float sun_direction[3];  /* unit vector; all zero = the scene's sun */
     uint32_t estimator;      /* SkyAdjointEstimator (backward only) */
+    float* chain_radiance;   /* optional: see above */
 } SkyAdjointParams;
 
 /*

@@ -666,6 +666,7 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
             while (next != kNextIdle && next != kNextTrace) {
                 if (next == kNextEnd) {
                     if (!kGrad) {
+                        if (A.chain_rad) A.chain_rad[uint64_t(cell) * L.spp + sample] = rad;
                         const double rd = double(resolve(A.P, Lc, band).kS * rad);
                         acc_sum += rd;
                         acc_sq += rd * rd;
@@ -705,6 +706,16 @@ __global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const 
                     }
                     const uint32_t pixel = py * L.width + px;
                     wc = kGrad ? __ldg(dloss + cell) * inv_spp : 0.0f;
+                    if (kGrad && pass == 0u && A.chain_rad) {
+                        // the forward's radiance of this chain stands in for its first trace
+                        total = __ldg(A.chain_rad + uint64_t(cell) * L.spp + sample);
+                        if (!(total > 0.0f)) {
+                            if (total != 0.0f) atomicAdd(sb + band * kAdjBandParams + 3u, wc * total);
+                            next = kNextIdle;
+                            continue;
+                        }
+                        pass = 1u;
+                    }
                     rng.init(pixel, L.sample_offset + sample, band, L.seed_lo, L.seed_hi);
                     dir = camera_dir(L, px, py, rng);
                     org = mk(0.0f, S.ground_radius + fmaxf(L.observer_altitude, 0.0f), 0.0f);

@@ -50,6 +50,10 @@ struct AdjCtx {
     uint32_t merge;        // merge uniform layers into tracking layers (else one per layer)
     float crossing_cost;   // merge cost of a shell crossing, in optical-depth units
     uint32_t estimator;    // SkyAdjointEstimator of the backward pass
+    // Optional [cells][spp] radiance of every chain (SkyAdjointParams::chain_radiance):
+    // written by the primal ray loop, read by the gradient pass in place of its first
+    // trace of each chain.
+    float* chain_rad;
 };
 
 // Writable views of the tables the prepare kernel fills.

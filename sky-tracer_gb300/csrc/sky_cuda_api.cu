@@ -919,6 +919,9 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
     } else {
         A.Q = A.P;
     }
+    if (p->chain_radiance && A.distinct)
+        return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance cannot be used with sample_* parameters");
+    A.chain_rad = p->chain_radiance;
     A.G.layer_maj = W.layer_maj;
     A.G.radius = W.radius;
     A.G.maj = W.maj;
@@ -1022,6 +1025,7 @@ extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointPa
         if (p.sample_band_params) p.band_params = p.sample_band_params;
         p.sample_layer_params = nullptr;
         p.sample_band_params = nullptr;
+        p.chain_radiance = nullptr;
     }
     AdjCtx A;
     AdjWorkspace W;

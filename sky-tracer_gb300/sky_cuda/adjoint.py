@@ -109,7 +109,17 @@ class AdjointRenderer:
         # elevation, say) sets this to False and calls check_status() once after them
         self.check_each_call = True
 
-    def _params(self, layer, band, sample_layer=None, sample_band=None, sun=None) -> SkyAdjointParams:
+    @property
+    def chain_count(self) -> int:
+        """Chains of one render: the length of a chain-radiance buffer."""
+        return self.pixels * self.bands * self.config.spp
+
+    def new_chain_buffer(self):
+        """A chain-radiance buffer for forward(chains=...) / backward(chains=...)."""
+        import torch
+        return torch.empty(self.chain_count, dtype=torch.float32, device="cuda")
+
+    def _params(self, layer, band, sample_layer=None, sample_band=None, sun=None, chains=None) -> SkyAdjointParams:
         for name, t, n in (("layer_params", layer, self.param_count), ("sample_layer_params", sample_layer,
                                                                        self.param_count),
                            ("band_params", band, self.bands * BAND_PARAMS),
@@ -125,6 +135,11 @@ class AdjointRenderer:
         p.sample_band_params = _ptr(sample_band)
         p.sun_direction = (ctypes.c_float * 3)(*(sun if sun is not None else (0.0, 0.0, 0.0)))
         p.estimator = self.estimator
+        if chains is not None:
+            if not (chains.is_cuda and chains.is_contiguous()) or chains.numel() != self.chain_count or \
+                    str(chains.dtype) != "torch.float32":
+                raise ValueError(f"chains must be a contiguous float32 CUDA tensor of {self.chain_count} values")
+            p.chain_radiance = chains.data_ptr()
         return p
 
     def check_status(self) -> None:
@@ -140,8 +155,10 @@ class AdjointRenderer:
             raise _abi.RenderWatchdog(_abi.SKY_ERR_WATCHDOG, "GPU path watchdog was reached")
 
     def forward(self, layer, band=None, *, sample_layer=None, sample_band=None, sun=None, xyz: bool = False,
-                check_status: bool = True) -> dict:
-        """Film [pixels * B] (float32) and cell sums; XYZ and its variance too with xyz=True."""
+                check_status: bool = True, chains=None) -> dict:
+        """Film [pixels * B] (float32) and cell sums; XYZ and its variance too with xyz=True.
+        chains (new_chain_buffer()) receives every chain's radiance for a
+        backward at the same parameters and sun."""
         import torch
         cells = self.pixels * self.bands
         out = {
@@ -156,7 +173,7 @@ class AdjointRenderer:
         for name, _ in SkyDeviceOutputs._fields_:
             setattr(o, name, _ptr(out.get(name)))
         o.status = self._status.data_ptr()
-        p = self._params(layer, band, sample_layer, sample_band, sun)
+        p = self._params(layer, band, sample_layer, sample_band, sun, chains)
         stream = torch.cuda.current_stream().cuda_stream
         check(self.lib.sky_cuda_adjoint_forward(self.gs.handle, ctypes.byref(self._c_config), ctypes.byref(p),
                                                 ctypes.byref(o), ctypes.c_void_p(stream)), self.lib)
@@ -165,10 +182,12 @@ class AdjointRenderer:
         return out
 
     def backward(self, layer, band, dloss_dfilm, *, sun=None, check_status: bool = True, decorrelate: bool = False,
-                 layer_grad: bool = True):
+                 layer_grad: bool = True, chains=None):
         """(dLoss/dlayer_params or None, dLoss/dband_params or None) as float64
         tensors.  decorrelate=True replays chains of another seed than the
-        forward's; layer_grad=False skips the layer gradient (band only)."""
+        forward's; layer_grad=False skips the layer gradient (band only).
+        chains: the buffer a forward at the same parameters and sun filled;
+        the replay then skips its first trace of each chain."""
         import torch
         d = dloss_dfilm.reshape(-1).to(torch.float32).contiguous()
         if d.numel() != self.pixels * self.bands:
@@ -182,7 +201,9 @@ class AdjointRenderer:
         g.layer_grad = _ptr(lg)
         g.band_grad = _ptr(bg)
         g.status = self._status.data_ptr()
-        p = self._params(layer, band, None, None, sun)
+        if decorrelate and chains is not None:
+            raise ValueError("a decorrelated backward traces other chains than the forward's: no chain buffer")
+        p = self._params(layer, band, None, None, sun, chains)
         stream = torch.cuda.current_stream().cuda_stream
         c = self._c_config
         if decorrelate:
@@ -215,7 +236,10 @@ def _autograd_function():
         def forward(ctx, layer, band, renderer, sun, decorrelate):
             layer_c = layer.detach().contiguous()
             band_c = band.detach().contiguous() if band is not None else None
-            out = renderer.forward(layer_c, band_c, sun=sun, check_status=renderer.check_each_call)
+            # each chain's radiance, so that the backward replays each chain once
+            ctx.chains = None if decorrelate else renderer.new_chain_buffer()
+            out = renderer.forward(layer_c, band_c, sun=sun, check_status=renderer.check_each_call,
+                                   chains=ctx.chains)
             ctx.renderer = renderer
             ctx.sun = sun
             ctx.decorrelate = decorrelate
@@ -231,7 +255,8 @@ def _autograd_function():
             want_layer = ctx.needs_input_grad[0] or band_c is None
             lg, bg = ctx.renderer.backward(layer_c, band_c, grad_film.contiguous(), sun=ctx.sun,
                                            decorrelate=ctx.decorrelate, layer_grad=want_layer,
-                                           check_status=ctx.renderer.check_each_call)
+                                           check_status=ctx.renderer.check_each_call, chains=ctx.chains)
+            ctx.chains = None
             gl = lg.to(layer_c.dtype).reshape(layer_c.shape) if lg is not None else None
             gb = bg.to(band_c.dtype).reshape(band_c.shape) if bg is not None else None
             return gl, gb, None, None, None

@@ -158,6 +158,42 @@ def _loss_setup(gs, scene, cfg, target_spp=256):
     return theta0, loss_of, dloss
 
 
+@pytest.mark.parametrize("estimator", [SEGMENT_INTEGRALS, NULL_COLLISIONS])
+def test_chain_buffer_backward_matches_retrace(gpu, small_scene, estimator):
+    """A backward given the forward's chain radiance (one float per chain)
+    replays each chain once instead of tracing it first for its radiance, and
+    skips the chains that collected nothing: the same gradient, to the
+    rounding of the per-warp FP32 gradient sums, with both estimators; band
+    gradients too.  The buffer holds every chain's radiance (before the solar
+    multiplier): per cell, the mean of its chains is the forward's film."""
+    import torch
+    cfg = RenderConfig(width=16, height=8, spp=32, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    B = small_scene.band_count
+    with GpuScene(small_scene) as gs:
+        theta0, _, dloss = _loss_setup(gs, small_scene, cfg)
+        r = AdjointRenderer(gs, cfg, estimator=estimator)
+        th0 = _t(theta0)
+        band0 = _t(np.ones(B * BAND_PARAMS, dtype=np.float32))
+        chains = r.new_chain_buffer()
+        chains.fill_(-1.0)
+        out = r.forward(th0, band0, chains=chains)
+        d = dloss(out)
+        lg_a, bg_a = r.backward(th0, band0, d, chains=chains)
+        lg_b, bg_b = r.backward(th0, band0, d)
+        with pytest.raises(ValueError):
+            r.backward(th0, band0, d, chains=chains, decorrelate=True)
+        with pytest.raises(SkyCudaError):
+            r.forward(th0, band0, sample_layer=_t(theta0 * np.float32(1.01)), chains=chains)
+    c = chains.cpu().numpy().reshape(cfg.pixels * B, cfg.spp)
+    assert np.all(c >= 0.0) and np.any(c > 0.0)
+    np.testing.assert_allclose(c.mean(axis=1), out["film"].cpu().numpy(), rtol=1e-5, atol=1e-7)
+    for a, b in ((lg_a, lg_b), (bg_a, bg_b)):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        assert np.any(a != 0.0)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
+
+
 def test_gradient_matches_central_differences(gpu, dome_scene):
     """The adjoint benchmark's finite-difference check (h = 1e-3) on a 32x16
     image, 32 bands, 64 spp: 16 parameters that all carry a gradient, drawn
