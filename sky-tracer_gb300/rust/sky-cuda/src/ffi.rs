@@ -19,6 +19,19 @@ pub const SKY_ERR_IO: c_int = 9;
 pub const SKY_FLAG_ACCUMULATE: u32 = 1;
 pub const SKY_FLAG_COUNT_EVENTS: u32 = 2;
 
+/// SkyRenderConfig.phase_sampling and .tracking values.
+pub const SKY_PHASE_ISOTROPIC: u32 = 0;
+pub const SKY_PHASE_TABULATED: u32 = 1;
+pub const SKY_TRACKING_SEGMENT_RESTART: u32 = 0;
+pub const SKY_TRACKING_RESIDUAL_CARRY: u32 = 1;
+pub const SKY_TRACKING_MERGED_LAYERS: u32 = 2;
+
+/// Differentiable rendering: band multipliers per band, and the estimators
+/// of the backward pass (SkyAdjointEstimator).
+pub const SKY_ADJOINT_BAND_PARAMS: u32 = 4;
+pub const SKY_ADJOINT_SEGMENT_INTEGRALS: u32 = 0;
+pub const SKY_ADJOINT_NULL_COLLISIONS: u32 = 1;
+
 /// = GpuBand (integrator.rs:79-86), 24 bytes.
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
@@ -120,6 +133,60 @@ pub struct SkyRenderStats {
     pub kernel_used: u32,
 }
 
+/// Device buffers of one render (SkyDeviceOutputs); null where not wanted.
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct SkyDeviceOutputs {
+    pub cell_sum: *mut f64,
+    pub cell_sumsq: *mut f64,
+    pub film: *mut f32,
+    pub xyz: *mut f64,
+    pub xyz_var: *mut f64,
+    pub counters: *mut u64,
+    pub status: *mut u32,
+    pub rgb: *mut f32,
+}
+
+impl Default for SkyDeviceOutputs {
+    fn default() -> Self {
+        let n = std::ptr::null_mut();
+        Self { cell_sum: n, cell_sumsq: n, film: std::ptr::null_mut(), xyz: n, xyz_var: n,
+               counters: std::ptr::null_mut(), status: std::ptr::null_mut(), rgb: std::ptr::null_mut() }
+    }
+}
+
+/// Parameters of a differentiable render (SkyAdjointParams); device pointers.
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct SkyAdjointParams {
+    pub layer_params: *const f32,
+    pub band_params: *const f32,
+    pub sample_layer_params: *const f32,
+    pub sample_band_params: *const f32,
+    pub sun_direction: [f32; 3],
+    pub estimator: u32,
+    pub chain_radiance: *mut f32,
+}
+
+impl Default for SkyAdjointParams {
+    fn default() -> Self {
+        Self { layer_params: std::ptr::null(), band_params: std::ptr::null(), sample_layer_params: std::ptr::null(),
+               sample_band_params: std::ptr::null(), sun_direction: [0.0; 3], estimator: SKY_ADJOINT_SEGMENT_INTEGRALS,
+               chain_radiance: std::ptr::null_mut() }
+    }
+}
+
+/// Gradient request of a backward call (SkyAdjointGrads); device pointers.
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct SkyAdjointGrads {
+    pub dloss_dfilm: *const f32,
+    pub layer_grad: *mut f64,
+    pub band_grad: *mut f64,
+    pub counters: *mut u64,
+    pub status: *mut u32,
+}
+
 /// Opaque scene handle (device tables owned by the library).
 #[repr(C)]
 pub struct SkyScene {
@@ -136,7 +203,14 @@ unsafe extern "C" {
     pub fn sky_cuda_render_desc(desc: *const SkySceneDesc, config: *const SkyRenderConfig, film_out: *mut f32,
                                 film_len: usize, stats: *mut SkyRenderStats) -> c_int;
     pub fn sky_cuda_render_device(scene: *const SkyScene, config: *const SkyRenderConfig,
-                                  outputs: *const c_void, cuda_stream: *mut c_void) -> c_int;
+                                  outputs: *const SkyDeviceOutputs, cuda_stream: *mut c_void) -> c_int;
+    pub fn sky_cuda_adjoint_param_count(scene: *const SkyScene) -> u32;
+    pub fn sky_cuda_adjoint_forward(scene: *const SkyScene, config: *const SkyRenderConfig,
+                                    params: *const SkyAdjointParams, outputs: *const SkyDeviceOutputs,
+                                    cuda_stream: *mut c_void) -> c_int;
+    pub fn sky_cuda_adjoint_backward(scene: *const SkyScene, config: *const SkyRenderConfig,
+                                     params: *const SkyAdjointParams, grads: *const SkyAdjointGrads,
+                                     cuda_stream: *mut c_void) -> c_int;
 }
 
 #[cfg(test)]
@@ -154,5 +228,8 @@ mod layout {
         assert_eq!(size_of::<SkySceneDesc>(), 120);
         assert_eq!(size_of::<SkyRenderConfig>(), 80);
         assert_eq!(size_of::<SkyRenderStats>(), 96);
+        assert_eq!(size_of::<SkyDeviceOutputs>(), 64);
+        assert_eq!(size_of::<SkyAdjointParams>(), 56);
+        assert_eq!(size_of::<SkyAdjointGrads>(), 40);
     }
 }

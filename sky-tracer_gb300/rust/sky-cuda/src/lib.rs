@@ -18,11 +18,18 @@
 //! `sky-reference-render` switches its dependency from
 //! `sky-spectral-path-tracer` to `sky-cuda` and calls `sky_cuda::render`
 //! (main.rs:113); nothing else changes.
+//!
+//! [`Adjoint`] is the differentiable render of a resident scene as a
+//! forward/backward pair (`sky_cuda_adjoint_forward` / `_backward`): the
+//! film over per-layer density scales, Mie albedo and asymmetry and per-band
+//! multipliers, and the path-replay gradient of a loss given dLoss/dfilm.
+//! Its buffers are the caller's device memory (a fitting host keeps
+//! parameters, film and gradients on the GPU between iterations).
 
 pub mod ffi;
 
 use std::ffi::CStr;
-use std::os::raw::c_char;
+use std::os::raw::{c_char, c_void};
 
 use sky_core::atmosphere::{GROUND_ALBEDO, PHASE_BINS, SceneData};
 pub use sky_spectral_path_tracer::config::{OutputProjection, RenderConfig};
@@ -212,6 +219,100 @@ impl GpuScene {
 impl Drop for GpuScene {
     fn drop(&mut self) {
         unsafe { ffi::sky_cuda_scene_destroy(self.handle) };
+    }
+}
+
+/// Device-side parameters of a differentiable render (SkyAdjointParams).
+#[derive(Clone, Copy, Debug)]
+pub struct AdjointParams {
+    /// [3 * layers + 2]: (Rayleigh, Mie, ozone) density scale per majorant
+    /// layer, then the Mie albedo and HG asymmetry.
+    pub layer_params: *const f32,
+    /// [bands][4] multipliers (Rayleigh, Mie, ozone, solar) or null for ones.
+    pub band_params: *const f32,
+    /// Unit sun direction, or all zero for the scene's own sun.
+    pub sun_direction: [f32; 3],
+    /// `ffi::SKY_ADJOINT_SEGMENT_INTEGRALS` or `ffi::SKY_ADJOINT_NULL_COLLISIONS`.
+    pub estimator: u32,
+    /// Optional [pixels][bands][spp] buffer: the forward writes each chain's
+    /// radiance, a backward at the same parameters and sun replays each chain
+    /// once instead of twice.
+    pub chain_radiance: *mut f32,
+}
+
+impl AdjointParams {
+    fn ffi(&self) -> ffi::SkyAdjointParams {
+        ffi::SkyAdjointParams {
+            layer_params: self.layer_params,
+            band_params: self.band_params,
+            sun_direction: self.sun_direction,
+            estimator: self.estimator,
+            chain_radiance: self.chain_radiance,
+            ..Default::default()
+        }
+    }
+}
+
+/// The forward/backward pair of the differentiable render of one config on
+/// a resident scene.  Tracking is merged-layer (residual carry over the
+/// merged grid) and phase sampling tabulated unless the config is changed
+/// through `config_mut`; the reference's segment-restart tracking is not
+/// differentiable here.
+pub struct Adjoint<'a> {
+    scene: &'a GpuScene,
+    config: ffi::SkyRenderConfig,
+}
+
+impl<'a> Adjoint<'a> {
+    pub fn new(scene: &'a GpuScene, config: &RenderConfig) -> Self {
+        let mut c = render_config(config);
+        c.tracking = ffi::SKY_TRACKING_MERGED_LAYERS;
+        c.phase_sampling = ffi::SKY_PHASE_TABULATED;
+        Self { scene, config: c }
+    }
+
+    pub fn config_mut(&mut self) -> &mut ffi::SkyRenderConfig {
+        &mut self.config
+    }
+
+    /// Length of `AdjointParams::layer_params`: 3 * majorant layers + 2.
+    pub fn param_count(&self) -> usize {
+        unsafe { ffi::sky_cuda_adjoint_param_count(self.scene.handle) as usize }
+    }
+
+    /// Film, cell sums and status of the render at `params`, queued on
+    /// `stream` (null: the default stream).
+    ///
+    /// # Safety
+    /// Every pointer in `params` and `outputs` is device memory of the
+    /// scene's GPU with the sizes include/sky_cuda.h gives (cell_sum and
+    /// status required), live until the stream has run the call.
+    pub unsafe fn forward(&self, params: &AdjointParams, outputs: &ffi::SkyDeviceOutputs,
+                          stream: *mut c_void) -> Result<(), RenderError> {
+        let p = params.ffi();
+        let status = unsafe { ffi::sky_cuda_adjoint_forward(self.scene.handle, &self.config, &p, outputs, stream) };
+        if status != ffi::SKY_OK {
+            return Err(render_error(status, last_error()));
+        }
+        Ok(())
+    }
+
+    /// Adds the gradient of the loss whose film derivative is
+    /// `grads.dloss_dfilm` to `grads.layer_grad` / `grads.band_grad`, queued
+    /// on `stream`.  The watchdog lands in `*grads.status` (read it after the
+    /// stream has run the call).
+    ///
+    /// # Safety
+    /// As for `forward`; `params.chain_radiance`, when set, holds what a
+    /// forward at the same parameters, sun and config wrote.
+    pub unsafe fn backward(&self, params: &AdjointParams, grads: &ffi::SkyAdjointGrads,
+                           stream: *mut c_void) -> Result<(), RenderError> {
+        let p = params.ffi();
+        let status = unsafe { ffi::sky_cuda_adjoint_backward(self.scene.handle, &self.config, &p, grads, stream) };
+        if status != ffi::SKY_OK {
+            return Err(render_error(status, last_error()));
+        }
+        Ok(())
     }
 }
 

@@ -203,17 +203,36 @@ class AdjointRenderer:
         g.status = self._status.data_ptr()
         if decorrelate and chains is not None:
             raise ValueError("a decorrelated backward traces other chains than the forward's: no chain buffer")
-        p = self._params(layer, band, None, None, sun, chains)
         stream = torch.cuda.current_stream().cuda_stream
         c = self._c_config
         if decorrelate:
             c = self.config.to_c()
             c.seed = self.config.seed ^ DECORRELATE_SEED
+            # the radiance of the backward's own chains from the (lighter) forward kernel,
+            # so that the replay traces each chain once and skips those that collected nothing
+            chains = self._decorrelated_chains(layer, band, sun, c)
+        p = self._params(layer, band, None, None, sun, chains)
         check(self.lib.sky_cuda_adjoint_backward(self.gs.handle, ctypes.byref(c), ctypes.byref(p),
                                                  ctypes.byref(g), ctypes.c_void_p(stream)), self.lib)
         if check_status:
             self._check_status()
         return lg, bg
+
+    def _decorrelated_chains(self, layer, band, sun, c):
+        """Chain radiance of config `c` (the decorrelated seed) at these
+        parameters, in a buffer the renderer keeps for its next backward."""
+        import torch
+        if getattr(self, "_dchains", None) is None:
+            self._dchains = self.new_chain_buffer()
+            self._dsums = torch.empty(self.pixels * self.bands, dtype=torch.float64, device="cuda")
+        o = SkyDeviceOutputs()
+        o.cell_sum = self._dsums.data_ptr()
+        o.status = self._status.data_ptr()
+        p = self._params(layer, band, None, None, sun, self._dchains)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(self.lib.sky_cuda_adjoint_forward(self.gs.handle, ctypes.byref(c), ctypes.byref(p), ctypes.byref(o),
+                                                ctypes.c_void_p(stream)), self.lib)
+        return self._dchains
 
     def bake_majorants(self, layer, band=None):
         """Majorant grid [B, L] of the parameterised medium (device bake)."""

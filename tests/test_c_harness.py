@@ -1,4 +1,5 @@
-"""The sky-cuda Rust crate's calls, made from C (tests/c_abi_harness.c).
+"""The sky-cuda Rust crate's calls, made from C (tests/c_abi_harness.c and,
+for its differentiable-render pair, tests/c_adjoint_harness.c).
 
 No Rust toolchain exists on these machines (cargo and rustc are absent here
 and on the GPU machine), so the crate's FFI sequence is exercised by a C program
@@ -8,7 +9,10 @@ sky_cuda_scene_destroy (its `GpuScene`), and the error path through
 sky_cuda_last_error (its RenderError mapping).  On the CPU the harness is
 compiled and linked against libsky_cuda.so; on the GPU it renders the
 reference's own data/ scene and its film must equal the Python one-shot
-render of the same scene and config.
+render of the same scene and config.  The adjoint harness makes the crate's
+Adjoint calls (sky_cuda_adjoint_forward with a chain-radiance buffer, then
+sky_cuda_adjoint_backward reading it) on device buffers of its own; its film
+and gradients must equal the Python AdjointRenderer's on the same inputs.
 """
 
 import os
@@ -31,6 +35,21 @@ def build_harness(out_dir: Path) -> Path:
     exe = out_dir / "c_abi_harness"
     cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"), str(HARNESS),
            "-L", str(LIB_DIR), "-lsky_cuda", f"-Wl,-rpath,{LIB_DIR}", "-o", str(exe)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    return exe
+
+
+ADJOINT_HARNESS = ROOT / "tests" / "c_adjoint_harness.c"
+CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+
+
+def build_adjoint_harness(out_dir: Path) -> Path:
+    exe = out_dir / "c_adjoint_harness"
+    cmd = ["gcc", "-std=c11", "-O2", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include"),
+           "-I", str(CUDA_HOME / "include"), str(ADJOINT_HARNESS), "-L", str(LIB_DIR), "-lsky_cuda",
+           f"-Wl,-rpath,{LIB_DIR}", "-L", str(CUDA_HOME / "lib64"), "-lcudart",
+           f"-Wl,-rpath,{CUDA_HOME / 'lib64'}", "-o", str(exe)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
     return exe
@@ -78,6 +97,60 @@ def test_harness_film_equals_the_python_render(gpu, ref_scene, tmp_path, project
     # the same one-shot call on the same inputs: equal up to the order of the FP64 cell sums
     np.testing.assert_allclose(film_c, film_py, rtol=1e-6, atol=0)
     assert np.all(np.isfinite(film_c)) and np.all(film_c >= 0) and np.any(film_c > 0)
+
+
+def test_adjoint_harness_compiles_and_links_against_the_library(lib_built, tmp_path):
+    if not (CUDA_HOME / "include" / "cuda_runtime.h").exists():
+        pytest.skip("no CUDA runtime headers")
+    exe = build_adjoint_harness(tmp_path)
+    res = subprocess.run(["nm", "-D", "--undefined-only", str(exe)], capture_output=True, text=True)
+    for sym in ("sky_cuda_scene_create", "sky_cuda_adjoint_param_count", "sky_cuda_adjoint_forward",
+                "sky_cuda_adjoint_backward", "sky_cuda_last_error", "sky_cuda_scene_destroy"):
+        assert sym in res.stdout
+
+
+@pytest.mark.gpu
+def test_adjoint_harness_matches_the_python_renderer(gpu, dome_scene, tmp_path):
+    """The crate's Adjoint forward/backward from C against AdjointRenderer on
+    the same scene, parameters, config and dLoss/dfilm: the film to the order
+    of the FP64 cell sums, the gradients to the rounding of the per-warp FP32
+    gradient sums."""
+    import torch
+
+    from sky_cuda import GpuScene, _abi
+    from sky_cuda.adjoint import BAND_PARAMS, AdjointRenderer, initial_layer_params
+
+    exe = build_adjoint_harness(tmp_path)
+    scene_file = tmp_path / "scene.bin"
+    write_scene(dome_scene, scene_file)
+    w, h, spp, seed = 16, 8, 16, 0x5EC7_2026_0430
+    theta = initial_layer_params(dome_scene, 0.76)
+    theta[:3 * dome_scene.layer_count] *= np.float32(1.02)
+    (tmp_path / "params.bin").write_bytes(theta.astype(np.float32).tobytes())
+    dloss = np.random.default_rng(7).normal(size=w * h * dome_scene.band_count).astype(np.float32)
+    (tmp_path / "dloss.bin").write_bytes(dloss.tobytes())
+    prefix = tmp_path / "out"
+    res = subprocess.run([str(exe), str(scene_file), str(w), str(h), str(spp), str(seed), str(tmp_path / "params.bin"),
+                          str(tmp_path / "dloss.bin"), str(prefix)], capture_output=True, text=True, timeout=300,
+                         env={**os.environ, "LD_LIBRARY_PATH": str(LIB_DIR)})
+    assert res.returncode == 0, res.stdout + res.stderr
+    film_c = np.fromfile(str(prefix) + ".film", dtype=np.float32)
+    lg_c = np.fromfile(str(prefix) + ".layer_grad", dtype=np.float64)
+    bg_c = np.fromfile(str(prefix) + ".band_grad", dtype=np.float64)
+
+    cfg = RenderConfig(width=w, height=h, spp=spp, seed=seed, observer_altitude_km=0.2,
+                       phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS)
+    with GpuScene(dome_scene) as gs:
+        r = AdjointRenderer(gs, cfg)
+        th = torch.as_tensor(theta, device="cuda").contiguous()
+        band = torch.ones(dome_scene.band_count * BAND_PARAMS, dtype=torch.float32, device="cuda")
+        chains = r.new_chain_buffer()
+        film_py = r.forward(th, band, chains=chains)["film"].cpu().numpy()
+        lg, bg = r.backward(th, band, torch.as_tensor(dloss, device="cuda"), chains=chains)
+    np.testing.assert_allclose(film_c, film_py, rtol=1e-6, atol=0)
+    for a, b in ((lg_c, lg.cpu().numpy()), (bg_c, bg.cpu().numpy())):
+        assert a.shape == b.shape and np.any(b != 0.0)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
 
 
 if __name__ == "__main__":
