@@ -48,7 +48,7 @@ DATA_DIR = ROOT / "tests" / "golden" / "data"
 # DRAM bytes (read + write) of one launch of the wavefront tracing kernel on
 # the production render, from a 1-pass ncu capture
 # (profiles/wave_kernel_plain-512x256-81wl-256spp_dram.txt).
-WAVE_LAUNCH_DRAM_BYTES = {"plain-512x256-81wl-256spp": 197.58e6 + 204.45e6}
+WAVE_LAUNCH_DRAM_BYTES = {"plain-512x256-81wl-256spp": 198.83e6 + 206.33e6}
 
 # Frozen per-event FP32 work weights (FLOP, an FMA counted as 2), counted
 # from the reference shader's arithmetic for each event type.
