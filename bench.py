@@ -930,7 +930,10 @@ def main():
             "time_to_1pct_xyz_s": t1pct, "p95_rel_se_at_spp": p95,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
-                         "traffic": WAVE_LAUNCH_DRAM_BYTES.get(args.workload) if cfg.kernel != 1 else None,
+                         # the captured traffic is one launch over the whole image (N = 1)
+                         "traffic": WAVE_LAUNCH_DRAM_BYTES.get(args.workload)
+                         if cfg.kernel != 1 and world == 1 else None,
+                         "scope": "the whole render" if world == 1 else "rank 0's slab",
                          "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
                          "peak_source": "measured: cuBLAS SGEMM 8192^3 with TF32 off (MEASURED_PEAKS.json "
                                         "has no FP32 figure)",
