@@ -570,7 +570,7 @@ enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLigh
 // gradient code.  Resident blocks: 4 per SM for the primal (64 registers),
 // 3 for the gradient passes (80 registers; 4 gains nothing there).
 template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
-__global__ void __launch_bounds__(256, kGrad ? 3 : 4) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
+__global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
                                                               const __grid_constant__ DevLaunch L,
                                                               const float* __restrict__ dloss,
                                                               double* __restrict__ layer_grad,
