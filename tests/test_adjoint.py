@@ -194,6 +194,33 @@ def test_chain_buffer_backward_matches_retrace(gpu, small_scene, estimator):
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
 
 
+def test_decorrelated_backward_replays_its_own_chains_once(gpu, small_scene):
+    """A decorrelated backward traces chains of another seed: it renders their
+    radiance with the forward kernel into a buffer of its own, then replays
+    each once.  Its gradient equals the backward of a renderer whose seed is
+    that other seed (both passes in the gradient kernel), to the rounding of
+    the per-warp FP32 gradient sums."""
+    from sky_cuda.adjoint import DECORRELATE_SEED
+    cfg = RenderConfig(width=16, height=8, spp=32, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    B = small_scene.band_count
+    with GpuScene(small_scene) as gs:
+        theta0, _, dloss = _loss_setup(gs, small_scene, cfg)
+        r = AdjointRenderer(gs, cfg)
+        th0 = _t(theta0)
+        band0 = _t(np.ones(B * BAND_PARAMS, dtype=np.float32))
+        d = dloss(r.forward(th0, band0))
+        lg_a, bg_a = r.backward(th0, band0, d, decorrelate=True)
+        other = AdjointRenderer(gs, dataclasses.replace(cfg, seed=cfg.seed ^ DECORRELATE_SEED))
+        lg_b, bg_b = other.backward(th0, band0, d)
+        lg_c, _ = r.backward(th0, band0, d)  # the forward's own chains: another estimate
+    for a, b in ((lg_a, lg_b), (bg_a, bg_b)):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        assert np.any(a != 0.0)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
+    assert not np.allclose(lg_a.cpu().numpy(), lg_c.cpu().numpy(), rtol=1e-3)
+
+
 def test_gradient_matches_central_differences(gpu, dome_scene):
     """The adjoint benchmark's finite-difference check (h = 1e-3) on a 32x16
     image, 32 bands, 64 spp: 16 parameters that all carry a gradient, drawn
