@@ -457,7 +457,8 @@ typedef enum SkyAdjointEstimator {
 
 /*
  * chain_radiance (optional, device float [slab pixels][band_count][spp],
- * the slab's cells in film order, each cell's samples in order): a forward
+ * the slab's cells in film order, each cell's samples in order;
+ * chain_radiance_len its length in floats, at least that count): a forward
  * call writes every chain's radiance into it (before the band's solar
  * multiplier); a backward call at the same config, parameters and sun reads
  * it instead of tracing each chain a first time for its radiance, and skips
@@ -474,6 +475,7 @@ typedef struct SkyAdjointParams {
     float sun_direction[3];  /* unit vector; all zero = the scene's sun */
     uint32_t estimator;      /* SkyAdjointEstimator (backward only) */
     float* chain_radiance;   /* optional: see above */
+    uint64_t chain_radiance_len;
 } SkyAdjointParams;
 
 /*

@@ -54,6 +54,7 @@ struct AdjCtx {
     // written by the primal ray loop, read by the gradient pass in place of its first
     // trace of each chain.
     float* chain_rad;
+    uint64_t chain_rad_len;  // floats in chain_rad (checked against the render's chains)
 };
 
 // Writable views of the tables the prepare kernel fills.

@@ -922,6 +922,7 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
     if (p->chain_radiance && A.distinct)
         return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance cannot be used with sample_* parameters");
     A.chain_rad = p->chain_radiance;
+    A.chain_rad_len = p->chain_radiance_len;
     A.G.layer_maj = W.layer_maj;
     A.G.radius = W.radius;
     A.G.maj = W.maj;
@@ -948,6 +949,13 @@ int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& 
     view.dev = A.S;
     L = make_launch(&view, c);
     view.dev = DevScene{};
+    if (A.chain_rad) {
+        const uint64_t chains = slab_pixels(c) * uint64_t(s->dev.band_count) * c->spp;
+        if (A.chain_rad_len < chains)
+            return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance holds " + std::to_string(A.chain_rad_len) +
+                                                         " floats; the render has " + std::to_string(chains) +
+                                                         " chains");
+    }
     return SKY_OK;
 }
 
@@ -1026,6 +1034,7 @@ extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointPa
         p.sample_layer_params = nullptr;
         p.sample_band_params = nullptr;
         p.chain_radiance = nullptr;
+        p.chain_radiance_len = 0;
     }
     AdjCtx A;
     AdjWorkspace W;

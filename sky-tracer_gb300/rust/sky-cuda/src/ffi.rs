@@ -166,13 +166,14 @@ pub struct SkyAdjointParams {
     pub sun_direction: [f32; 3],
     pub estimator: u32,
     pub chain_radiance: *mut f32,
+    pub chain_radiance_len: u64,
 }
 
 impl Default for SkyAdjointParams {
     fn default() -> Self {
         Self { layer_params: std::ptr::null(), band_params: std::ptr::null(), sample_layer_params: std::ptr::null(),
                sample_band_params: std::ptr::null(), sun_direction: [0.0; 3], estimator: SKY_ADJOINT_SEGMENT_INTEGRALS,
-               chain_radiance: std::ptr::null_mut() }
+               chain_radiance: std::ptr::null_mut(), chain_radiance_len: 0 }
     }
 }
 
@@ -229,7 +230,7 @@ mod layout {
         assert_eq!(size_of::<SkyRenderConfig>(), 80);
         assert_eq!(size_of::<SkyRenderStats>(), 96);
         assert_eq!(size_of::<SkyDeviceOutputs>(), 64);
-        assert_eq!(size_of::<SkyAdjointParams>(), 56);
+        assert_eq!(size_of::<SkyAdjointParams>(), 64);
         assert_eq!(size_of::<SkyAdjointGrads>(), 40);
     }
 }

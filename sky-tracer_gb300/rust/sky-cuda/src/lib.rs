@@ -238,6 +238,8 @@ pub struct AdjointParams {
     /// radiance, a backward at the same parameters and sun replays each chain
     /// once instead of twice.
     pub chain_radiance: *mut f32,
+    /// Floats in `chain_radiance` (the library refuses a shorter buffer).
+    pub chain_radiance_len: u64,
 }
 
 impl AdjointParams {
@@ -248,6 +250,7 @@ impl AdjointParams {
             sun_direction: self.sun_direction,
             estimator: self.estimator,
             chain_radiance: self.chain_radiance,
+            chain_radiance_len: self.chain_radiance_len,
             ..Default::default()
         }
     }

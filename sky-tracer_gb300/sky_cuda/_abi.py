@@ -121,7 +121,7 @@ class SkyBatchJob(ctypes.Structure):
 class SkyAdjointParams(ctypes.Structure):
     _fields_ = [
         ("layer_params", _vp), ("band_params", _vp), ("sample_layer_params", _vp), ("sample_band_params", _vp),
-        ("sun_direction", _f * 3), ("estimator", _u32), ("chain_radiance", _vp),
+        ("sun_direction", _f * 3), ("estimator", _u32), ("chain_radiance", _vp), ("chain_radiance_len", ctypes.c_uint64),
     ]
 
 

@@ -140,6 +140,7 @@ class AdjointRenderer:
                     str(chains.dtype) != "torch.float32":
                 raise ValueError(f"chains must be a contiguous float32 CUDA tensor of {self.chain_count} values")
             p.chain_radiance = chains.data_ptr()
+            p.chain_radiance_len = chains.numel()
         return p
 
     def check_status(self) -> None:

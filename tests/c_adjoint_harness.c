@@ -13,7 +13,8 @@
  * chain-radiance buffer, then the backward that reads it, and writes
  * OUT_PREFIX.film (float32), OUT_PREFIX.layer_grad and OUT_PREFIX.band_grad
  * (float64).  It also checks the refusals the crate maps to
- * RenderError::InvalidConfig (segment-restart tracking, a missing status).
+ * RenderError::InvalidConfig (segment-restart tracking, a chain buffer shorter
+ * than the render's chains, a missing status).
  * Exit status 0 on success, 2 without a CUDA device.
  */
 #include <stdint.h>
@@ -171,6 +172,7 @@ int main(int argc, char** argv) {
     p.band_params = band;
     p.estimator = SKY_ADJOINT_SEGMENT_INTEGRALS;
     p.chain_radiance = chains;
+    p.chain_radiance_len = cells * c.spp;
     SkyDeviceOutputs o;
     memset(&o, 0, sizeof(o));
     o.cell_sum = cell_sum;
@@ -198,6 +200,13 @@ int main(int argc, char** argv) {
     restart.tracking = SKY_TRACKING_SEGMENT_RESTART;
     if ((st = sky_cuda_adjoint_forward(scene, &restart, &p, &o, NULL)) != SKY_ERR_INVALID_CONFIG) {
         fprintf(stderr, "segment-restart tracking returned %d\n", st);
+        return 1;
+    }
+    /* a chain buffer shorter than the render's chains is refused */
+    SkyAdjointParams short_buffer = p;
+    short_buffer.chain_radiance_len = cells * c.spp - 1u;
+    if ((st = sky_cuda_adjoint_forward(scene, &c, &short_buffer, &o, NULL)) != SKY_ERR_INVALID_CONFIG) {
+        fprintf(stderr, "a short chain buffer returned %d\n", st);
         return 1;
     }
     SkyAdjointGrads no_status = g;
