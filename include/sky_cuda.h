@@ -514,6 +514,39 @@ int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderConfig* conf
                               const SkyAdjointGrads* grads, void* cuda_stream);
 
 /*
+ * One render of a differentiable batch: its config and sun (all zero = the
+ * params' sun, else the scene's), its outputs (forward: cell_sum required;
+ * outputs.status and outputs.counters of job 0 serve the whole batch), its
+ * dLoss/dfilm (backward) and its optional chain-radiance buffer (as
+ * SkyAdjointParams.chain_radiance, per render).
+ */
+typedef struct SkyAdjointJob {
+    SkyRenderConfig config;
+    float sun_direction[3];
+    float _reserved;
+    SkyDeviceOutputs outputs;
+    const float* dloss_dfilm;
+    float* chain_radiance;
+    uint64_t chain_radiance_len;
+} SkyAdjointJob;
+
+/*
+ * Batched forward / backward: `job_count` renders over one parameter set
+ * (params.layer_params / band_params / estimator; sample_* must be NULL and
+ * params.chain_radiance is not read) in one launch of the differentiable
+ * renderer per 32 renders, instead of one launch each: an elevation sweep of
+ * a fit renders all its suns in one launch per direction.  Every render needs
+ * the same tracking mode, phase sampling and accumulate flag.  The backward
+ * ADDS the gradient of sum_i Loss_i to grads->layer_grad / band_grad
+ * (grads->dloss_dfilm is not read: each job carries its own).  Asynchronous on
+ * `cuda_stream`.  No counterpart in the reference.
+ */
+int sky_cuda_adjoint_forward_batch(const SkyScene* scene, const SkyAdjointJob* jobs, uint32_t job_count,
+                                   const SkyAdjointParams* params, void* cuda_stream);
+int sky_cuda_adjoint_backward_batch(const SkyScene* scene, const SkyAdjointJob* jobs, uint32_t job_count,
+                                    const SkyAdjointParams* params, const SkyAdjointGrads* grads, void* cuda_stream);
+
+/*
  * Device majorant bake (compute_majorant_grid, medium.rs:63-102) of the
  * parameterised medium: writes majorants [band_count][majorant_layers] to
  * device memory.  With all scales 1 it reproduces the scene's own grid.

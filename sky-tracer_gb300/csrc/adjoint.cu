@@ -564,22 +564,43 @@ enum : uint32_t { kRayPrimary = 0u, kRayShadow = 1u, kRayRetrace = 2u };
 enum : uint32_t { kNextTrace = 0u, kNextStart = 1u, kNextPrimary = 2u, kNextLights = 3u, kNextEnd = 4u,
                   kNextIdle = 5u };
 
+// Render of global cell `g` in a launch: the last one whose first cell is <= g.
+__device__ __forceinline__ uint32_t adj_job_of(const AdjJobs& J, uint32_t g) {
+    uint32_t lo = 0u, hi = J.count;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (J.j[mid].cell_begin <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The slab cell (pixel-major, band-minor) of render-local claim index c
+// (band-major), and its band and pixel.
+__device__ __forceinline__ uint32_t adj_claimed_cell(const DevLaunch& L, uint32_t c, uint32_t& band, uint32_t& pixel) {
+    const uint32_t npix = L.width * L.rows;
+    band = c / npix;
+    pixel = c - band * npix;
+    return pixel * L.band_count + band;
+}
+
 // kCount: count events (counters given); without it the counters are never
 // read and their increments compile away.  kSegEst: the segment-integral
 // estimator (else null collisions); each instantiation holds only its own
-// gradient code.  Resident blocks: 4 per SM for the primal (64 registers),
-// 3 for the gradient passes (80 registers; 4 gains nothing there).
-template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
+// gradient code.  Resident blocks: 4 of 256 per SM (64 registers) for the
+// primal and the gradient passes (the latter spill ~150 B but hide more latency
+// than at 3 blocks and 80 registers).  J: the renders of the launch (one, or a
+// batch sharing the parameterised medium); their cells are numbered in a row.
+// kBatch: J holds more than one render (a single render reads J.j[0] at fixed
+// offsets, with no per-lane render index: 7 % faster).
+template <int kPhase, bool kGrad, bool kCount, bool kSegEst, bool kBatch>
 __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_constant__ AdjCtx A,
-                                                              const __grid_constant__ DevLaunch L,
-                                                              const float* __restrict__ dloss,
+                                                              const __grid_constant__ AdjJobs J,
                                                               double* __restrict__ layer_grad,
                                                               double* __restrict__ band_grad,
                                                               unsigned long long* __restrict__ counters,
-                                                              uint32_t* __restrict__ status, uint32_t cells,
-                                                              uint32_t copies, uint32_t* __restrict__ next_cell,
-                                                              double* __restrict__ cell_sum,
-                                                              double* __restrict__ cell_sumsq) {
+                                                              uint32_t* __restrict__ status,
+                                                              uint32_t copies, uint32_t* __restrict__ next_cell) {
     extern __shared__ float smem[];
     const DevScene& S = A.S;
     const uint32_t Lc = S.layer_count, B = S.band_count, bins = S.phase_bins;
@@ -593,20 +614,21 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
         for (uint32_t i = threadIdx.x; i < copies * nlayer + kAdjBandParams * B; i += blockDim.x) smem[i] = 0.0f;
         __syncthreads();
     }
+    const uint32_t cells = J.cells;
     // primal: FP64 sums of the lane's current cell
-    uint32_t acc_cell = 0xffffffffu;
+    uint32_t acc_cell = 0xffffffffu, acc_job = 0u;
     double acc_sum = 0.0, acc_sq = 0.0;
     Counters n;
     n.clear();
     bool watchdog = false;
-    const float inv_spp = 1.0f / float(L.spp), inv_lights = 1.0f / float(L.direct_light_samples);
     AdjAcc acc{sg, Lc, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     // the warp's cell and its next unclaimed sample (warp-uniform)
-    uint32_t claim_cell = 0u, claim_next = L.spp;
+    uint32_t claim_cell = 0u, claim_next = 0u, claim_spp = 0u, claim_job = 0u;
     uint32_t claim_band = 0u, claim_x = 0u, claim_y = 0u;  // divided out once per cell
     bool exhausted = false;
     // the lane's chain
-    uint32_t next = kNextIdle, pass = 0u, cell = 0u, sample = 0u, band = 0u, px = 0u, py = 0u, ray = kRayPrimary,
+    uint32_t next = kNextIdle, pass = 0u, job = 0u, cell = 0u, sample = 0u, band = 0u, px = 0u, py = 0u,
+             ray = kRayPrimary,
              depth = 0u,
              ls = 0u, boundary = 0u, dim0 = 0u, dim1 = 0u;
     bool ground = false;
@@ -626,31 +648,38 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
             for (;;) {
                 const uint32_t need = __ballot_sync(0xffffffffu, next == kNextIdle);
                 if (need == 0u || exhausted) break;
-                if (claim_next >= L.spp) {
+                if (claim_next >= claim_spp) {
                     // claims run band-major, as in the wavefront tracer (the warps of an SM
                     // share a band's tables in L1); cells keep the pixel-major layout
-                    const uint32_t npix = L.width * L.rows;
                     uint32_t cn = 0u;
                     if (lane == 0u) {
-                        do cn = atomicAdd(next_cell, 1u);
-                        while (kGrad && cn < cells &&
-                               __ldg(dloss + (cn % npix) * L.band_count + cn / npix) == 0.0f);  // no loss: no gradient
+                        for (;;) {
+                            cn = atomicAdd(next_cell, 1u);
+                            if (!kGrad || cn >= cells) break;
+                            const AdjJob& Jc = J.j[kBatch ? adj_job_of(J, cn) : 0u];
+                            uint32_t b_, p_;
+                            const uint32_t lc = adj_claimed_cell(Jc.L, cn - Jc.cell_begin, b_, p_);
+                            if (__ldg(Jc.dloss + lc) != 0.0f) break;  // no loss: no gradient
+                        }
                     }
                     cn = __shfl_sync(0xffffffffu, cn, 0);
                     if (cn >= cells) {
                         exhausted = true;
                         break;
                     }
-                    claim_band = cn / npix;
-                    const uint32_t pixel = cn - claim_band * npix;
-                    claim_cell = pixel * L.band_count + claim_band;
-                    const uint32_t row = pixel / L.width;  // row within the slab
-                    claim_x = pixel - row * L.width;
-                    claim_y = row + L.row_begin;
+                    claim_job = kBatch ? adj_job_of(J, cn) : 0u;
+                    const DevLaunch& CL = J.j[claim_job].L;
+                    uint32_t pixel;
+                    claim_cell = adj_claimed_cell(CL, cn - J.j[claim_job].cell_begin, claim_band, pixel);
+                    const uint32_t row = pixel / CL.width;  // row within the slab
+                    claim_x = pixel - row * CL.width;
+                    claim_y = row + CL.row_begin;
+                    claim_spp = CL.spp;
                     claim_next = 0u;
                 }
                 const uint32_t rank = __popc(need & ((1u << lane) - 1u));
-                if (next == kNextIdle && claim_next + rank < L.spp) {
+                if (next == kNextIdle && claim_next + rank < claim_spp) {
+                    job = claim_job;
                     cell = claim_cell;
                     band = claim_band;
                     px = claim_x;
@@ -659,14 +688,16 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                     pass = 0u;
                     next = kNextStart;
                 }
-                claim_next = min(L.spp, claim_next + uint32_t(__popc(need)));
+                claim_next = min(claim_spp, claim_next + uint32_t(__popc(need)));
             }
             // event code up to the lane's next ray
 #pragma unroll 1
             while (next != kNextIdle && next != kNextTrace) {
+                const AdjJob& JJ = J.j[kBatch ? job : 0u];
+                const DevLaunch& L = JJ.L;
                 if (next == kNextEnd) {
                     if (!kGrad) {
-                        if (A.chain_rad) A.chain_rad[uint64_t(cell) * L.spp + sample] = rad;
+                        if (JJ.chain_rad) JJ.chain_rad[uint64_t(cell) * L.spp + sample] = rad;
                         const double rd = double(resolve(A.P, Lc, band).kS * rad);
                         acc_sum += rd;
                         acc_sq += rd * rd;
@@ -696,19 +727,21 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                     continue;
                 }
                 if (next == kNextStart) {
-                    if (!kGrad && cell != acc_cell) {
+                    if (!kGrad && (cell != acc_cell || (kBatch && job != acc_job))) {
                         if (acc_cell != 0xffffffffu) {
-                            atomicAdd(cell_sum + acc_cell, acc_sum);
-                            if (cell_sumsq) atomicAdd(cell_sumsq + acc_cell, acc_sq);
+                            const AdjJob& JA = J.j[kBatch ? acc_job : 0u];
+                            atomicAdd(JA.cell_sum + acc_cell, acc_sum);
+                            if (JA.cell_sumsq) atomicAdd(JA.cell_sumsq + acc_cell, acc_sq);
                         }
+                        acc_job = job;
                         acc_cell = cell;
                         acc_sum = acc_sq = 0.0;
                     }
                     const uint32_t pixel = py * L.width + px;
-                    wc = kGrad ? __ldg(dloss + cell) * inv_spp : 0.0f;
-                    if (kGrad && pass == 0u && A.chain_rad) {
+                    wc = kGrad ? __ldg(JJ.dloss + cell) * (1.0f / float(L.spp)) : 0.0f;
+                    if (kGrad && pass == 0u && JJ.chain_rad) {
                         // the forward's radiance of this chain stands in for its first trace
-                        total = __ldg(A.chain_rad + uint64_t(cell) * L.spp + sample);
+                        total = __ldg(JJ.chain_rad + uint64_t(cell) * L.spp + sample);
                         if (!(total > 0.0f)) {
                             if (total != 0.0f) atomicAdd(sb + band * kAdjBandParams + 3u, wc * total);
                             next = kNextIdle;
@@ -751,7 +784,7 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                 bool shadow = false;
                 while (ls < L.direct_light_samples) {
                     ++ls;
-                    const V3 ldir = sample_sun_cone(S, rng);
+                    const V3 ldir = sample_sun_cone(JJ.sun, JJ.sun_t, JJ.sun_b, S.one_minus_cos_max, rng);
                     ++n.e[SKY_EVENT_NEE];
                     float cos_sun = 0.0f;
                     if (ground) {
@@ -771,7 +804,7 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                         const float ph = mp.s > 0.0f ? vertex_phase(P, bins, mp, mu) / mp.s : 0.0f;
                         term = l_sun * ph / S.light_pdf;
                     }
-                    c = w * thr * term * inv_lights;
+                    c = w * thr * term * (1.0f / float(L.direct_light_samples));
                     shadow = true;
                     break;
                 }
@@ -780,7 +813,7 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                     next = kNextTrace;
                     continue;
                 }
-                rad += thr * (nee * inv_lights);
+                rad += thr * (nee * (1.0f / float(L.direct_light_samples)));
                 // each branch draws its angles; one shared frame step turns them into
                 // the direction (as direction_from_axis_mu / sample_cosine_hemisphere)
                 V3 nd = mk(0.0f, 1.0f, 0.0f), axis = dir;
@@ -901,7 +934,7 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
                         next = kNextLights;
                     }
                 } else if (boundary == 1u) {
-                    if (depth == 0u && dot3(dir, load3(S.sun)) >= S.cos_max)
+                    if (depth == 0u && dot3(dir, load3(J.j[kBatch ? job : 0u].sun)) >= S.cos_max)
                         rad += thr * __ldg(&S.bands[band].solar_radiance);
                     rad = fmaxf(rad, 0.0f);
                     next = kNextEnd;
@@ -937,8 +970,9 @@ __global__ void __launch_bounds__(256, 4) adjoint_grad_kernel(const __grid_const
     if (__any_sync(0xffffffffu, watchdog) && lane == 0) atomicOr(status, 1u);
     if (!kGrad) {
         if (acc_cell != 0xffffffffu) {
-            atomicAdd(cell_sum + acc_cell, acc_sum);
-            if (cell_sumsq) atomicAdd(cell_sumsq + acc_cell, acc_sq);
+            const AdjJob& JA = J.j[kBatch ? acc_job : 0u];
+            atomicAdd(JA.cell_sum + acc_cell, acc_sum);
+            if (JA.cell_sumsq) atomicAdd(JA.cell_sumsq + acc_cell, acc_sq);
         }
         return;
     }
@@ -1126,104 +1160,103 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
     return cudaGetLastError();
 }
 
+// Kernel arguments may hold up to 32764 bytes on this architecture.
+static_assert(sizeof(AdjCtx) + sizeof(AdjJobs) + 64 <= 32000, "ray-loop kernel arguments exceed the limit");
+
 // One launch of the ray-loop kernel, persistent grid.
-template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
-cudaError_t launch_ray_loop_est(const AdjCtx& A, const DevLaunch& L, const float* dloss, double* layer_grad,
-                            double* band_grad, unsigned long long* counters, uint32_t* status, uint32_t cells,
-                            uint32_t copies, uint32_t* next_cell, double* cell_sum, double* cell_sumsq, size_t smem,
-                            uint64_t want, cudaStream_t stream) {
-    const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst>);
-    adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst><<<grid_blocks(k, 256, smem, want), 256, smem, stream>>>(
-        A, L, dloss, layer_grad, band_grad, counters, status, cells, copies, next_cell, cell_sum, cell_sumsq);
+template <int kPhase, bool kGrad, bool kCount, bool kSegEst, bool kBatch>
+cudaError_t launch_ray_loop_shape(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                                  unsigned long long* counters, uint32_t* status, uint32_t copies,
+                                  uint32_t* next_cell, size_t smem, cudaStream_t stream) {
+    const void* k = reinterpret_cast<const void*>(adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst, kBatch>);
+    const uint64_t want = (uint64_t(J.cells) * 32u + 255u) / 256u;  // a warp per cell at most
+    adjoint_grad_kernel<kPhase, kGrad, kCount, kSegEst, kBatch>
+        <<<grid_blocks(k, 256, smem, want), 256, smem, stream>>>(A, J, layer_grad, band_grad, counters, status,
+                                                                 copies, next_cell);
     return cudaGetLastError();
+}
+
+template <int kPhase, bool kGrad, bool kCount, bool kSegEst>
+cudaError_t launch_ray_loop_est(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                                unsigned long long* counters, uint32_t* status, uint32_t copies, uint32_t* next_cell,
+                                size_t smem, cudaStream_t stream) {
+    if (J.count > 1u)
+        return launch_ray_loop_shape<kPhase, kGrad, kCount, kSegEst, true>(A, J, layer_grad, band_grad, counters,
+                                                                           status, copies, next_cell, smem, stream);
+    return launch_ray_loop_shape<kPhase, kGrad, kCount, kSegEst, false>(A, J, layer_grad, band_grad, counters, status,
+                                                                        copies, next_cell, smem, stream);
 }
 
 // The estimator's instantiation (the primal needs no gradient code: segment form).
 template <int kPhase, bool kGrad, bool kCount>
-cudaError_t launch_ray_loop(const AdjCtx& A, const DevLaunch& L, const float* dloss, double* layer_grad,
-                            double* band_grad, unsigned long long* counters, uint32_t* status, uint32_t cells,
-                            uint32_t copies, uint32_t* next_cell, double* cell_sum, double* cell_sumsq, size_t smem,
-                            uint64_t want, cudaStream_t stream) {
+cudaError_t launch_ray_loop(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                            unsigned long long* counters, uint32_t* status, uint32_t copies, uint32_t* next_cell,
+                            size_t smem, cudaStream_t stream) {
     if (kGrad && A.estimator == SKY_ADJOINT_NULL_COLLISIONS)
-        return launch_ray_loop_est<kPhase, kGrad, kCount, false>(A, L, dloss, layer_grad, band_grad, counters, status,
-                                                                 cells, copies, next_cell, cell_sum, cell_sumsq,
-                                                                 smem, want, stream);
-    return launch_ray_loop_est<kPhase, kGrad, kCount, true>(A, L, dloss, layer_grad, band_grad, counters, status,
-                                                            cells, copies, next_cell, cell_sum, cell_sumsq, smem,
-                                                            want, stream);
+        return launch_ray_loop_est<kPhase, kGrad, kCount, false>(A, J, layer_grad, band_grad, counters, status, copies,
+                                                                 next_cell, smem, stream);
+    return launch_ray_loop_est<kPhase, kGrad, kCount, true>(A, J, layer_grad, band_grad, counters, status, copies,
+                                                            next_cell, smem, stream);
 }
 
-cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
-                                  bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  uint32_t* next_cell, cudaStream_t stream) {
-    const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;  // the slab's cells
+template <bool kGrad>
+cudaError_t launch_ray_loop_phase(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                                  unsigned long long* counters, uint32_t* status, uint32_t copies,
+                                  uint32_t* next_cell, size_t smem, cudaStream_t stream) {
+    if (J.j[0].L.phase_sampling == SKY_PHASE_TABULATED)
+        return counters ? launch_ray_loop<SKY_PHASE_TABULATED, kGrad, true>(A, J, layer_grad, band_grad, counters,
+                                                                             status, copies, next_cell, smem, stream)
+                        : launch_ray_loop<SKY_PHASE_TABULATED, kGrad, false>(A, J, layer_grad, band_grad, counters,
+                                                                              status, copies, next_cell, smem, stream);
+    return counters ? launch_ray_loop<SKY_PHASE_ISOTROPIC, kGrad, true>(A, J, layer_grad, band_grad, counters, status,
+                                                                         copies, next_cell, smem, stream)
+                    : launch_ray_loop<SKY_PHASE_ISOTROPIC, kGrad, false>(A, J, layer_grad, band_grad, counters,
+                                                                          status, copies, next_cell, smem, stream);
+}
+
+cudaError_t launch_adjoint_primal(const AdjCtx& A, const AdjJobs& J, bool accumulate, unsigned long long* counters,
+                                  uint32_t* status, uint32_t* next_cell, cudaStream_t stream) {
     cudaError_t e;
-    if (!A.distinct && cells <= 0xffffffffull) {
+    if (!A.distinct) {
         // P = Q: the ray loop, adding into the cell sums
-        if (!accumulate) {
-            if ((e = cudaMemsetAsync(cell_sum, 0, cells * sizeof(double), stream)) != cudaSuccess) return e;
-            if (cell_sumsq && (e = cudaMemsetAsync(cell_sumsq, 0, cells * sizeof(double), stream)) != cudaSuccess)
-                return e;
-        }
+        if (!accumulate)
+            for (uint32_t i = 0; i < J.count; ++i) {
+                const AdjJob& j = J.j[i];
+                if ((e = cudaMemsetAsync(j.cell_sum, 0, size_t(j.cell_count) * sizeof(double), stream)) != cudaSuccess)
+                    return e;
+                if (j.cell_sumsq &&
+                    (e = cudaMemsetAsync(j.cell_sumsq, 0, size_t(j.cell_count) * sizeof(double), stream)) != cudaSuccess)
+                    return e;
+            }
         if ((e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream)) != cudaSuccess) return e;
-        const uint64_t want = (cells * 32u + 255u) / 256u;
-        const uint32_t n = static_cast<uint32_t>(cells);
-        if (L.phase_sampling == SKY_PHASE_TABULATED)
-            e = counters ? launch_ray_loop<SKY_PHASE_TABULATED, false, true>(A, L, nullptr, nullptr, nullptr, counters,
-                                                                               status, n, 0u, next_cell, cell_sum,
-                                                                               cell_sumsq, 0, want, stream)
-                         : launch_ray_loop<SKY_PHASE_TABULATED, false, false>(A, L, nullptr, nullptr, nullptr, counters,
-                                                                                status, n, 0u, next_cell, cell_sum,
-                                                                                cell_sumsq, 0, want, stream);
-        else
-            e = counters ? launch_ray_loop<SKY_PHASE_ISOTROPIC, false, true>(A, L, nullptr, nullptr, nullptr, counters,
-                                                                               status, n, 0u, next_cell, cell_sum,
-                                                                               cell_sumsq, 0, want, stream)
-                         : launch_ray_loop<SKY_PHASE_ISOTROPIC, false, false>(A, L, nullptr, nullptr, nullptr, counters,
-                                                                                status, n, 0u, next_cell, cell_sum,
-                                                                                cell_sumsq, 0, want, stream);
-        return e;
+        return launch_ray_loop_phase<false>(A, J, nullptr, nullptr, counters, status, 0u, next_cell, 0, stream);
     }
-    // sampling under Q, evaluation under P: a warp per cell
+    // sampling under Q, evaluation under P: a warp per cell (one render)
+    const AdjJob& j = J.j[0];
+    const uint64_t cells = j.cell_count;
     const uint64_t blocks = (cells * 32u + 255u) / 256u;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     const dim3 grid(static_cast<uint32_t>(blocks));
     const uint32_t acc = accumulate ? 1u : 0u;
-    if (L.phase_sampling == SKY_PHASE_TABULATED)
+    if (j.L.phase_sampling == SKY_PHASE_TABULATED)
         adjoint_primal_kernel<SKY_PHASE_TABULATED>
-            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+            <<<grid, 256, 0, stream>>>(A, j.L, j.cell_sum, j.cell_sumsq, acc, counters, status, cells);
     else
         adjoint_primal_kernel<SKY_PHASE_ISOTROPIC>
-            <<<grid, 256, 0, stream>>>(A, L, cell_sum, cell_sumsq, acc, counters, status, cells);
+            <<<grid, 256, 0, stream>>>(A, j.L, j.cell_sum, j.cell_sumsq, acc, counters, status, cells);
     return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
-                                double* band_grad, unsigned long long* counters, uint32_t* status,
-                                uint32_t* next_cell, cudaStream_t stream) {
-    const uint64_t cells = uint64_t(L.width) * L.rows * L.band_count;  // the slab's cells
-    if (cells > 0xffffffffull) return cudaErrorInvalidConfiguration;  // the cell counter is 32-bit
+cudaError_t launch_adjoint_grad(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                                unsigned long long* counters, uint32_t* status, uint32_t* next_cell,
+                                cudaStream_t stream) {
     cudaError_t e = cudaMemsetAsync(next_cell, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     const size_t nlayer = size_t(3u * A.S.layer_count + 2u), nband = size_t(kAdjBandParams) * A.S.band_count;
     // one layer-gradient copy per warp while it stays within the default 48 KB
     const uint32_t copies = (8 * nlayer + nband) * sizeof(float) <= 48u * 1024u ? 8u : 1u;
     const size_t smem = (copies * nlayer + nband) * sizeof(float);
-    const uint64_t want = (cells * 32u + 255u) / 256u;
-    const uint32_t n = static_cast<uint32_t>(cells);
-    if (L.phase_sampling == SKY_PHASE_TABULATED)
-        return counters ? launch_ray_loop<SKY_PHASE_TABULATED, true, true>(A, L, dloss_dfilm, layer_grad, band_grad,
-                                                                            counters, status, n, copies, next_cell,
-                                                                            nullptr, nullptr, smem, want, stream)
-                        : launch_ray_loop<SKY_PHASE_TABULATED, true, false>(A, L, dloss_dfilm, layer_grad, band_grad,
-                                                                             counters, status, n, copies, next_cell,
-                                                                             nullptr, nullptr, smem, want, stream);
-    return counters ? launch_ray_loop<SKY_PHASE_ISOTROPIC, true, true>(A, L, dloss_dfilm, layer_grad, band_grad,
-                                                                        counters, status, n, copies, next_cell,
-                                                                        nullptr, nullptr, smem, want, stream)
-                    : launch_ray_loop<SKY_PHASE_ISOTROPIC, true, false>(A, L, dloss_dfilm, layer_grad, band_grad,
-                                                                         counters, status, n, copies, next_cell,
-                                                                         nullptr, nullptr, smem, want, stream);
+    return launch_ray_loop_phase<true>(A, J, layer_grad, band_grad, counters, status, copies, next_cell, smem, stream);
 }
 
 }  // namespace sky

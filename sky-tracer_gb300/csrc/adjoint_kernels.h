@@ -50,11 +50,33 @@ struct AdjCtx {
     uint32_t merge;        // merge uniform layers into tracking layers (else one per layer)
     float crossing_cost;   // merge cost of a shell crossing, in optical-depth units
     uint32_t estimator;    // SkyAdjointEstimator of the backward pass
+};
+
+// One render of a ray-loop launch: its launch constants and sun frame (the
+// renders of a batch share the parameterised medium and differ in sun and
+// view), its outputs and its range of the launch's cells.  Cells are the
+// render's (pixel, band) pairs, band-major in the claim order.
+struct AdjJob {
+    DevLaunch L;
+    float sun[3], sun_t[3], sun_b[3];
+    const float* dloss;   // gradient pass: dLoss/dfilm [pixels][bands]
+    double* cell_sum;     // primal: FP64 sums [pixels][bands]
+    double* cell_sumsq;
     // Optional [cells][spp] radiance of every chain (SkyAdjointParams::chain_radiance):
-    // written by the primal ray loop, read by the gradient pass in place of its first
-    // trace of each chain.
+    // written by the primal, read by the gradient pass in place of its first trace
+    // of each chain.
     float* chain_rad;
-    uint64_t chain_rad_len;  // floats in chain_rad (checked against the render's chains)
+    uint32_t cell_begin;  // first global cell of the render in the launch
+    uint32_t cell_count;
+};
+
+// The renders of one launch, passed by value as a kernel parameter (no job
+// table in device memory; a larger batch takes several launches).
+constexpr uint32_t kAdjMaxJobs = 32;
+struct AdjJobs {
+    AdjJob j[kAdjMaxJobs];
+    uint32_t count;
+    uint32_t cells;  // sum of the renders' cells
 };
 
 // Writable views of the tables the prepare kernel fills.
@@ -80,14 +102,16 @@ cudaError_t launch_adjoint_prepare(const AdjCtx& A, const AdjWorkspace& W, cudaS
 // of the radiance of P, sampled with Q.  With P = Q it runs the ray loop of
 // the adjoint kernel (next_cell is its work counter); otherwise a warp per
 // cell.
-cudaError_t launch_adjoint_primal(const AdjCtx& A, const DevLaunch& L, double* cell_sum, double* cell_sumsq,
-                                  bool accumulate, unsigned long long* counters, uint32_t* status,
-                                  uint32_t* next_cell, cudaStream_t stream);
+// A batch (J) takes the ray loop and needs P = Q; the warp-per-cell form
+// renders J.j[0] alone.
+cudaError_t launch_adjoint_primal(const AdjCtx& A, const AdjJobs& J, bool accumulate, unsigned long long* counters,
+                                  uint32_t* status, uint32_t* next_cell, cudaStream_t stream);
 
 // Path-replay gradient (P == Q): adds dLoss/dparams to layer_grad [3 L + 2]
-// and band_grad [B][4] (may be null) given dLoss/dfilm [pixels][B].
-cudaError_t launch_adjoint_grad(const AdjCtx& A, const DevLaunch& L, const float* dloss_dfilm, double* layer_grad,
-                                double* band_grad, unsigned long long* counters, uint32_t* status,
-                                uint32_t* next_cell, cudaStream_t stream);
+// and band_grad [B][4] (may be null) given each render's dLoss/dfilm
+// [pixels][B] (J.j[i].dloss).
+cudaError_t launch_adjoint_grad(const AdjCtx& A, const AdjJobs& J, double* layer_grad, double* band_grad,
+                                unsigned long long* counters, uint32_t* status, uint32_t* next_cell,
+                                cudaStream_t stream);
 
 }  // namespace sky

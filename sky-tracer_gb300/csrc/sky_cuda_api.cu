@@ -921,8 +921,6 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
     }
     if (p->chain_radiance && A.distinct)
         return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance cannot be used with sample_* parameters");
-    A.chain_rad = p->chain_radiance;
-    A.chain_rad_len = p->chain_radiance_len;
     A.G.layer_maj = W.layer_maj;
     A.G.radius = W.radius;
     A.G.maj = W.maj;
@@ -935,7 +933,12 @@ int adjoint_setup(SkyScene* s, const SkyAdjointParams* p, AdjCtx& A, AdjWorkspac
     return SKY_OK;
 }
 
-int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& L) {
+// One render of a differentiable launch: its launch constants for its sun (a
+// non-zero sun_direction, else the context's sun), its sun frame and its
+// chain-radiance buffer.  The first render of a launch sets the tracking mode
+// (A.merge) the others must share.
+int adjoint_job(SkyScene* s, const SkyRenderConfig* c, const float* sun_direction, float* chain_rad,
+                uint64_t chain_len, bool first, AdjCtx& A, AdjJob& job) {
     int st = validate_config(s, c);
     if (st) return st;
     // the ray loop's 32-bit cell counter also counts one failed claim per warp
@@ -944,18 +947,50 @@ int adjoint_config(SkyScene* s, const SkyRenderConfig* c, AdjCtx& A, DevLaunch& 
     if (c->tracking != SKY_TRACKING_RESIDUAL_CARRY && c->tracking != SKY_TRACKING_MERGED_LAYERS)
         return set_error(SKY_ERR_INVALID_CONFIG,
                          "differentiable renders track with SKY_TRACKING_RESIDUAL_CARRY or SKY_TRACKING_MERGED_LAYERS");
-    A.merge = c->tracking == SKY_TRACKING_MERGED_LAYERS ? 1u : 0u;
+    const uint32_t merge = c->tracking == SKY_TRACKING_MERGED_LAYERS ? 1u : 0u;
+    if (first) A.merge = merge;
+    else if (merge != A.merge) return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same tracking");
+    job = AdjJob{};
     SkyScene view;  // launch constants (sky-view LUT frame) for the render's sun
     view.dev = A.S;
-    L = make_launch(&view, c);
+    const float len = sun_direction ? std::sqrt(sun_direction[0] * sun_direction[0] +
+                                                sun_direction[1] * sun_direction[1] +
+                                                sun_direction[2] * sun_direction[2])
+                                    : 0.0f;
+    if (len > 0.0f) {
+        if (!std::isfinite(len)) return set_error(SKY_ERR_INVALID_CONFIG, "sun direction must be finite");
+        for (int k = 0; k < 3; ++k) view.dev.sun[k] = sun_direction[k] / len;
+        host_orthonormal_basis(view.dev.sun, view.dev.sun_t, view.dev.sun_b);
+    }
+    job.L = make_launch(&view, c);
+    for (int k = 0; k < 3; ++k) {
+        job.sun[k] = view.dev.sun[k];
+        job.sun_t[k] = view.dev.sun_t[k];
+        job.sun_b[k] = view.dev.sun_b[k];
+    }
     view.dev = DevScene{};
-    if (A.chain_rad) {
-        const uint64_t chains = slab_pixels(c) * uint64_t(s->dev.band_count) * c->spp;
-        if (A.chain_rad_len < chains)
-            return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance holds " + std::to_string(A.chain_rad_len) +
+    const uint64_t cells = slab_pixels(c) * uint64_t(s->dev.band_count);
+    job.cell_count = uint32_t(cells);
+    if (chain_rad) {
+        if (A.distinct)
+            return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance cannot be used with sample_* parameters");
+        const uint64_t chains = cells * c->spp;
+        if (chain_len < chains)
+            return set_error(SKY_ERR_INVALID_CONFIG, "chain_radiance holds " + std::to_string(chain_len) +
                                                          " floats; the render has " + std::to_string(chains) +
                                                          " chains");
     }
+    job.chain_rad = chain_rad;
+    return SKY_OK;
+}
+
+// Append `job` to the launch J (cells numbered in a row).
+int adjoint_place(AdjJobs& J, AdjJob& job) {
+    if (uint64_t(J.cells) + job.cell_count > kMaxLaunchCells)
+        return set_error(SKY_ERR_INVALID_CONFIG, "a launch holds at most 4026531840 (pixel, band) cells");
+    job.cell_begin = J.cells;
+    J.j[J.count++] = job;
+    J.cells += job.cell_count;
     return SKY_OK;
 }
 
@@ -965,61 +1000,200 @@ extern "C" uint32_t sky_cuda_adjoint_param_count(const SkyScene* scene) {
     return scene ? 3u * scene->dev.layer_count + 2u : 0u;
 }
 
+namespace {
+
+// The primal launches of renders `jobs` (n of them, outputs[i] each) over one
+// parameter set, in launches of at most kAdjMaxJobs renders, then each
+// render's finalize.  The context's tables are baked first, once.
+int adjoint_forward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const SkyRenderConfig* const* configs,
+                         const float* const* suns, float* const* chains, const uint64_t* chain_lens,
+                         const SkyDeviceOutputs* const* outputs, uint32_t n, cudaStream_t stream) {
+    if (n == 0) return set_error(SKY_ERR_INVALID_CONFIG, "at least one render is required");
+    if (!outputs[0]->status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.status is required");
+    if (A.distinct && n > 1)
+        return set_error(SKY_ERR_INVALID_CONFIG, "a batch is rendered at its sampling parameters: no sample_*");
+    AdjJobs J;
+    std::memset(&J, 0, sizeof(J));
+    int st;
+    bool prepared = false;
+    for (uint32_t i0 = 0; i0 < n; i0 += kAdjMaxJobs) {
+        J.count = 0;
+        J.cells = 0;
+        const uint32_t i1 = std::min(n, i0 + kAdjMaxJobs);
+        bool accumulate = false;
+        for (uint32_t i = i0; i < i1; ++i) {
+            AdjJob job;
+            if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
+            if (!outputs[i] || !outputs[i]->cell_sum)
+                return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
+            if (configs[i]->phase_sampling != configs[0]->phase_sampling)
+                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
+            const bool acc_i = (configs[i]->flags & SKY_FLAG_ACCUMULATE) != 0;
+            if (i > i0 && acc_i != accumulate)
+                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch accumulate, or none");
+            accumulate = acc_i;
+            job.cell_sum = outputs[i]->cell_sum;
+            job.cell_sumsq = outputs[i]->cell_sumsq;
+            if ((st = adjoint_place(J, job))) return st;
+        }
+        clear_stale_error();
+        cudaError_t e;
+        if (!prepared) {
+            if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
+                return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+            prepared = true;
+        }
+        e = launch_adjoint_primal(A, J, accumulate, outputs[0]->counters, outputs[0]->status, W.next_cell, stream);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
+        for (uint32_t i = i0; i < i1; ++i) {
+            const SkyRenderConfig* c = configs[i];
+            const uint32_t total_spp =
+                (c->flags & SKY_FLAG_ACCUMULATE) != 0 ? c->sample_offset + c->spp : c->spp;
+            const SkyDeviceOutputs* o = outputs[i];
+            e = launch_finalize(A.S, slab_pixels(c), total_spp, o->cell_sum, o->cell_sumsq, o->film,
+                                s->has_xyz ? o->xyz : nullptr, s->has_xyz ? o->xyz_var : nullptr,
+                                s->has_xyz ? o->rgb : nullptr, stream);
+            if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
+        }
+    }
+    return SKY_OK;
+}
+
+// The gradient launches of renders over one parameter set (dloss[i] each).
+int adjoint_backward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const SkyRenderConfig* const* configs,
+                          const float* const* suns, float* const* chains, const uint64_t* chain_lens,
+                          const float* const* dloss, uint32_t n, const SkyAdjointGrads* grads,
+                          cudaStream_t stream) {
+    if (n == 0) return set_error(SKY_ERR_INVALID_CONFIG, "at least one render is required");
+    if (!grads || (!grads->layer_grad && !grads->band_grad))
+        return set_error(SKY_ERR_INVALID_CONFIG, "at least one of grads.layer_grad, grads.band_grad is required");
+    if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
+    AdjJobs J;
+    std::memset(&J, 0, sizeof(J));
+    int st;
+    bool prepared = false;
+    for (uint32_t i0 = 0; i0 < n; i0 += kAdjMaxJobs) {
+        J.count = 0;
+        J.cells = 0;
+        const uint32_t i1 = std::min(n, i0 + kAdjMaxJobs);
+        for (uint32_t i = i0; i < i1; ++i) {
+            AdjJob job;
+            if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
+            if (!dloss[i]) return set_error(SKY_ERR_INVALID_CONFIG, "dloss_dfilm is required for every render");
+            if (configs[i]->phase_sampling != configs[0]->phase_sampling)
+                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
+            job.dloss = dloss[i];
+            if ((st = adjoint_place(J, job))) return st;
+        }
+        clear_stale_error();
+        cudaError_t e;
+        if (!prepared) {
+            if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
+                return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+            prepared = true;
+        }
+        e = launch_adjoint_grad(A, J, grads->layer_grad, grads->band_grad, grads->counters, grads->status, W.next_cell,
+                                stream);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);
+    }
+    return SKY_OK;
+}
+
+int require_sampling_at_evaluation(const SkyAdjointParams* params) {
+    if (params && (params->sample_layer_params || params->sample_band_params))
+        return set_error(SKY_ERR_INVALID_CONFIG,
+                         "the gradient is taken at the sampling parameters: sample_layer_params and "
+                         "sample_band_params must be NULL");
+    return SKY_OK;
+}
+
+}  // namespace
+
 extern "C" int sky_cuda_adjoint_forward(const SkyScene* scene, const SkyRenderConfig* config,
                                         const SkyAdjointParams* params, const SkyDeviceOutputs* outputs,
                                         void* cuda_stream) {
     SkyScene* s = const_cast<SkyScene*>(scene);
     AdjCtx A;
     AdjWorkspace W;
-    DevLaunch L;
     int st = adjoint_setup(s, params, A, W);
     if (st) return st;
-    if ((st = adjoint_config(s, config, A, L))) return st;
-    if (!outputs || !outputs->cell_sum) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
-    if (!outputs->status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.status is required");
-    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
-    const bool accumulate = (config->flags & SKY_FLAG_ACCUMULATE) != 0;
-    const uint32_t total_spp = accumulate ? config->sample_offset + config->spp : config->spp;
-    const uint64_t pixels = slab_pixels(config);
-    clear_stale_error();
-    cudaError_t e = launch_adjoint_prepare(A, W, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
-    e = launch_adjoint_primal(A, L, outputs->cell_sum, outputs->cell_sumsq, accumulate, outputs->counters,
-                              outputs->status, W.next_cell, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
-    e = launch_finalize(A.S, pixels, total_spp, outputs->cell_sum, outputs->cell_sumsq, outputs->film,
-                        s->has_xyz ? outputs->xyz : nullptr, s->has_xyz ? outputs->xyz_var : nullptr,
-                        s->has_xyz ? outputs->rgb : nullptr, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
-    return SKY_OK;
+    if (!outputs) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
+    const float* sun = nullptr;  // the context's sun: the params' or the scene's
+    float* chain = params->chain_radiance;
+    const uint64_t chain_len = params->chain_radiance_len;
+    return adjoint_forward_jobs(s, A, W, &config, &sun, &chain, &chain_len, &outputs, 1,
+                                static_cast<cudaStream_t>(cuda_stream));
 }
 
 extern "C" int sky_cuda_adjoint_backward(const SkyScene* scene, const SkyRenderConfig* config,
                                          const SkyAdjointParams* params, const SkyAdjointGrads* grads,
                                          void* cuda_stream) {
     SkyScene* s = const_cast<SkyScene*>(scene);
-    if (params && (params->sample_layer_params || params->sample_band_params))
-        return set_error(SKY_ERR_INVALID_CONFIG,
-                         "the gradient is taken at the sampling parameters: sample_layer_params and "
-                         "sample_band_params must be NULL");
+    int st = require_sampling_at_evaluation(params);
+    if (st) return st;
     AdjCtx A;
     AdjWorkspace W;
-    DevLaunch L;
-    int st = adjoint_setup(s, params, A, W);
-    if (st) return st;
-    if ((st = adjoint_config(s, config, A, L))) return st;
+    if ((st = adjoint_setup(s, params, A, W))) return st;
     if (!grads || !grads->dloss_dfilm || (!grads->layer_grad && !grads->band_grad))
         return set_error(SKY_ERR_INVALID_CONFIG,
                          "grads.dloss_dfilm and at least one of grads.layer_grad, grads.band_grad are required");
-    if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
-    cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
-    clear_stale_error();
-    cudaError_t e = launch_adjoint_prepare(A, W, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
-    e = launch_adjoint_grad(A, L, grads->dloss_dfilm, grads->layer_grad, grads->band_grad, grads->counters,
-                            grads->status, W.next_cell, stream);
-    if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);
-    return SKY_OK;
+    const float* sun = nullptr;
+    float* chain = params->chain_radiance;
+    const uint64_t chain_len = params->chain_radiance_len;
+    const float* dloss = grads->dloss_dfilm;
+    return adjoint_backward_jobs(s, A, W, &config, &sun, &chain, &chain_len, &dloss, 1, grads,
+                                 static_cast<cudaStream_t>(cuda_stream));
+}
+
+extern "C" int sky_cuda_adjoint_forward_batch(const SkyScene* scene, const SkyAdjointJob* jobs, uint32_t job_count,
+                                              const SkyAdjointParams* params, void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    int st = require_sampling_at_evaluation(params);
+    if (st) return st;
+    if (!jobs || job_count == 0) return set_error(SKY_ERR_INVALID_CONFIG, "jobs and job_count >= 1 are required");
+    AdjCtx A;
+    AdjWorkspace W;
+    if ((st = adjoint_setup(s, params, A, W))) return st;
+    std::vector<const SkyRenderConfig*> configs(job_count);
+    std::vector<const float*> suns(job_count);
+    std::vector<float*> chains(job_count);
+    std::vector<uint64_t> lens(job_count);
+    std::vector<const SkyDeviceOutputs*> outs(job_count);
+    for (uint32_t i = 0; i < job_count; ++i) {
+        configs[i] = &jobs[i].config;
+        suns[i] = jobs[i].sun_direction;
+        chains[i] = jobs[i].chain_radiance;
+        lens[i] = jobs[i].chain_radiance_len;
+        outs[i] = &jobs[i].outputs;
+    }
+    return adjoint_forward_jobs(s, A, W, configs.data(), suns.data(), chains.data(), lens.data(), outs.data(),
+                                job_count, static_cast<cudaStream_t>(cuda_stream));
+}
+
+extern "C" int sky_cuda_adjoint_backward_batch(const SkyScene* scene, const SkyAdjointJob* jobs, uint32_t job_count,
+                                               const SkyAdjointParams* params, const SkyAdjointGrads* grads,
+                                               void* cuda_stream) {
+    SkyScene* s = const_cast<SkyScene*>(scene);
+    int st = require_sampling_at_evaluation(params);
+    if (st) return st;
+    if (!jobs || job_count == 0) return set_error(SKY_ERR_INVALID_CONFIG, "jobs and job_count >= 1 are required");
+    AdjCtx A;
+    AdjWorkspace W;
+    if ((st = adjoint_setup(s, params, A, W))) return st;
+    std::vector<const SkyRenderConfig*> configs(job_count);
+    std::vector<const float*> suns(job_count);
+    std::vector<float*> chains(job_count);
+    std::vector<uint64_t> lens(job_count);
+    std::vector<const float*> dloss(job_count);
+    for (uint32_t i = 0; i < job_count; ++i) {
+        configs[i] = &jobs[i].config;
+        suns[i] = jobs[i].sun_direction;
+        chains[i] = jobs[i].chain_radiance;
+        lens[i] = jobs[i].chain_radiance_len;
+        dloss[i] = jobs[i].dloss_dfilm;
+    }
+    return adjoint_backward_jobs(s, A, W, configs.data(), suns.data(), chains.data(), lens.data(), dloss.data(),
+                                 job_count, grads, static_cast<cudaStream_t>(cuda_stream));
 }
 
 extern "C" int sky_cuda_bake_majorants(const SkyScene* scene, const SkyAdjointParams* params, float* majorants_out,

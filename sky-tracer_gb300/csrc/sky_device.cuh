@@ -471,13 +471,18 @@ __device__ __forceinline__ V3 direction_from_axis_mu(V3 axis_in, float mu_in, fl
 // sample_uniform_cone around the sun (:541-546); the sun's frame is
 // precomputed per scene, and sin(theta) uses (1-c)(1+c) to stay accurate for
 // the 0.27-degree cone.
-__device__ __forceinline__ V3 sample_sun_cone(const DevScene& S, Rng& rng) {
+// The cone around a sun frame given apart from its scene (a batch's render).
+__device__ __forceinline__ V3 sample_sun_cone(const float* sun, const float* sun_t, const float* sun_b,
+                                              float one_minus_cos_max, Rng& rng) {
     float xi = fminf(fmaxf(rng.next(), 0.0f), 0.99999994f);
-    float one_minus_cos = xi * S.one_minus_cos_max;
+    float one_minus_cos = xi * one_minus_cos_max;
     float cos_theta = 1.0f - one_minus_cos;
     float sin_theta = sqrtf(fmaxf(one_minus_cos * (2.0f - one_minus_cos), 0.0f));
     float xi_phi = rng.next();
-    return direction_from_frame(load3(S.sun), load3(S.sun_t), load3(S.sun_b), cos_theta, sin_theta, xi_phi);
+    return direction_from_frame(load3(sun), load3(sun_t), load3(sun_b), cos_theta, sin_theta, xi_phi);
+}
+__device__ __forceinline__ V3 sample_sun_cone(const DevScene& S, Rng& rng) {
+    return sample_sun_cone(S.sun, S.sun_t, S.sun_b, S.one_minus_cos_max, rng);
 }
 
 // sample_isotropic (:534-539)

@@ -131,6 +131,13 @@ class SkyAdjointGrads(ctypes.Structure):
     ]
 
 
+class SkyAdjointJob(ctypes.Structure):
+    _fields_ = [
+        ("config", SkyRenderConfig), ("sun_direction", _f * 3), ("_reserved", _f), ("outputs", SkyDeviceOutputs),
+        ("dloss_dfilm", _vp), ("chain_radiance", _vp), ("chain_radiance_len", ctypes.c_uint64),
+    ]
+
+
 class SkyComboScore(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("mean", "rmse", "p50", "p90", "p95", "p99", "max", "score")] + [
         ("finite", ctypes.c_uint64)]
@@ -187,6 +194,11 @@ _SIGNATURES = {
     "sky_cuda_adjoint_backward": (ctypes.c_int, [_vp, ctypes.POINTER(SkyRenderConfig),
                                                  ctypes.POINTER(SkyAdjointParams), ctypes.POINTER(SkyAdjointGrads),
                                                  _vp]),
+    "sky_cuda_adjoint_forward_batch": (ctypes.c_int, [_vp, ctypes.POINTER(SkyAdjointJob), ctypes.c_uint32,
+                                                      ctypes.POINTER(SkyAdjointParams), _vp]),
+    "sky_cuda_adjoint_backward_batch": (ctypes.c_int, [_vp, ctypes.POINTER(SkyAdjointJob), ctypes.c_uint32,
+                                                       ctypes.POINTER(SkyAdjointParams),
+                                                       ctypes.POINTER(SkyAdjointGrads), _vp]),
     "sky_cuda_bake_majorants": (ctypes.c_int, [_vp, ctypes.POINTER(SkyAdjointParams), _vp, _vp]),
     "sky_cuda_score_combos": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, ctypes.c_float,
                                              ctypes.POINTER(ctypes.c_uint32), _fp, ctypes.c_uint32, ctypes.c_uint32,

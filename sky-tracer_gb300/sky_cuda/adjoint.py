@@ -24,7 +24,7 @@ import ctypes
 import numpy as np
 
 from . import _abi
-from ._abi import SkyAdjointGrads, SkyAdjointParams, SkyDeviceOutputs, check
+from ._abi import SkyAdjointGrads, SkyAdjointJob, SkyAdjointParams, SkyDeviceOutputs, check
 from .render import GpuScene, RenderConfig
 from .scene import Scene
 
@@ -235,6 +235,96 @@ class AdjointRenderer:
                                                 ctypes.c_void_p(stream)), self.lib)
         return self._dchains
 
+    def _jobs(self, suns, config, dlosses=None, chains=None, outputs=None):
+        """SkyAdjointJob rows of the renders at `suns` (one each)."""
+        n = len(suns)
+        jobs = (SkyAdjointJob * n)()
+        c = config
+        for i, sun in enumerate(suns):
+            j = jobs[i]
+            j.config = c
+            j.sun_direction = (ctypes.c_float * 3)(*(sun if sun is not None else (0.0, 0.0, 0.0)))
+            if outputs is not None:
+                o = outputs[i]
+                for name, _ in SkyDeviceOutputs._fields_:
+                    setattr(j.outputs, name, _ptr(o.get(name)))
+                j.outputs.status = self._status.data_ptr()
+            if dlosses is not None:
+                j.dloss_dfilm = dlosses[i].data_ptr()
+            if chains is not None and chains[i] is not None:
+                ch = chains[i]
+                if not (ch.is_cuda and ch.is_contiguous()) or ch.numel() != self.chain_count or \
+                        str(ch.dtype) != "torch.float32":
+                    raise ValueError(f"chains must be contiguous float32 CUDA tensors of {self.chain_count} values")
+                j.chain_radiance = ch.data_ptr()
+                j.chain_radiance_len = ch.numel()
+        return jobs
+
+    def forward_batch(self, layer, band, suns, *, chains=None, check_status: bool = True, config=None) -> list:
+        """One launch (per 32 renders) of the forward at every sun of `suns`
+        (unit vectors, None = the scene's): a list of films and cell sums as
+        forward() returns them.  chains: a chain-radiance buffer per sun, or
+        None."""
+        import torch
+        cells = self.pixels * self.bands
+        outs = [{"cell_sum": torch.empty(cells, dtype=torch.float64, device="cuda"),
+                 "cell_sumsq": torch.empty(cells, dtype=torch.float64, device="cuda"),
+                 "film": torch.empty(cells, dtype=torch.float32, device="cuda")} for _ in suns]
+        jobs = self._jobs(suns, config or self._c_config, chains=chains, outputs=outs)
+        p = self._params(layer, band)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(self.lib.sky_cuda_adjoint_forward_batch(self.gs.handle, jobs, len(suns), ctypes.byref(p),
+                                                      ctypes.c_void_p(stream)), self.lib)
+        if check_status:
+            self._check_status()
+        return outs
+
+    def backward_batch(self, layer, band, dlosses, suns, *, check_status: bool = True, decorrelate: bool = False,
+                       layer_grad: bool = True, chains=None):
+        """Gradient of sum_i Loss_i over the renders at `suns` given each
+        dLoss_i/dfilm_i, in one launch per direction (per 32 renders).  With
+        decorrelate=True each render's chains come from another seed: their
+        radiance is rendered first by the forward kernel (one launch), then
+        replayed once."""
+        import torch
+        if decorrelate and chains is not None:
+            raise ValueError("a decorrelated backward traces other chains than the forward's: no chain buffer")
+        if not layer_grad and band is None:
+            raise ValueError("nothing to differentiate: layer_grad=False and no band parameters")
+        ds = [d.reshape(-1).to(torch.float32).contiguous() for d in dlosses]
+        for d in ds:
+            if d.numel() != self.pixels * self.bands:
+                raise ValueError("each dloss_dfilm must hold pixels * bands values")
+        lg = torch.zeros(self.param_count, dtype=torch.float64, device="cuda") if layer_grad else None
+        bg = torch.zeros(self.bands * BAND_PARAMS, dtype=torch.float64, device="cuda") if band is not None else None
+        c = self._c_config
+        stream = torch.cuda.current_stream().cuda_stream
+        if decorrelate:
+            c = self.config.to_c()
+            c.seed = self.config.seed ^ DECORRELATE_SEED
+            chains = self._decorrelated_chain_batch(layer, band, suns, c)
+        jobs = self._jobs(suns, c, dlosses=ds, chains=chains)
+        g = SkyAdjointGrads()
+        g.layer_grad = _ptr(lg)
+        g.band_grad = _ptr(bg)
+        g.status = self._status.data_ptr()
+        p = self._params(layer, band)
+        check(self.lib.sky_cuda_adjoint_backward_batch(self.gs.handle, jobs, len(suns), ctypes.byref(p),
+                                                       ctypes.byref(g), ctypes.c_void_p(stream)), self.lib)
+        if check_status:
+            self._check_status()
+        return lg, bg
+
+    def _decorrelated_chain_batch(self, layer, band, suns, c):
+        """Chain radiance of config `c` at every sun, from one forward launch,
+        in buffers the renderer keeps for its next backward."""
+        n = len(suns)
+        if len(getattr(self, "_dchain_batch", [])) < n:
+            self._dchain_batch = [self.new_chain_buffer() for _ in range(n)]
+        chains = self._dchain_batch[:n]
+        self.forward_batch(layer, band, suns, chains=chains, check_status=False, config=c)
+        return chains
+
     def bake_majorants(self, layer, band=None):
         """Majorant grid [B, L] of the parameterised medium (device bake)."""
         import torch
@@ -285,6 +375,56 @@ def _autograd_function():
 
 
 _FUNCTION = None
+_BATCH_FUNCTION = None
+
+
+def _batch_autograd_function():
+    import torch
+
+    class SkyBatchRenderFunction(torch.autograd.Function):
+        """films[i] = render(layer_params, band_params, sun_i) for every sun in
+        one launch; the backward runs one adjoint launch for all of them."""
+
+        @staticmethod
+        def forward(ctx, layer, band, renderer, suns, decorrelate):
+            layer_c = layer.detach().contiguous()
+            band_c = band.detach().contiguous() if band is not None else None
+            ctx.chains = None if decorrelate else [renderer.new_chain_buffer() for _ in suns]
+            outs = renderer.forward_batch(layer_c, band_c, suns, chains=ctx.chains,
+                                          check_status=renderer.check_each_call)
+            ctx.renderer = renderer
+            ctx.suns = suns
+            ctx.decorrelate = decorrelate
+            ctx.has_band = band is not None
+            ctx.save_for_backward(layer_c, band_c if band_c is not None else layer_c)
+            cfg = renderer.config
+            return torch.stack([o["film"].reshape(cfg.rows, cfg.width, renderer.bands) for o in outs])
+
+        @staticmethod
+        def backward(ctx, grad_films):
+            layer_c, band_c = ctx.saved_tensors
+            band_c = band_c if ctx.has_band else None
+            want_layer = ctx.needs_input_grad[0] or band_c is None
+            grads = [grad_films[i].contiguous() for i in range(grad_films.shape[0])]
+            lg, bg = ctx.renderer.backward_batch(layer_c, band_c, grads, ctx.suns, decorrelate=ctx.decorrelate,
+                                                 layer_grad=want_layer, check_status=ctx.renderer.check_each_call,
+                                                 chains=ctx.chains)
+            ctx.chains = None
+            gl = lg.to(layer_c.dtype).reshape(layer_c.shape) if lg is not None else None
+            gb = bg.to(band_c.dtype).reshape(band_c.shape) if bg is not None else None
+            return gl, gb, None, None, None
+
+    return SkyBatchRenderFunction
+
+
+def render_films(renderer: AdjointRenderer, layer, band=None, suns=(None,), decorrelate: bool = False):
+    """Differentiable films [len(suns), H, W, B] (float32) of the renderer's
+    config at every sun: one forward launch and, on backward, one adjoint
+    launch for all of them (per 32 suns)."""
+    global _BATCH_FUNCTION
+    if _BATCH_FUNCTION is None:
+        _BATCH_FUNCTION = _batch_autograd_function()
+    return _BATCH_FUNCTION.apply(layer, band, renderer, list(suns), decorrelate)
 
 
 def render_film(renderer: AdjointRenderer, layer, band=None, sun=None, decorrelate: bool = False):

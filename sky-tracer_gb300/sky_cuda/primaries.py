@@ -33,7 +33,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
-from .adjoint import AdjointRenderer, initial_layer_params, render_film
+from .adjoint import AdjointRenderer, initial_layer_params, render_films
 from .render import GpuScene, RenderConfig
 from .scene import SyntheticAtmosphere, load_bands, sun_from_degrees, synthetic_scene, wavelengths
 from .sweep import elevation_schedule
@@ -361,9 +361,8 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
     lam = torch.tensor(cfg.primaries_nm, dtype=torch.float64, device="cuda", requires_grad=True)
     t_setup = time.perf_counter()
     with torch.no_grad():
-        films0 = torch.stack([render_film(AdjointRenderer(gs, cfg.render_config(cfg.fit_spp, cfg.seed)), layer,
-                                          model.multipliers(lam), sun=s).reshape(-1, scene.band_count)
-                              for s in suns]).double()
+        films0 = render_films(AdjointRenderer(gs, cfg.render_config(cfg.fit_spp, cfg.seed)), layer,
+                              model.multipliers(lam), suns=suns).reshape(len(suns), -1, scene.band_count).double()
     keep = cfg.keep()
     objective = Objective(cfg, target, keep)
     matrix = _initial_matrix(films0, target, keep).clone().requires_grad_(True)
@@ -382,8 +381,8 @@ def fit_adjoint(cfg: PrimaryFitConfig, target, iterations=None, log_every: int =
         r.check_each_call = False  # the elevations' renders queue back to back; one check per step
         opt.zero_grad()
         k = model.multipliers(lam)
-        films = torch.stack([render_film(r, layer, k, sun=s, decorrelate=True).reshape(-1, scene.band_count)
-                             for s in suns])
+        # every elevation in one forward launch and one adjoint launch
+        films = render_films(r, layer, k, suns=suns, decorrelate=True).reshape(len(suns), -1, scene.band_count)
         loss = objective(films.double() @ matrix) + spacing_penalty(lam, cfg)
         loss.backward()
         r.check_status()

@@ -387,6 +387,53 @@ def test_autograd_function_matches_direct_backward(gpu, small_scene):
                                atol=1e-6 * float(bg.abs().max()))
 
 
+def test_batch_matches_separate_renders(gpu, small_scene):
+    """The batched forward and backward (one launch per direction for every
+    sun) against the single-render calls at each sun: films and cell sums
+    equal to FP64 rounding (the same chains), the gradient of the summed loss
+    to the per-warp FP32 rounding; also with chain-radiance buffers, with a
+    decorrelated backward, and through the batched autograd Function."""
+    import torch
+    from sky_cuda import sun_from_degrees
+    from sky_cuda.adjoint import render_films
+    cfg = RenderConfig(width=16, height=8, spp=32, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    B = small_scene.band_count
+    suns = [sun_from_degrees(e, 0.0, small_scene.sun_angular_radius_rad)[0] for e in (-2.0, 5.0, 30.0)]
+    rng = np.random.default_rng(11)
+    with GpuScene(small_scene) as gs:
+        r = AdjointRenderer(gs, cfg)
+        th0 = _t(initial_layer_params(small_scene, G0))
+        band0 = _t(np.ones(B * BAND_PARAMS, dtype=np.float32))
+        single = [r.forward(th0, band0, sun=s) for s in suns]
+        batch = r.forward_batch(th0, band0, suns)
+        for a, b in zip(single, batch):
+            np.testing.assert_allclose(b["cell_sum"].cpu().numpy(), a["cell_sum"].cpu().numpy(), rtol=1e-12, atol=0)
+            np.testing.assert_allclose(b["film"].cpu().numpy(), a["film"].cpu().numpy(), rtol=1e-6, atol=0)
+        ds = [_t(rng.normal(size=cfg.pixels * B).astype(np.float32)) for _ in suns]
+        lg_b, bg_b = r.backward_batch(th0, band0, ds, suns)
+        parts = [r.backward(th0, band0, d, sun=s) for d, s in zip(ds, suns)]
+        lg_s = sum(p_[0] for p_ in parts)
+        bg_s = sum(p_[1] for p_ in parts)
+        chains = [r.new_chain_buffer() for _ in suns]
+        r.forward_batch(th0, band0, suns, chains=chains)
+        lg_c, bg_c = r.backward_batch(th0, band0, ds, suns, chains=chains)
+        lg_d, _ = r.backward_batch(th0, band0, ds, suns, decorrelate=True)
+        lg_ds = sum(r.backward(th0, band0, d, sun=s, decorrelate=True)[0] for d, s in zip(ds, suns))
+        # the batched autograd Function: films stacked, gradient of their summed loss
+        layer = th0.clone().requires_grad_(True)
+        films = render_films(r, layer, band0, suns=suns)
+        assert films.shape == (len(suns), cfg.height, cfg.width, B)
+        np.testing.assert_allclose(films[1].reshape(-1).detach().cpu().numpy(),
+                                   single[1]["film"].cpu().numpy(), rtol=1e-6, atol=0)
+        (films.reshape(len(suns), -1) * torch.stack(ds)).sum().backward()
+    for a, b in ((lg_b, lg_s), (bg_b, bg_s), (lg_c, lg_s), (bg_c, bg_s), (lg_d, lg_ds),
+                 (layer.grad.double(), lg_s)):
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        assert np.any(b != 0.0)
+        np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
+
+
 def test_adjoint_errors(gpu, ref_scene, dome_scene):
     import ctypes
     import torch
