@@ -188,6 +188,19 @@ pub struct SkyAdjointGrads {
     pub status: *mut u32,
 }
 
+/// One render of a differentiable batch (SkyAdjointJob).
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct SkyAdjointJob {
+    pub config: SkyRenderConfig,
+    pub sun_direction: [f32; 3],
+    pub _reserved: f32,
+    pub outputs: SkyDeviceOutputs,
+    pub dloss_dfilm: *const f32,
+    pub chain_radiance: *mut f32,
+    pub chain_radiance_len: u64,
+}
+
 /// Opaque scene handle (device tables owned by the library).
 #[repr(C)]
 pub struct SkyScene {
@@ -212,6 +225,11 @@ unsafe extern "C" {
     pub fn sky_cuda_adjoint_backward(scene: *const SkyScene, config: *const SkyRenderConfig,
                                      params: *const SkyAdjointParams, grads: *const SkyAdjointGrads,
                                      cuda_stream: *mut c_void) -> c_int;
+    pub fn sky_cuda_adjoint_forward_batch(scene: *const SkyScene, jobs: *const SkyAdjointJob, job_count: u32,
+                                          params: *const SkyAdjointParams, cuda_stream: *mut c_void) -> c_int;
+    pub fn sky_cuda_adjoint_backward_batch(scene: *const SkyScene, jobs: *const SkyAdjointJob, job_count: u32,
+                                           params: *const SkyAdjointParams, grads: *const SkyAdjointGrads,
+                                           cuda_stream: *mut c_void) -> c_int;
 }
 
 #[cfg(test)]
@@ -232,5 +250,6 @@ mod layout {
         assert_eq!(size_of::<SkyDeviceOutputs>(), 64);
         assert_eq!(size_of::<SkyAdjointParams>(), 64);
         assert_eq!(size_of::<SkyAdjointGrads>(), 40);
+        assert_eq!(size_of::<SkyAdjointJob>(), 184);
     }
 }

@@ -274,6 +274,11 @@ impl<'a> Adjoint<'a> {
         Self { scene, config: c }
     }
 
+    /// The render config (the starting point of a batch's `SkyAdjointJob`s).
+    pub fn config(&self) -> ffi::SkyRenderConfig {
+        self.config
+    }
+
     pub fn config_mut(&mut self) -> &mut ffi::SkyRenderConfig {
         &mut self.config
     }
@@ -294,6 +299,43 @@ impl<'a> Adjoint<'a> {
                           stream: *mut c_void) -> Result<(), RenderError> {
         let p = params.ffi();
         let status = unsafe { ffi::sky_cuda_adjoint_forward(self.scene.handle, &self.config, &p, outputs, stream) };
+        if status != ffi::SKY_OK {
+            return Err(render_error(status, last_error()));
+        }
+        Ok(())
+    }
+
+    /// Forward renders of this config at several suns and views in one launch
+    /// per 32 renders (`jobs[i].config`, `.sun_direction`, `.outputs`,
+    /// `.chain_radiance`; `params.chain_radiance` is not read).
+    ///
+    /// # Safety
+    /// As for `forward`, for every job.
+    pub unsafe fn forward_batch(&self, params: &AdjointParams, jobs: &[ffi::SkyAdjointJob],
+                                stream: *mut c_void) -> Result<(), RenderError> {
+        let p = params.ffi();
+        let status = unsafe {
+            ffi::sky_cuda_adjoint_forward_batch(self.scene.handle, jobs.as_ptr(), jobs.len() as u32, &p, stream)
+        };
+        if status != ffi::SKY_OK {
+            return Err(render_error(status, last_error()));
+        }
+        Ok(())
+    }
+
+    /// The gradient of the summed loss of a batch (`jobs[i].dloss_dfilm`),
+    /// added to `grads.layer_grad` / `grads.band_grad` in one launch per 32
+    /// renders.
+    ///
+    /// # Safety
+    /// As for `backward`, for every job.
+    pub unsafe fn backward_batch(&self, params: &AdjointParams, jobs: &[ffi::SkyAdjointJob],
+                                 grads: &ffi::SkyAdjointGrads, stream: *mut c_void) -> Result<(), RenderError> {
+        let p = params.ffi();
+        let status = unsafe {
+            ffi::sky_cuda_adjoint_backward_batch(self.scene.handle, jobs.as_ptr(), jobs.len() as u32, &p, grads,
+                                                 stream)
+        };
         if status != ffi::SKY_OK {
             return Err(render_error(status, last_error()));
         }
