@@ -1028,10 +1028,9 @@ int adjoint_forward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const Sk
                 return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
             if (configs[i]->phase_sampling != configs[0]->phase_sampling)
                 return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
-            const bool acc_i = (configs[i]->flags & SKY_FLAG_ACCUMULATE) != 0;
-            if (i > i0 && acc_i != accumulate)
+            accumulate = (configs[i]->flags & SKY_FLAG_ACCUMULATE) != 0;
+            if (accumulate != ((configs[0]->flags & SKY_FLAG_ACCUMULATE) != 0))
                 return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch accumulate, or none");
-            accumulate = acc_i;
             job.cell_sum = outputs[i]->cell_sum;
             job.cell_sumsq = outputs[i]->cell_sumsq;
             if ((st = adjoint_place(J, job))) return st;
