@@ -464,3 +464,30 @@ def test_adjoint_errors(gpu, ref_scene, dome_scene):
         assert lib.sky_cuda_adjoint_backward(gs.handle, ctypes.byref(r._c_config), ctypes.byref(p),
                                              ctypes.byref(g), None) == _abi.SKY_ERR_INVALID_CONFIG
         assert lib.sky_cuda_adjoint_param_count(gs.handle) == 3 * dome_scene.layer_count + 2
+        # batches: one parameter set, one tracking mode, phase sampling and accumulate flag
+        assert lib.sky_cuda_adjoint_forward_batch(gs.handle, None, 0, ctypes.byref(p),
+                                                  None) == _abi.SKY_ERR_INVALID_CONFIG
+        p.sample_layer_params = None
+        jobs = (_abi.SkyAdjointJob * 2)()
+        for j in jobs:
+            j.config = RenderConfig(width=4, height=4, spp=1, tracking=_abi.TRACKING_MERGED_LAYERS).to_c()
+            j.outputs.cell_sum, j.outputs.status = s.data_ptr(), st.data_ptr()
+            j.dloss_dfilm = d.data_ptr()
+        jobs[1].config.tracking = _abi.TRACKING_RESIDUAL_CARRY
+        assert lib.sky_cuda_adjoint_forward_batch(gs.handle, jobs, 2, ctypes.byref(p),
+                                                  None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert "same tracking" in _abi.last_error(lib)
+        jobs[1].config.tracking = _abi.TRACKING_MERGED_LAYERS
+        jobs[1].config.phase_sampling = _abi.PHASE_TABULATED
+        assert lib.sky_cuda_adjoint_backward_batch(gs.handle, jobs, 2, ctypes.byref(p), ctypes.byref(g),
+                                                   None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert "phase sampling" in _abi.last_error(lib)
+        jobs[1].config.phase_sampling = _abi.PHASE_ISOTROPIC
+        jobs[1].config.flags = _abi.FLAG_ACCUMULATE
+        assert lib.sky_cuda_adjoint_forward_batch(gs.handle, jobs, 2, ctypes.byref(p),
+                                                  None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert "accumulate" in _abi.last_error(lib)
+        jobs[1].config.flags = 0
+        assert lib.sky_cuda_adjoint_forward_batch(gs.handle, jobs, 2, ctypes.byref(p), None) == _abi.SKY_OK
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
