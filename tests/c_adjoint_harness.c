@@ -12,9 +12,14 @@
  * tabulated phase sampling (Adjoint::new), it runs the forward with a
  * chain-radiance buffer, then the backward that reads it, and writes
  * OUT_PREFIX.film (float32), OUT_PREFIX.layer_grad and OUT_PREFIX.band_grad
- * (float64).  It also checks the refusals the crate maps to
+ * (float64).  Then Adjoint::forward_batch / backward_batch over two renders,
+ * one at the scene's sun (a zero direction) and one at the sun direction
+ * (0, 0.5, 0.8660254), each with its own chain-radiance buffer and the same
+ * dLoss/dfilm: OUT_PREFIX.batch_film0, .batch_film1 (float32),
+ * .batch_layer_grad and .batch_band_grad (float64, the gradient of the summed
+ * loss).  It also checks the refusals the crate maps to
  * RenderError::InvalidConfig (segment-restart tracking, a chain buffer shorter
- * than the render's chains, a missing status).
+ * than the render's chains, a missing status, an empty batch).
  * Exit status 0 on success, 2 without a CUDA device.
  */
 #include <stdint.h>
@@ -218,6 +223,52 @@ int main(int argc, char** argv) {
     write_file(argv[8], "film", film, cells * sizeof(float));
     write_file(argv[8], "layer_grad", layer_grad, np * sizeof(double));
     write_file(argv[8], "band_grad", band_grad, (size_t)B * SKY_ADJOINT_BAND_PARAMS * sizeof(double));
+
+    /* Adjoint::forward_batch, Adjoint::backward_batch: two renders, one launch
+       per direction; the parameter set's own chain buffer is not read */
+    static const float batch_sun[2][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.5f, 0.8660254f}};
+    SkyAdjointJob jobs[2];
+    memset(jobs, 0, sizeof(jobs));
+    void* batch_buffers[2][4];
+    for (int i = 0; i < 2; ++i) {
+        SkyAdjointJob* j = &jobs[i];
+        j->config = c;
+        memcpy(j->sun_direction, batch_sun[i], sizeof(batch_sun[i]));
+        batch_buffers[i][0] = j->outputs.cell_sum = device(cells * sizeof(double));
+        batch_buffers[i][1] = j->outputs.cell_sumsq = device(cells * sizeof(double));
+        batch_buffers[i][2] = j->outputs.film = device(cells * sizeof(float));
+        batch_buffers[i][3] = j->chain_radiance = device(cells * c.spp * sizeof(float));
+        j->outputs.status = status;
+        j->chain_radiance_len = cells * c.spp;
+        j->dloss_dfilm = dloss;
+    }
+    double* batch_layer_grad = device(np * sizeof(double));
+    double* batch_band_grad = device((size_t)B * SKY_ADJOINT_BAND_PARAMS * sizeof(double));
+    SkyAdjointGrads bg = g;
+    bg.dloss_dfilm = NULL;
+    bg.layer_grad = batch_layer_grad;
+    bg.band_grad = batch_band_grad;
+    if ((st = sky_cuda_adjoint_forward_batch(scene, jobs, 2, &p, NULL)) != SKY_OK)
+        return fail("adjoint forward batch", st);
+    if ((st = sky_cuda_adjoint_backward_batch(scene, jobs, 2, &p, &bg, NULL)) != SKY_OK)
+        return fail("adjoint backward batch", st);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(&watchdog, status, sizeof(watchdog), cudaMemcpyDeviceToHost) != cudaSuccess || watchdog != 0) {
+        fprintf(stderr, "the batch failed or tripped the watchdog (%u)\n", watchdog);
+        return 1;
+    }
+    if ((st = sky_cuda_adjoint_forward_batch(scene, jobs, 0, &p, NULL)) != SKY_ERR_INVALID_CONFIG) {
+        fprintf(stderr, "an empty batch returned %d\n", st);
+        return 1;
+    }
+    write_file(argv[8], "batch_film0", jobs[0].outputs.film, cells * sizeof(float));
+    write_file(argv[8], "batch_film1", jobs[1].outputs.film, cells * sizeof(float));
+    write_file(argv[8], "batch_layer_grad", batch_layer_grad, np * sizeof(double));
+    write_file(argv[8], "batch_band_grad", batch_band_grad, (size_t)B * SKY_ADJOINT_BAND_PARAMS * sizeof(double));
+    for (int i = 0; i < 2; ++i)
+        for (int k = 0; k < 4; ++k) cudaFree(batch_buffers[i][k]);
+    cudaFree(batch_layer_grad);
+    cudaFree(batch_band_grad);
     cudaFree(layer);
     cudaFree(band);
     cudaFree(dloss);

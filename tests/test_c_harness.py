@@ -111,10 +111,10 @@ def test_adjoint_harness_compiles_and_links_against_the_library(lib_built, tmp_p
 
 @pytest.mark.gpu
 def test_adjoint_harness_matches_the_python_renderer(gpu, dome_scene, tmp_path):
-    """The crate's Adjoint forward/backward from C against AdjointRenderer on
-    the same scene, parameters, config and dLoss/dfilm: the film to the order
-    of the FP64 cell sums, the gradients to the rounding of the per-warp FP32
-    gradient sums."""
+    """The crate's Adjoint forward/backward and forward_batch/backward_batch
+    from C against AdjointRenderer on the same scene, parameters, config and
+    dLoss/dfilm: the films to the order of the FP64 cell sums, the gradients
+    to the rounding of the per-warp FP32 gradient sums."""
     import torch
 
     from sky_cuda import GpuScene, _abi
@@ -137,6 +137,10 @@ def test_adjoint_harness_matches_the_python_renderer(gpu, dome_scene, tmp_path):
     film_c = np.fromfile(str(prefix) + ".film", dtype=np.float32)
     lg_c = np.fromfile(str(prefix) + ".layer_grad", dtype=np.float64)
     bg_c = np.fromfile(str(prefix) + ".band_grad", dtype=np.float64)
+    batch_films = [np.fromfile(str(prefix) + f".batch_film{i}", dtype=np.float32) for i in range(2)]
+    batch_lg = np.fromfile(str(prefix) + ".batch_layer_grad", dtype=np.float64)
+    batch_bg = np.fromfile(str(prefix) + ".batch_band_grad", dtype=np.float64)
+    high_sun = (0.0, 0.5, 0.8660254)  # the harness's second render
 
     cfg = RenderConfig(width=w, height=h, spp=spp, seed=seed, observer_altitude_km=0.2,
                        phase_sampling=_abi.PHASE_TABULATED, tracking=_abi.TRACKING_MERGED_LAYERS)
@@ -146,9 +150,17 @@ def test_adjoint_harness_matches_the_python_renderer(gpu, dome_scene, tmp_path):
         band = torch.ones(dome_scene.band_count * BAND_PARAMS, dtype=torch.float32, device="cuda")
         chains = r.new_chain_buffer()
         film_py = r.forward(th, band, chains=chains)["film"].cpu().numpy()
-        lg, bg = r.backward(th, band, torch.as_tensor(dloss, device="cuda"), chains=chains)
+        d = torch.as_tensor(dloss, device="cuda")
+        lg, bg = r.backward(th, band, d, chains=chains)
+        film_high = r.forward(th, band, sun=high_sun)["film"].cpu().numpy()
+        lg_high, bg_high = r.backward(th, band, d, sun=high_sun)
     np.testing.assert_allclose(film_c, film_py, rtol=1e-6, atol=0)
-    for a, b in ((lg_c, lg.cpu().numpy()), (bg_c, bg.cpu().numpy())):
+    np.testing.assert_allclose(batch_films[0], film_py, rtol=1e-6, atol=0)
+    np.testing.assert_allclose(batch_films[1], film_high, rtol=1e-6, atol=0)
+    assert not np.array_equal(batch_films[0], batch_films[1])
+    lg, bg = lg.cpu().numpy(), bg.cpu().numpy()
+    for a, b in ((lg_c, lg), (bg_c, bg), (batch_lg, lg + lg_high.cpu().numpy()),
+                 (batch_bg, bg + bg_high.cpu().numpy())):
         assert a.shape == b.shape and np.any(b != 0.0)
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
 

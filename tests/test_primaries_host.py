@@ -66,7 +66,7 @@ def test_spacing_penalty_pushes_close_primaries_apart():
     # two pairs 1 nm apart (what the unconstrained fit converged to): each pair costs (9/10)^2
     lam = torch.tensor([479.0, 480.0, 579.0, 580.0], dtype=torch.float64, requires_grad=True)
     pen = spacing_penalty(lam, cfg)
-    assert float(pen) == pytest.approx(cfg.spacing_weight * 2 * 0.81)
+    assert pen.item() == pytest.approx(cfg.spacing_weight * 2 * 0.81)
     pen.backward()
     g = lam.grad.numpy()
     # descending the penalty separates each pair
