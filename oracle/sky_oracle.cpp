@@ -1,7 +1,7 @@
 // sky_oracle.cpp — CPU ORACLE for the spectral sky path tracer.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the correctness checker and the
-// timed CPU baseline; the product (libsky_cuda.so) never links, loads or
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle the tests compare with and
+// the timed CPU baseline; the product (libsky_cuda.so) never links, loads or
 // calls it.  Only tests/, __graft_entry__.smoke() and bench.py's CPU legs may
 // use it.
 //
@@ -982,7 +982,7 @@ float cpu_extinction_total(const CpuCoeffs& k) {
 
 }  // namespace
 
-// ============================ exported checker API ==========================
+// ============================ exported oracle API ===========================
 
 extern "C" {
 

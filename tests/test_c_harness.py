@@ -1,8 +1,8 @@
 """The sky-cuda Rust crate's calls, made from C (tests/c_abi_harness.c and,
 for its differentiable-render pair, tests/c_adjoint_harness.c).
 
-No Rust toolchain exists on these machines (cargo and rustc are absent here
-and on the GPU machine), so the crate's FFI sequence is exercised by a C program
+No Rust toolchain is installed (cargo and rustc are absent on the x86 build
+host and on the aarch64 GPU host), so the crate's FFI sequence is exercised by a C program
 that makes the same calls with the same structs: sky_cuda_render_desc (the
 crate's `render`), sky_cuda_scene_create / sky_cuda_render /
 sky_cuda_scene_destroy (its `GpuScene`), and the error path through
