@@ -1004,7 +1004,8 @@ namespace {
 
 // The primal launches of renders `jobs` (n of them, outputs[i] each) over one
 // parameter set, in launches of at most kAdjMaxJobs renders, then each
-// render's finalize.  The context's tables are baked first, once.
+// render's finalize.  Every render is checked before the first launch (a
+// refused batch writes nothing); the context's tables are baked first, once.
 int adjoint_forward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const SkyRenderConfig* const* configs,
                          const float* const* suns, float* const* chains, const uint64_t* chain_lens,
                          const SkyDeviceOutputs* const* outputs, uint32_t n, cudaStream_t stream) {
@@ -1012,53 +1013,45 @@ int adjoint_forward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const Sk
     if (!outputs[0]->status) return set_error(SKY_ERR_INVALID_CONFIG, "outputs.status is required");
     if (A.distinct && n > 1)
         return set_error(SKY_ERR_INVALID_CONFIG, "a batch is rendered at its sampling parameters: no sample_*");
-    AdjJobs J;
-    std::memset(&J, 0, sizeof(J));
+    const bool accumulate = (configs[0]->flags & SKY_FLAG_ACCUMULATE) != 0;
+    std::vector<AdjJobs> launches((n + kAdjMaxJobs - 1u) / kAdjMaxJobs);
+    std::memset(launches.data(), 0, launches.size() * sizeof(AdjJobs));
     int st;
-    bool prepared = false;
-    for (uint32_t i0 = 0; i0 < n; i0 += kAdjMaxJobs) {
-        J.count = 0;
-        J.cells = 0;
-        const uint32_t i1 = std::min(n, i0 + kAdjMaxJobs);
-        bool accumulate = false;
-        for (uint32_t i = i0; i < i1; ++i) {
-            AdjJob job;
-            if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
-            if (!outputs[i] || !outputs[i]->cell_sum)
-                return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
-            if (configs[i]->phase_sampling != configs[0]->phase_sampling)
-                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
-            accumulate = (configs[i]->flags & SKY_FLAG_ACCUMULATE) != 0;
-            if (accumulate != ((configs[0]->flags & SKY_FLAG_ACCUMULATE) != 0))
-                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch accumulate, or none");
-            job.cell_sum = outputs[i]->cell_sum;
-            job.cell_sumsq = outputs[i]->cell_sumsq;
-            if ((st = adjoint_place(J, job))) return st;
-        }
-        clear_stale_error();
-        cudaError_t e;
-        if (!prepared) {
-            if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
-                return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
-            prepared = true;
-        }
+    for (uint32_t i = 0; i < n; ++i) {
+        AdjJob job;
+        if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
+        if (!outputs[i] || !outputs[i]->cell_sum)
+            return set_error(SKY_ERR_INVALID_CONFIG, "outputs.cell_sum is required");
+        if (configs[i]->phase_sampling != configs[0]->phase_sampling)
+            return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
+        if (((configs[i]->flags & SKY_FLAG_ACCUMULATE) != 0) != accumulate)
+            return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch accumulate, or none");
+        job.cell_sum = outputs[i]->cell_sum;
+        job.cell_sumsq = outputs[i]->cell_sumsq;
+        if ((st = adjoint_place(launches[i / kAdjMaxJobs], job))) return st;
+    }
+    clear_stale_error();
+    cudaError_t e;
+    if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
+        return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+    for (const AdjJobs& J : launches) {
         e = launch_adjoint_primal(A, J, accumulate, outputs[0]->counters, outputs[0]->status, W.next_cell, stream);
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "differentiable render launch", e);
-        for (uint32_t i = i0; i < i1; ++i) {
-            const SkyRenderConfig* c = configs[i];
-            const uint32_t total_spp =
-                (c->flags & SKY_FLAG_ACCUMULATE) != 0 ? c->sample_offset + c->spp : c->spp;
-            const SkyDeviceOutputs* o = outputs[i];
-            e = launch_finalize(A.S, slab_pixels(c), total_spp, o->cell_sum, o->cell_sumsq, o->film,
-                                s->has_xyz ? o->xyz : nullptr, s->has_xyz ? o->xyz_var : nullptr,
-                                s->has_xyz ? o->rgb : nullptr, stream);
-            if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
-        }
+    }
+    for (uint32_t i = 0; i < n; ++i) {
+        const SkyRenderConfig* c = configs[i];
+        const uint32_t total_spp = accumulate ? c->sample_offset + c->spp : c->spp;
+        const SkyDeviceOutputs* o = outputs[i];
+        e = launch_finalize(A.S, slab_pixels(c), total_spp, o->cell_sum, o->cell_sumsq, o->film,
+                            s->has_xyz ? o->xyz : nullptr, s->has_xyz ? o->xyz_var : nullptr,
+                            s->has_xyz ? o->rgb : nullptr, stream);
+        if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "finalize kernel launch", e);
     }
     return SKY_OK;
 }
 
-// The gradient launches of renders over one parameter set (dloss[i] each).
+// The gradient launches of renders over one parameter set (dloss[i] each),
+// every render checked before the first launch.
 int adjoint_backward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const SkyRenderConfig* const* configs,
                           const float* const* suns, float* const* chains, const uint64_t* chain_lens,
                           const float* const* dloss, uint32_t n, const SkyAdjointGrads* grads,
@@ -1067,30 +1060,23 @@ int adjoint_backward_jobs(SkyScene* s, AdjCtx& A, const AdjWorkspace& W, const S
     if (!grads || (!grads->layer_grad && !grads->band_grad))
         return set_error(SKY_ERR_INVALID_CONFIG, "at least one of grads.layer_grad, grads.band_grad is required");
     if (!grads->status) return set_error(SKY_ERR_INVALID_CONFIG, "grads.status is required");
-    AdjJobs J;
-    std::memset(&J, 0, sizeof(J));
+    std::vector<AdjJobs> launches((n + kAdjMaxJobs - 1u) / kAdjMaxJobs);
+    std::memset(launches.data(), 0, launches.size() * sizeof(AdjJobs));
     int st;
-    bool prepared = false;
-    for (uint32_t i0 = 0; i0 < n; i0 += kAdjMaxJobs) {
-        J.count = 0;
-        J.cells = 0;
-        const uint32_t i1 = std::min(n, i0 + kAdjMaxJobs);
-        for (uint32_t i = i0; i < i1; ++i) {
-            AdjJob job;
-            if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
-            if (!dloss[i]) return set_error(SKY_ERR_INVALID_CONFIG, "dloss_dfilm is required for every render");
-            if (configs[i]->phase_sampling != configs[0]->phase_sampling)
-                return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
-            job.dloss = dloss[i];
-            if ((st = adjoint_place(J, job))) return st;
-        }
-        clear_stale_error();
-        cudaError_t e;
-        if (!prepared) {
-            if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
-                return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
-            prepared = true;
-        }
+    for (uint32_t i = 0; i < n; ++i) {
+        AdjJob job;
+        if ((st = adjoint_job(s, configs[i], suns[i], chains[i], chain_lens[i], i == 0, A, job))) return st;
+        if (!dloss[i]) return set_error(SKY_ERR_INVALID_CONFIG, "dloss_dfilm is required for every render");
+        if (configs[i]->phase_sampling != configs[0]->phase_sampling)
+            return set_error(SKY_ERR_INVALID_CONFIG, "all renders of a batch need the same phase sampling");
+        job.dloss = dloss[i];
+        if ((st = adjoint_place(launches[i / kAdjMaxJobs], job))) return st;
+    }
+    clear_stale_error();
+    cudaError_t e;
+    if ((e = launch_adjoint_prepare(A, W, stream)) != cudaSuccess)
+        return cuda_fail(SKY_ERR_LAUNCH, "majorant bake launch", e);
+    for (const AdjJobs& J : launches) {
         e = launch_adjoint_grad(A, J, grads->layer_grad, grads->band_grad, grads->counters, grads->status, W.next_cell,
                                 stream);
         if (e != cudaSuccess) return cuda_fail(SKY_ERR_LAUNCH, "adjoint launch", e);

@@ -434,6 +434,48 @@ def test_batch_matches_separate_renders(gpu, small_scene):
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
 
 
+def test_batch_beyond_one_launch(gpu, small_scene):
+    """33 renders take two launches per direction (32 + 1): each film equals
+    its single render, the gradient of the summed loss equals the sum of the
+    single gradients; a 33-render batch whose last render is refused returns
+    SKY_ERR_INVALID_CONFIG before any launch, so no render's outputs change."""
+    import ctypes
+    import torch
+    from sky_cuda import sun_from_degrees
+    cfg = RenderConfig(width=4, height=4, spp=4, phase_sampling=_abi.PHASE_TABULATED,
+                       tracking=_abi.TRACKING_MERGED_LAYERS)
+    B = small_scene.band_count
+    suns = [sun_from_degrees(e, 10.0 * e, small_scene.sun_angular_radius_rad)[0]
+            for e in np.linspace(-3.0, 60.0, 33)]
+    rng = np.random.default_rng(3)
+    with GpuScene(small_scene) as gs:
+        r = AdjointRenderer(gs, cfg)
+        th = _t(initial_layer_params(small_scene, G0))
+        band = _t(np.ones(B * BAND_PARAMS, dtype=np.float32))
+        batch = r.forward_batch(th, band, suns)
+        for i in (0, 31, 32):
+            single = r.forward(th, band, sun=suns[i])
+            np.testing.assert_allclose(batch[i]["cell_sum"].cpu().numpy(), single["cell_sum"].cpu().numpy(),
+                                       rtol=1e-12, atol=0)
+        ds = [_t(rng.normal(size=cfg.pixels * B).astype(np.float32)) for _ in suns]
+        lg_b, _ = r.backward_batch(th, band, ds, suns)
+        lg_s = sum(r.backward(th, band, d, sun=sn)[0] for d, sn in zip(ds, suns))
+        # the refused batch: every render's cell sums hold a sentinel before and after
+        outs = [{"cell_sum": torch.full((cfg.pixels * B,), -7.0, dtype=torch.float64, device="cuda")}
+                for _ in suns]
+        jobs = r._jobs(suns, r._c_config, outputs=outs)
+        jobs[32].config.tracking = _abi.TRACKING_RESIDUAL_CARRY
+        p = r._params(th, band)
+        assert gs.lib.sky_cuda_adjoint_forward_batch(gs.handle, jobs, len(suns), ctypes.byref(p),
+                                                     None) == _abi.SKY_ERR_INVALID_CONFIG
+        assert "same tracking" in _abi.last_error(gs.lib)
+        torch.cuda.synchronize()
+        assert all(bool((o["cell_sum"] == -7.0).all()) for o in outs)
+    a, b = lg_b.cpu().numpy(), lg_s.cpu().numpy()
+    assert np.any(b != 0.0)
+    np.testing.assert_allclose(a, b, rtol=0, atol=1e-4 * np.abs(b).max())
+
+
 def test_adjoint_errors(gpu, ref_scene, dome_scene):
     import ctypes
     import torch
