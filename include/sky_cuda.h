@@ -536,8 +536,9 @@ typedef struct SkyAdjointJob {
  * params.chain_radiance is not read) in one launch of the differentiable
  * renderer per 32 renders, instead of one launch each: an elevation sweep of
  * a fit renders all its suns in one launch per direction.  Every render needs
- * the same tracking mode, phase sampling and accumulate flag.  The backward
- * ADDS the gradient of sum_i Loss_i to grads->layer_grad / band_grad
+ * the same tracking mode, phase sampling and accumulate flag.  Every render
+ * is checked before the first launch: a refused batch launches nothing.  The
+ * backward ADDS the gradient of sum_i Loss_i to grads->layer_grad / band_grad
  * (grads->dloss_dfilm is not read: each job carries its own).  Asynchronous on
  * `cuda_stream`.  No counterpart in the reference.
  */
